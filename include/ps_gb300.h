@@ -1,0 +1,178 @@
+/* ps_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * PLUTO-sirocco per-step hydro path.
+ *
+ * Plain C types only (ints, doubles, pointers and sizes).  A PLUTO build
+ * binds these entry points from its own C host code in place of the
+ * functions named beside each declaration (paths inside the reference
+ * project); the array arguments are the very arrays PLUTO allocates:
+ *   Vc        Data.Vc, primitive variables [nv][k][j][i] over the total box
+ *             (ghost zones included), one contiguous block as made by
+ *             ARRAY_4D (Src/structs.h:526, Src/arrays.c:250-300)
+ *   x/xl/xr/dx Grid.x / Grid.xl / Grid.xr / Grid.dx per direction over the
+ *             total box (Src/structs.h:133-187)
+ *
+ * Return convention: 0 on success; a negative PS_E* code for a host-side
+ * error (see ps_last_error()); a positive value is the OR of PS_F* flags
+ * raised by the device during the call.
+ */
+#ifndef PS_GB300_H
+#define PS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* geometry, limiter, solver and boundary codes (Src/pluto.h:163-171) */
+#define PS_CARTESIAN      0
+#define PS_SPHERICAL      3
+#define PS_LIM_MC         0
+#define PS_LIM_VL         1
+#define PS_LIM_MM         2
+#define PS_HLLC           0
+#define PS_HLL            1
+#define PS_BC_OUTFLOW     1
+#define PS_BC_REFLECTIVE  2
+#define PS_BC_AXISYM      3
+#define PS_BC_EQTSYM      4
+#define PS_BC_PERIODIC    5
+#define PS_BC_USERDEF     8
+#define PS_GRID_UNIFORM   0
+#define PS_GRID_LOG_INC   1
+#define PS_GRID_RATIO     2
+
+/* host-side error codes */
+#define PS_EINVAL   (-1)
+#define PS_ECUDA    (-2)
+#define PS_ENOMEM   (-3)
+#define PS_ESTATE   (-4)
+
+/* device flags (positive return values) */
+#define PS_F_NAN          0x01  /* NaN in the state (Src/debug_tools.c:13-38)   */
+#define PS_F_CONS2PRIM    0x02  /* FLAG_CONS2PRIM_FAIL (Src/HD/mappers.c:139-200) */
+#define PS_F_NEG_DENSITY  0x04  /* FLAG_NEGATIVE_DENSITY                          */
+#define PS_F_DT_SMALL     0x08  /* dt too small (Src/main.c:672-683)              */
+#define PS_F_TMA_TIMEOUT  0x10  /* a bounded wait on a tile copy ran out          */
+
+typedef struct ps_config {
+  int    dims;         /* DIMENSIONS: 2 or 3                                  */
+  int    nx[3];        /* active cells per direction (1 when inactive)        */
+  int    nvar;         /* NVAR: 5 (rho, vx1, vx2, vx3, prs) + passive scalars */
+  int    geometry;     /* GEOMETRY: PS_CARTESIAN                              */
+  int    limiter;      /* LIMITER: PS_LIM_*                                   */
+  int    solver;       /* [Solver] Solver: PS_HLLC / PS_HLL                   */
+  int    bc[6];        /* [Boundary] X1-beg, X1-end, X2-beg, ... : PS_BC_*    */
+  double gamma;        /* g_gamma                                             */
+  double cfl;          /* [Time] CFL                                          */
+  double cfl_max_var;  /* [Time] CFL_max_var                                  */
+  double tstop;        /* [Time] tstop                                        */
+  double first_dt;     /* [Time] first_dt                                     */
+  int    cooling;      /* COOLING != NO: dt is recomputed after odd steps only */
+  int    reserved;
+} ps_config;
+
+typedef struct ps_ctx ps_ctx;
+
+const char *ps_last_error(void);
+
+/* ---------------------------------------------------------------- */
+/* host helpers (no device needed)                                   */
+/* ---------------------------------------------------------------- */
+
+/* One direction of the grid over the total box: n active cells between
+ * xbeg and xend plus ngh ghost cells on each side, as SetGrid builds it
+ * (Src/set_grid.c:100-140 for ghosts and centres, 405-450 for the
+ * uniform, logarithmic "l+" and ratio "r" patches).  Arrays hold n+2*ngh
+ * entries. */
+int ps_grid_build(int type, int n, int ngh, double xbeg, double xend,
+                  double ratio, double *x, double *xl, double *xr, double *dx);
+
+/* Blast-wave initial condition used by the 2-D/3-D Cartesian tests and
+ * benchmark: rho = 1*(1 + U(-noise, noise)) from PLUTO's PRNG_MT sequence
+ * (RandomSeed(seed, 0) / RandomNumber, Src/Math_Tools/math_random.c:36-183)
+ * drawn over the active cells in (k, j, i) order; v = 0; p = p_in where
+ * the distance from the box centre (0.5, 0.5[, 0.5]) is below r_in,
+ * p_amb elsewhere.  Ghost cells are set to the ambient state.  x1..x3 are
+ * the cell-centre arrays of the total box; Vc is [nv][k][j][i]. */
+int ps_init_blast(const ps_config *cfg, const double *x1, const double *x2,
+                  const double *x3, double p_amb, double p_in, double r_in,
+                  double noise, long seed, double *Vc);
+
+/* ---------------------------------------------------------------- */
+/* device context                                                    */
+/* ---------------------------------------------------------------- */
+
+/* Allocates the device mirrors of Data.Vc and the stage scratch for one
+ * grid on the current CUDA device (the device-side counterpart of
+ * Initialize(), Src/initialize.c, and of the static scratch of
+ * AdvanceStep/UpdateStage, Src/Time_Stepping/rk_step.c:78-101,
+ * update_stage.c:85-95). */
+int ps_create(const ps_config *cfg, ps_ctx **out);
+int ps_destroy(ps_ctx *ctx);
+
+/* Copies one direction of Grid (x, xl, xr, dx over the total box) to the
+ * device; replaces the device side of SetGrid/SetGeometry. */
+int ps_set_grid(ps_ctx *ctx, int dir, const double *x, const double *xl,
+                const double *xr, const double *dx);
+
+/* Host Data.Vc -> device (after Startup / restart / InitDomain), and
+ * device -> host Data.Vc (before WriteData / Analysis / restart dumps). */
+int ps_set_state(ps_ctx *ctx, const double *Vc);
+int ps_get_state(ps_ctx *ctx, double *Vc);
+
+/* g_time, g_dt, g_stepNumber of the main loop (Src/globals.h:104-110). */
+int ps_set_time(ps_ctx *ctx, double t, double dt, long step);
+int ps_get_time(ps_ctx *ctx, double *t, double *dt, long *step,
+                double *inv_dt_hyp);
+
+/* AdvanceStep (Src/Time_Stepping/rk_step.c:29-384) for TIME_STEPPING RK2
+ * with the given dt: V^n -> V^{n+1} on the device.  On return
+ * *inv_dt_hyp holds Dts->invDt_hyp as UpdateStage leaves it
+ * (update_stage.c:389-394), ready for PLUTO's own NextTimeStep(). */
+int ps_advance_step(ps_ctx *ctx, double dt, double *inv_dt_hyp);
+
+/* The main loop of Src/main.c:215-337 (Integrate + NextTimeStep and the
+ * tstop clamp) for nsteps steps, entirely on the device and replayed
+ * from a captured CUDA graph; no host synchronisation between steps. */
+int ps_run(ps_ctx *ctx, int nsteps);
+
+/* Waits for the context's stream and returns the accumulated device
+ * flags (PS_F_*), or a negative error. */
+int ps_sync(ps_ctx *ctx);
+
+/* Device address of the primitive state (pitched [nv][k][j][px]) and its
+ * row pitch in elements, for callers that keep inputs resident. */
+double *ps_device_state(ps_ctx *ctx, int *pitch_elems);
+
+/* Number of kernels launched by this context since creation. */
+long ps_launch_count(const ps_ctx *ctx);
+
+/* dt used by each of the first `max` steps (indexed by g_stepNumber, up to
+ * 4096), as recorded on the device; returns the count copied. */
+int ps_get_dt_history(ps_ctx *ctx, double *out, int max);
+
+/* Issue all further work of the context on `stream` (a cudaStream_t owned
+ * by the caller; NULL restores the context's own stream).  No reference
+ * counterpart: lets a host framework order the path with its own work. */
+int ps_set_stream(ps_ctx *ctx, void *stream);
+
+/* Device-side checkpoint / restore of Data.Vc and the main-loop scalars:
+ * the backup that FAILSAFE keeps before a step (Src/failsafe.c:5-160),
+ * held on the GPU so that a step can be retried or a run replayed. */
+int ps_save_state(ps_ctx *ctx);
+int ps_restore_state(ps_ctx *ctx);
+
+/* Diagnostic with no reference counterpart: runs one step with a CUDA
+ * event around each of its kernels; ms[0..2] = stage 1, stage 2 and the
+ * dt kernel.  Advances the state by one step. */
+int ps_time_step_kernels(ps_ctx *ctx, double *ms);
+
+/* Diagnostic with no reference counterpart: measured FP64 FMA throughput
+ * of the current device in FLOP/s (2 per FMA), or < 0 on error. */
+double ps_probe_fp64_flops(int reps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,75 @@
+# Builds the reference's own serial CPU PLUTO for one problem configuration,
+# straight from the reference sources with gcc (no setup.py, no generated
+# makefile).  Test infrastructure only: the binary lands in
+# oracle/_ref/<CFG>/ (git-ignored) and is used to generate and pin golden
+# vectors for the oracle restatement.
+#
+#   make -f oracle/ref.mk CFG=blast2d REF=/root/reference
+#
+# Flags follow Config/Linux.gcc.defs of the reference (-O3 -std=c17, no
+# -march, so no FMA contraction); the object list follows
+# Src/Templates/makefile plus the module makefiles for HD, EOS/Ideal,
+# Math_Tools and the RK2/PLM choices made by setup.py.
+
+REF     ?= /root/reference
+CFG     ?= blast2d
+HERE    := $(dir $(abspath $(lastword $(MAKEFILE_LIST))))
+CFGDIR  := $(HERE)ref_cfg/$(CFG)
+OUT     := $(HERE)_ref/$(CFG)
+SRC     := $(REF)/Src
+
+CC      := gcc
+CFLAGS  := -O3 -std=c17 -w
+LDFLAGS := -lm
+
+SRCDIRS := $(SRC) $(SRC)/HD $(SRC)/MHD $(SRC)/EOS/Ideal $(SRC)/States \
+           $(SRC)/Time_Stepping $(SRC)/Math_Tools
+INCS    := -I$(CFGDIR) -I$(SRC) -I$(SRC)/HD -I$(SRC)/EOS/Ideal \
+           -I$(SRC)/States -I$(SRC)/Math_Tools
+
+OBJ := adv_flux.o arrays.o array_reconstruct.o boundary.o check_states.o \
+       cmd_line_opt.o debug_tools.o entropy_switch.o failsafe.o \
+       flag_shock.o flatten.o fluid_interface_boundary.o get_nghost.o \
+       init.o int_bound_reset.o input_data.o mappers3D.o mean_mol_weight.o \
+       parse_file.o plm_coeffs.o rbox.o reconstruct.o rotate.o \
+       set_indexes.o set_geometry.o set_output.o tools.o var_names.o \
+       bin_io.o colortable.o initialize.o jet_domain.o main.o output_log.o \
+       restart.o ring_average.o runtime_setup.o set_image.o show_config.o \
+       set_grid.o startup.o split_source.o userdef_output.o write_data.o \
+       write_tab.o write_img.o write_vtk.o write_vtk_proc.o \
+       math_interp.o math_lu_decomp.o math_qr_decomp.o math_misc.o \
+       math_ode.o math_quadrature.o math_random.o math_root_finders.o \
+       math_table2D.o \
+       advection_solver.o ausm.o eigenv.o fluxes.o mappers.o mappers_loc.o \
+       hll_speed.o hll.o hllc.o set_solver.o tvdlf.o two_shock.o roe.o \
+       prim_eqn.o rhs.o rhs_source.o eos.o plm_states.o rk_step.o \
+       update_stage.o
+
+# Extra modules for the line-driven wind configurations.
+ifneq ($(wildcard $(CFGDIR)/WIND),)
+SRCDIRS += $(SRC)/Cooling/BLONDIN $(SRC)/LineDriven
+INCS    += -I$(SRC)/Cooling/BLONDIN -I$(SRC)/LineDriven
+OBJ     += cooling.o line_connect.o
+endif
+
+# The configuration directory comes first so that its init.c (and any
+# file it overrides) wins, as with PLUTO's own VPATH.
+VPATH := $(CFGDIR) $(SRCDIRS)
+
+OBJS := $(addprefix $(OUT)/,$(OBJ))
+
+all: $(OUT)/pluto $(OUT)/pluto.ini
+
+$(OUT)/pluto: $(OBJS)
+	$(CC) $(OBJS) $(LDFLAGS) -o $@
+
+$(OUT)/pluto.ini: $(CFGDIR)/pluto.ini
+	cp $< $@
+
+$(OUT)/%.o: %.c $(CFGDIR)/definitions.h | $(OUT)
+	$(CC) $(CFLAGS) $(INCS) -c $< -o $@
+
+$(OUT):
+	mkdir -p $@
+
+.PHONY: all

@@ -1,0 +1,652 @@
+// ps_api.cu -- C ABI of the GB300 hydro path: device context, TMA tensor
+// maps, the device-side main-loop scalars (dt selection) and CUDA-graph
+// replay of whole runs.
+//
+// Reference (paths inside the reference project):
+//   main loop / tstop clamp   Src/main.c:215-337
+//   Integrate (resets)        Src/main.c:383-497
+//   NextTimeStep              Src/main.c:521-697
+//   invDt_hyp reduction       Src/Time_Stepping/update_stage.c:389-394
+#include "ps_gb300.h"
+#include "ps_hydro.cuh"
+#include "ps_physics.cuh"
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+namespace ps {
+const void *stage_kernel_2d(int nv, int lim, int solver, int stage);
+const void *stage_kernel_3d(int nv, int lim, int solver, int stage);
+size_t stage_smem_2d(int nv);
+size_t stage_smem_3d(int nv);
+void stage_tile_2d(int *t);
+void stage_tile_3d(int *t);
+
+enum { MODE_BEGIN = 0, MODE_STEP = 1, MODE_INV = 2, MODE_PREP = 3 };
+
+// End of one step and start of the next, on one CTA: invDt_hyp from the
+// stage-1 maximum of C_dt, g_time update, NextTimeStep, the tstop clamp and
+// the per-step resets of Integrate(); then dt/dx for the new dt.
+__global__ void k_finish(FinishArgs f)
+{
+  __shared__ double s_dt;
+  __shared__ int s_run;
+  if (threadIdx.x == 0) {
+    Scalars *sc = f.sc;
+    const Params &p = f.p;
+    if (!sc->done && (f.mode == MODE_STEP || f.mode == MODE_INV)) {
+      const double maxc = __longlong_as_double((long long)sc->cdt_bits);
+      double inv = dmax(sc->inv_dt_hyp, maxc);
+      inv /= (double)(p.dims);
+      sc->inv_dt_hyp = inv;
+      const long long n = sc->step;
+      if (n >= 0 && n < kHist) f.hist_dt[n] = sc->dt;
+      if (f.mode == MODE_STEP) {
+        sc->t += sc->dt;
+        if (!p.cooling || n % 2 == 1) {
+          double dt_hyp = 1.0 / sc->inv_dt_hyp;
+          dt_hyp *= p.cfl;
+          double dtnext = dt_hyp;
+          if (p.cooling) dtnext = dmin(dtnext, sc->dt_cool);
+          dtnext = dmin(dtnext, p.cfl_max_var * sc->dt);
+          if (dtnext < p.first_dt * 1.e-9) {
+            sc->flags |= F_DT_SMALL;
+            sc->done = 1;
+          } else if (p.cfl_max_var != 1.0) {
+            sc->dt = dtnext;
+          }
+        }
+        sc->step = n + 1;
+        if (sc->last) sc->done = 1;
+      }
+    }
+    if (!sc->done && (f.mode == MODE_BEGIN || f.mode == MODE_STEP)) {
+      if ((sc->t + sc->dt) >= p.tstop * (1.0 - 1.e-8)) {
+        sc->dt = p.tstop - sc->t;
+        sc->last = 1;
+      }
+      const long long n = sc->step;
+      if (!p.cooling || (n - 1) % 2 == 1) {
+        sc->inv_dt_hyp = 0.0;
+        sc->dt_cool = 1.e38;
+      }
+    }
+    if (f.mode != MODE_INV) sc->cdt_bits = 0ull;
+    s_dt = sc->dt;
+    s_run = !sc->done && f.mode != MODE_INV;
+  }
+  __syncthreads();
+  if (!s_run) return;
+  for (int d = 0; d < f.p.dims; d++)
+    for (int i = threadIdx.x; i < f.p.ntot[d]; i += blockDim.x)
+      f.dtdx[d][i] = s_dt / f.dx[d][i];
+}
+
+void fill_ghosts_2d(double *V, const Params &p, cudaStream_t s);
+void fill_ghosts_3d(double *V, const Params &p, cudaStream_t s);
+
+}  // namespace ps
+
+// ------------------------------------------------------------------
+// error reporting
+// ------------------------------------------------------------------
+
+static thread_local char g_errmsg[512] = "";
+
+extern "C" void ps_set_error_msg(const char *msg)
+{
+  std::snprintf(g_errmsg, sizeof(g_errmsg), "%s", msg ? msg : "");
+}
+
+extern "C" const char *ps_last_error(void) { return g_errmsg; }
+
+static int cuda_fail(cudaError_t e, const char *where)
+{
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
+  ps_set_error_msg(buf);
+  return PS_ECUDA;
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// ------------------------------------------------------------------
+// context
+// ------------------------------------------------------------------
+
+struct ps_ctx {
+  ps_config cfg;
+  ps::Params p;
+  int tile[6];
+  dim3 grid, block;
+  size_t smem;
+  const void *k1, *k2;
+  double *V, *Vs, *Us;
+  double *Vsave;            // device checkpoint of V (ps_save_state)
+  ps::Scalars *sc_save;
+  double *dx[3], *inv_dx[3], *dtdx[3];
+  ps::Scalars *sc;
+  double *hist;
+  CUtensorMap tmV, tmVs;
+  cudaStream_t stream;      // stream the work is issued on
+  cudaStream_t own_stream;  // stream created by the context
+  cudaGraphExec_t g1, gN;
+  int nG;
+  long launches;
+  int grid_mask;
+};
+
+namespace ps {
+static void launch_fill_ghosts(const ps_ctx *c, double *V, cudaStream_t s)
+{
+  if (c->p.dims == 2)
+    fill_ghosts_2d(V, c->p, s);
+  else
+    fill_ghosts_3d(V, c->p, s);
+}
+}  // namespace ps
+
+static int encode_map(ps_ctx *c, double *base, CUtensorMap *tm)
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+      ps_set_error_msg("cuTensorMapEncodeTiled entry point not available");
+      return PS_ECUDA;
+    }
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const ps::Params &p = c->p;
+  cuuint64_t dims[4] = {(cuuint64_t)p.ntot[0], (cuuint64_t)p.ntot[1], (cuuint64_t)p.ntot[2],
+                        (cuuint64_t)p.nvar};
+  cuuint64_t strides[3] = {(cuuint64_t)p.px * 8, (cuuint64_t)p.px * p.ntot[1] * 8,
+                           (cuuint64_t)p.vstride * 8};
+  cuuint32_t box[4] = {(cuuint32_t)(c->tile[0] + 2 * c->tile[3]),
+                       (cuuint32_t)(c->tile[1] + 2 * c->tile[4]),
+                       (cuuint32_t)(c->tile[2] + 2 * c->tile[5]), (cuuint32_t)p.nvar};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, base, dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    ps_set_error_msg(buf);
+    return PS_ECUDA;
+  }
+  return 0;
+}
+
+static void free_ctx(ps_ctx *c)
+{
+  if (!c) return;
+  if (c->g1) cudaGraphExecDestroy(c->g1);
+  if (c->gN) cudaGraphExecDestroy(c->gN);
+  cudaFree(c->V);
+  cudaFree(c->Vs);
+  cudaFree(c->Us);
+  for (int d = 0; d < 3; d++) {
+    cudaFree(c->dx[d]);
+    cudaFree(c->inv_dx[d]);
+    cudaFree(c->dtdx[d]);
+  }
+  cudaFree(c->sc);
+  cudaFree(c->hist);
+  cudaFree(c->Vsave);
+  cudaFree(c->sc_save);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
+{
+  if (!cfg || !out) {
+    ps_set_error_msg("ps_create: null argument");
+    return PS_EINVAL;
+  }
+  *out = nullptr;
+  if ((cfg->dims != 2 && cfg->dims != 3) || (cfg->nvar != 5 && cfg->nvar != 6) ||
+      cfg->geometry != PS_CARTESIAN || cfg->limiter < 0 || cfg->limiter > 2 ||
+      (cfg->solver != PS_HLLC && cfg->solver != PS_HLL) || cfg->gamma <= 1.0) {
+    ps_set_error_msg("ps_create: unsupported configuration (dims 2/3, nvar 5/6, Cartesian, "
+                     "MC/VL/MM limiter, HLLC/HLL)");
+    return PS_EINVAL;
+  }
+  for (int d = 0; d < 3; d++) {
+    if (d < cfg->dims && cfg->nx[d] < 4) {
+      ps_set_error_msg("ps_create: at least 4 active cells per active direction");
+      return PS_EINVAL;
+    }
+    if (d >= cfg->dims && cfg->nx[d] != 1) {
+      ps_set_error_msg("ps_create: inactive directions must have nx = 1");
+      return PS_EINVAL;
+    }
+  }
+  for (int s = 0; s < 2 * cfg->dims; s++) {
+    int b = cfg->bc[s];
+    if (b != PS_BC_OUTFLOW && b != PS_BC_PERIODIC && b != PS_BC_REFLECTIVE &&
+        b != PS_BC_AXISYM && b != PS_BC_EQTSYM) {
+      ps_set_error_msg("ps_create: boundary type not supported on this path");
+      return PS_EINVAL;
+    }
+    if ((b == PS_BC_PERIODIC) != (cfg->bc[s ^ 1] == PS_BC_PERIODIC)) {
+      ps_set_error_msg("ps_create: periodic boundaries must be paired");
+      return PS_EINVAL;
+    }
+  }
+
+  ps_ctx *c = new ps_ctx();
+  std::memset(&c->p, 0, sizeof(c->p));
+  c->cfg = *cfg;
+  ps::Params &p = c->p;
+  p.dims = cfg->dims;
+  p.nvar = cfg->nvar;
+  p.limiter = cfg->limiter;
+  p.solver = cfg->solver;
+  p.cooling = cfg->cooling;
+  for (int d = 0; d < 3; d++) {
+    p.nx[d] = cfg->nx[d];
+    p.beg[d] = d < cfg->dims ? 2 : 0;
+    p.ntot[d] = cfg->nx[d] + 2 * p.beg[d];
+  }
+  for (int s = 0; s < 6; s++) p.bc[s] = cfg->bc[s];
+  p.px = (p.ntot[0] + 3) & ~3;
+  p.vstride = (long long)p.px * p.ntot[1] * p.ntot[2];
+  p.gamma = cfg->gamma;
+  p.gmm1 = cfg->gamma - 1.0;
+  p.cfl = cfg->cfl;
+  p.cfl_max_var = cfg->cfl_max_var;
+  p.tstop = cfg->tstop;
+  p.first_dt = cfg->first_dt;
+
+  if (cfg->dims == 2) {
+    ps::stage_tile_2d(c->tile);
+    c->smem = ps::stage_smem_2d(p.nvar);
+    c->k1 = ps::stage_kernel_2d(p.nvar, p.limiter, p.solver, 1);
+    c->k2 = ps::stage_kernel_2d(p.nvar, p.limiter, p.solver, 2);
+  } else {
+    ps::stage_tile_3d(c->tile);
+    c->smem = ps::stage_smem_3d(p.nvar);
+    c->k1 = ps::stage_kernel_3d(p.nvar, p.limiter, p.solver, 1);
+    c->k2 = ps::stage_kernel_3d(p.nvar, p.limiter, p.solver, 2);
+  }
+  c->block = dim3(c->tile[0] * c->tile[1] * c->tile[2]);
+  c->grid = dim3((p.nx[0] + c->tile[0] - 1) / c->tile[0], (p.nx[1] + c->tile[1] - 1) / c->tile[1],
+                 (p.nx[2] + c->tile[2] - 1) / c->tile[2]);
+
+  cudaError_t e;
+  const size_t nbytes = (size_t)p.vstride * p.nvar * sizeof(double);
+#define TRY(call)                                  \
+  do {                                             \
+    e = (call);                                    \
+    if (e != cudaSuccess) {                        \
+      int r_ = cuda_fail(e, #call);                \
+      free_ctx(c);                                 \
+      return r_;                                   \
+    }                                              \
+  } while (0)
+  TRY(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+  c->stream = c->own_stream;
+  TRY(cudaMalloc(&c->V, nbytes));
+  TRY(cudaMalloc(&c->Vs, nbytes));
+  TRY(cudaMalloc(&c->Us, nbytes));
+  TRY(cudaMemset(c->V, 0, nbytes));
+  TRY(cudaMemset(c->Vs, 0, nbytes));
+  TRY(cudaMemset(c->Us, 0, nbytes));
+  for (int d = 0; d < 3; d++) {
+    TRY(cudaMalloc(&c->dx[d], p.ntot[d] * sizeof(double)));
+    TRY(cudaMalloc(&c->inv_dx[d], p.ntot[d] * sizeof(double)));
+    TRY(cudaMalloc(&c->dtdx[d], p.ntot[d] * sizeof(double)));
+    TRY(cudaMemset(c->dx[d], 0, p.ntot[d] * sizeof(double)));
+    TRY(cudaMemset(c->inv_dx[d], 0, p.ntot[d] * sizeof(double)));
+    TRY(cudaMemset(c->dtdx[d], 0, p.ntot[d] * sizeof(double)));
+  }
+  TRY(cudaMalloc(&c->sc, sizeof(ps::Scalars)));
+  TRY(cudaMalloc(&c->hist, ps::kHist * sizeof(double)));
+  TRY(cudaMemset(c->hist, 0, ps::kHist * sizeof(double)));
+  TRY(cudaFuncSetAttribute(c->k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+  TRY(cudaFuncSetAttribute(c->k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+#undef TRY
+  ps::Scalars s0;
+  std::memset(&s0, 0, sizeof(s0));
+  s0.dt = cfg->first_dt;
+  s0.dt_cool = 1.e38;
+  if (cudaMemcpy(c->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice) != cudaSuccess) {
+    free_ctx(c);
+    return cuda_fail(cudaGetLastError(), "ps_create: scalars");
+  }
+  int r = encode_map(c, c->V, &c->tmV);
+  if (!r) r = encode_map(c, c->Vs, &c->tmVs);
+  if (r) {
+    free_ctx(c);
+    return r;
+  }
+  *out = c;
+  return 0;
+}
+
+extern "C" int ps_destroy(ps_ctx *c)
+{
+  if (!c) return PS_EINVAL;
+  cudaStreamSynchronize(c->stream);
+  free_ctx(c);
+  return 0;
+}
+
+extern "C" int ps_set_grid(ps_ctx *c, int dir, const double *x, const double *xl,
+                           const double *xr, const double *dx)
+{
+  (void)x;
+  (void)xl;
+  (void)xr;
+  if (!c || dir < 0 || dir >= c->p.dims || !dx) {
+    ps_set_error_msg("ps_set_grid: bad arguments");
+    return PS_EINVAL;
+  }
+  const int n = c->p.ntot[dir];
+  double *inv = (double *)std::malloc(n * sizeof(double));
+  if (!inv) return PS_ENOMEM;
+  for (int i = 0; i < n; i++) inv[i] = 1.0 / (dx[i]);  // Src/set_geometry.c:243-245
+  cudaError_t e = cudaMemcpy(c->dx[dir], dx, n * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->inv_dx[dir], inv, n * sizeof(double), cudaMemcpyHostToDevice);
+  std::free(inv);
+  if (e != cudaSuccess) return cuda_fail(e, "ps_set_grid");
+  c->grid_mask |= 1 << dir;
+  return 0;
+}
+
+static int launch_finish(ps_ctx *c, int mode)
+{
+  ps::FinishArgs f;
+  f.sc = c->sc;
+  f.hist_dt = c->hist;
+  for (int d = 0; d < 3; d++) {
+    f.dtdx[d] = c->dtdx[d];
+    f.dx[d] = c->dx[d];
+  }
+  f.p = c->p;
+  f.mode = mode;
+  ps::k_finish<<<1, 256, 0, c->stream>>>(f);
+  c->launches++;
+  return 0;
+}
+
+static ps::StageArgs stage_args(ps_ctx *c, int stage)
+{
+  ps::StageArgs a;
+  a.Vn = c->V;
+  a.Vout = stage == 1 ? c->Vs : c->V;
+  a.Us = c->Us;
+  for (int d = 0; d < 3; d++) {
+    a.dtdx[d] = c->dtdx[d];
+    a.inv_dx[d] = c->inv_dx[d];
+  }
+  a.sc = c->sc;
+  a.p = c->p;
+  return a;
+}
+
+static cudaError_t launch_stage(ps_ctx *c, int stage)
+{
+  ps::StageArgs a = stage_args(c, stage);
+  CUtensorMap *tm = stage == 1 ? &c->tmV : &c->tmVs;
+  void *args[2] = {tm, &a};
+  cudaError_t e = cudaLaunchKernel(stage == 1 ? c->k1 : c->k2, c->grid, c->block, args, c->smem,
+                                   c->stream);
+  c->launches++;
+  return e;
+}
+
+static int check_ready(ps_ctx *c, const char *who)
+{
+  if (!c) {
+    ps_set_error_msg("null context");
+    return PS_EINVAL;
+  }
+  if (c->grid_mask != (1 << c->p.dims) - 1) {
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "%s: ps_set_grid not called for every direction", who);
+    ps_set_error_msg(buf);
+    return PS_ESTATE;
+  }
+  return 0;
+}
+
+extern "C" int ps_set_state(ps_ctx *c, const double *Vc)
+{
+  int r = check_ready(c, "ps_set_state");
+  if (r) return r;
+  if (!Vc) return PS_EINVAL;
+  const ps::Params &p = c->p;
+  CK(cudaMemcpy2DAsync(c->V, (size_t)p.px * 8, Vc, (size_t)p.ntot[0] * 8, (size_t)p.ntot[0] * 8,
+                       (size_t)p.ntot[1] * p.ntot[2] * p.nvar, cudaMemcpyHostToDevice, c->stream));
+  ps::launch_fill_ghosts(c, c->V, c->stream);
+  c->launches++;
+  CK(cudaGetLastError());
+  launch_finish(c, ps::MODE_BEGIN);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+extern "C" int ps_get_state(ps_ctx *c, double *Vc)
+{
+  if (!c || !Vc) return PS_EINVAL;
+  const ps::Params &p = c->p;
+  CK(cudaMemcpy2DAsync(Vc, (size_t)p.ntot[0] * 8, c->V, (size_t)p.px * 8, (size_t)p.ntot[0] * 8,
+                       (size_t)p.ntot[1] * p.ntot[2] * p.nvar, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+extern "C" int ps_set_time(ps_ctx *c, double t, double dt, long step)
+{
+  if (!c) return PS_EINVAL;
+  ps::Scalars s;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
+  s.t = t;
+  s.dt = dt;
+  s.step = step;
+  s.last = 0;
+  s.done = 0;
+  s.inv_dt_hyp = 0.0;
+  s.dt_cool = 1.e38;
+  CK(cudaMemcpy(c->sc, &s, sizeof(s), cudaMemcpyHostToDevice));
+  if (check_ready(c, "ps_set_time") == 0) {
+    launch_finish(c, ps::MODE_BEGIN);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return 0;
+}
+
+extern "C" int ps_get_time(ps_ctx *c, double *t, double *dt, long *step, double *inv)
+{
+  if (!c) return PS_EINVAL;
+  ps::Scalars s;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
+  if (t) *t = s.t;
+  if (dt) *dt = s.dt;
+  if (step) *step = (long)s.step;
+  if (inv) *inv = s.inv_dt_hyp;
+  return 0;
+}
+
+extern "C" int ps_sync(ps_ctx *c)
+{
+  if (!c) return PS_EINVAL;
+  unsigned flags = 0;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(&flags, &c->sc->flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  return (int)flags;
+}
+
+extern "C" int ps_advance_step(ps_ctx *c, double dt, double *inv_dt_hyp)
+{
+  int r = check_ready(c, "ps_advance_step");
+  if (r) return r;
+  ps::Scalars s;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
+  s.dt = dt;
+  s.inv_dt_hyp = inv_dt_hyp ? *inv_dt_hyp : 0.0;
+  s.done = 0;
+  s.last = 0;
+  CK(cudaMemcpy(c->sc, &s, sizeof(s), cudaMemcpyHostToDevice));
+  launch_finish(c, ps::MODE_PREP);
+  CK(launch_stage(c, 1));
+  CK(launch_stage(c, 2));
+  launch_finish(c, ps::MODE_INV);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
+  if (inv_dt_hyp) *inv_dt_hyp = s.inv_dt_hyp;
+  return (int)s.flags;
+}
+
+static int build_graph(ps_ctx *c, int nsteps, cudaGraphExec_t *out)
+{
+  cudaGraph_t g;
+  long before = c->launches;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < nsteps; s++) {
+    launch_stage(c, 1);
+    launch_stage(c, 2);
+    launch_finish(c, ps::MODE_STEP);
+  }
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->launches = before;  // captured, not yet launched
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  return 0;
+}
+
+extern "C" int ps_run(ps_ctx *c, int nsteps)
+{
+  int r = check_ready(c, "ps_run");
+  if (r) return r;
+  if (nsteps < 0) return PS_EINVAL;
+  const int G = 16;
+  if (!c->g1) {
+    r = build_graph(c, 1, &c->g1);
+    if (r) return r;
+  }
+  if (nsteps >= G && !c->gN) {
+    r = build_graph(c, G, &c->gN);
+    if (r) return r;
+    c->nG = G;
+  }
+  int left = nsteps;
+  while (left >= G) {
+    CK(cudaGraphLaunch(c->gN, c->stream));
+    c->launches += 3L * G;
+    left -= G;
+  }
+  while (left > 0) {
+    CK(cudaGraphLaunch(c->g1, c->stream));
+    c->launches += 3;
+    left--;
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
+extern "C" double *ps_device_state(ps_ctx *c, int *pitch)
+{
+  if (!c) return nullptr;
+  if (pitch) *pitch = c->p.px;
+  return c->V;
+}
+
+extern "C" long ps_launch_count(const ps_ctx *c) { return c ? c->launches : -1; }
+
+extern "C" int ps_get_dt_history(ps_ctx *c, double *out, int max)
+{
+  if (!c || !out || max < 0) return PS_EINVAL;
+  int n = max < ps::kHist ? max : ps::kHist;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(out, c->hist, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return n;
+}
+
+extern "C" int ps_set_stream(ps_ctx *c, void *stream)
+{
+  if (!c) return PS_EINVAL;
+  CK(cudaStreamSynchronize(c->stream));
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  return 0;
+}
+
+// Device-side checkpoint of the state and the main-loop scalars (the
+// role of the FAILSAFE backup in Src/failsafe.c:5-160, kept on the GPU).
+extern "C" int ps_save_state(ps_ctx *c)
+{
+  if (!c) return PS_EINVAL;
+  const size_t nbytes = (size_t)c->p.vstride * c->p.nvar * sizeof(double);
+  if (!c->Vsave) {
+    CK(cudaMalloc(&c->Vsave, nbytes));
+    CK(cudaMalloc(&c->sc_save, sizeof(ps::Scalars)));
+  }
+  CK(cudaMemcpyAsync(c->Vsave, c->V, nbytes, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->sc_save, c->sc, sizeof(ps::Scalars), cudaMemcpyDeviceToDevice,
+                     c->stream));
+  return 0;
+}
+
+extern "C" int ps_restore_state(ps_ctx *c)
+{
+  if (!c || !c->Vsave) {
+    ps_set_error_msg("ps_restore_state: no saved state");
+    return PS_ESTATE;
+  }
+  const size_t nbytes = (size_t)c->p.vstride * c->p.nvar * sizeof(double);
+  CK(cudaMemcpyAsync(c->V, c->Vsave, nbytes, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->sc, c->sc_save, sizeof(ps::Scalars), cudaMemcpyDeviceToDevice,
+                     c->stream));
+  return 0;
+}
+
+// Runs one step with a CUDA event around each of its three kernels and
+// returns their durations in ms (stage 1, stage 2, finish).  Advances the
+// state by one step like ps_run(ctx, 1).
+extern "C" int ps_time_step_kernels(ps_ctx *c, double *ms)
+{
+  int r = check_ready(c, "ps_time_step_kernels");
+  if (r) return r;
+  if (!ms) return PS_EINVAL;
+  cudaEvent_t ev[4];
+  for (int i = 0; i < 4; i++) CK(cudaEventCreate(&ev[i]));
+  CK(cudaEventRecord(ev[0], c->stream));
+  CK(launch_stage(c, 1));
+  CK(cudaEventRecord(ev[1], c->stream));
+  CK(launch_stage(c, 2));
+  CK(cudaEventRecord(ev[2], c->stream));
+  launch_finish(c, ps::MODE_STEP);
+  CK(cudaEventRecord(ev[3], c->stream));
+  CK(cudaEventSynchronize(ev[3]));
+  for (int i = 0; i < 3; i++) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+    ms[i] = t;
+  }
+  for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
+  return 0;
+}

@@ -1,0 +1,203 @@
+// ps_physics.cuh -- per-cell / per-interface FP64 arithmetic of the HD path.
+//
+// Every expression keeps the operand order and rounding steps of the
+// reference so that the device result is bit-identical to the reference's
+// serial build (compiled without FMA contraction).  This file is built with
+// -fmad=false; divisions and square roots are IEEE correctly rounded.
+//
+// Reference (paths inside the reference project):
+//   PrimToCons / ConsToPrim   Src/HD/mappers.c:26-200
+//   limiters                  Src/States/plm_coeffs.h:72-180
+//   SoundSpeed2               Src/EOS/Ideal/eos.c:16-42
+//   Flux                      Src/HD/fluxes.c:23-51
+//   MaxSignalSpeed / Davis    Src/HD/eigenv.c:34-65, Src/HD/hll_speed.c:24-91
+//   HLLC / HLL                Src/HD/hllc.c:28-180, Src/HD/hll.c:30-107
+//   passive scalar flux       Src/adv_flux.c:47-80
+#pragma once
+
+#include <cstdint>
+
+namespace ps {
+
+constexpr int RHO = 0, VX1 = 1, VX2 = 2, VX3 = 3, PRS = 4, NFLX = 5;
+constexpr int LIM_MC = 0, LIM_VL = 1, LIM_MM = 2;
+constexpr int HLLC = 0, HLL = 1;
+
+constexpr double kSmallDensity = 1.e-12;   // g_smallDensity  (Src/globals.h:115)
+constexpr double kSmallPressure = 1.e-12;  // g_smallPressure (Src/globals.h:116)
+
+// device flag bits (mirrors PS_F_* of the C ABI)
+constexpr unsigned F_NAN = 0x01, F_CONS2PRIM = 0x02, F_NEG_DENSITY = 0x04,
+                   F_DT_SMALL = 0x08, F_TMA_TIMEOUT = 0x10;
+
+__device__ __forceinline__ double abs_min(double a, double b)
+{
+  return fabs(a) < fabs(b) ? a : b;
+}
+__device__ __forceinline__ double dmax(double a, double b) { return a >= b ? a : b; }
+__device__ __forceinline__ double dmin(double a, double b) { return a <= b ? a : b; }
+
+__device__ __forceinline__ bool is_nan_bits(double x)
+{
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+}
+
+// Limited slope on a uniform Cartesian grid (cp = cm = 2, d = 1/2).
+template <int LIM>
+__device__ __forceinline__ double limited_slope(double dvp, double dvm)
+{
+  if constexpr (LIM == LIM_MC) {
+    double dv = 0.0;
+    if (dvp * dvm > 0.0) {
+      double qc = 0.5 * (dvm + dvp), scrh = 2.0 * abs_min(dvp, dvm);
+      dv = abs_min(qc, scrh);
+    }
+    return dv;
+  } else if constexpr (LIM == LIM_VL) {
+    return dvp * dvm > 0.0 ? 2.0 * dvp * dvm / (dvp + dvm) : 0.0;
+  } else {
+    return dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0;
+  }
+}
+
+template <int NV>
+__device__ __forceinline__ void prim_to_cons(const double (&v)[NV], double (&u)[NV],
+                                             double gmm1)
+{
+  const double rho = v[RHO];
+  u[RHO] = rho;
+  u[VX1] = rho * v[VX1];
+  u[VX2] = rho * v[VX2];
+  u[VX3] = rho * v[VX3];
+  double e = v[VX1] * v[VX1] + v[VX2] * v[VX2] + v[VX3] * v[VX3];
+  u[PRS] = 0.5 * rho * e + v[PRS] / gmm1;
+#pragma unroll
+  for (int nv = NFLX; nv < NV; nv++) u[nv] = rho * v[nv];
+}
+
+// Returns device flag bits; u may be repaired in place as in the reference.
+template <int NV>
+__device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV],
+                                                 double gmm1)
+{
+  unsigned flag = 0;
+  const double m2 = u[VX1] * u[VX1] + u[VX2] * u[VX2] + u[VX3] * u[VX3];
+  if (u[RHO] < 0.0) {
+    u[RHO] = kSmallDensity;
+    flag |= F_CONS2PRIM | F_NEG_DENSITY;
+  }
+  v[RHO] = u[RHO];
+  const double tau = 1.0 / u[RHO];
+  v[VX1] = u[VX1] * tau;
+  v[VX2] = u[VX2] * tau;
+  v[VX3] = u[VX3] * tau;
+  const double kin = 0.5 * m2 / u[RHO];
+  if (u[PRS] < 0.0) {
+    u[PRS] = kSmallPressure / gmm1 + kin;
+    flag |= F_CONS2PRIM;
+  }
+  v[PRS] = gmm1 * (u[PRS] - kin);
+  if (v[PRS] < 0.0) {
+    v[PRS] = kSmallPressure;
+    u[PRS] = v[PRS] / gmm1 + kin;
+    flag |= F_CONS2PRIM;
+  }
+#pragma unroll
+  for (int nv = NFLX; nv < NV; nv++) v[nv] = u[nv] * tau;
+  return flag;
+}
+
+// Riemann problem at one interface.  vL is the + state of the left cell,
+// vR the - state of the right cell, VN the normal velocity index.
+// Outputs the numerical flux (pressure kept apart, as with
+// USE_PRS_GRADIENT), the interface pressure and cmax = max(|SL|, |SR|).
+template <int NV, int SOLVER, int VN>
+__device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&vR)[NV],
+                                        double gam, double gmm1, double (&f)[NV],
+                                        double &pr, double &cmax)
+{
+  double uL[NV], uR[NV];
+  prim_to_cons<NV>(vL, uL, gmm1);
+  prim_to_cons<NV>(vR, uR, gmm1);
+  const double a2L = gam * vL[PRS] / vL[RHO];
+  const double a2R = gam * vR[PRS] / vR[RHO];
+  const double aL = sqrt(a2L), aR = sqrt(a2R);
+  const double SL = dmin(vL[VN] - aL, vR[VN] - aR);
+  const double SR = dmax(vL[VN] + aL, vR[VN] + aR);
+  cmax = dmax(fabs(SL), fabs(SR));
+
+  if (SL > 0.0) {
+    f[RHO] = uL[VN];
+    f[VX1] = uL[VX1] * vL[VN];
+    f[VX2] = uL[VX2] * vL[VN];
+    f[VX3] = uL[VX3] * vL[VN];
+    f[PRS] = (uL[PRS] + vL[PRS]) * vL[VN];
+    pr = vL[PRS];
+  } else if (SR < 0.0) {
+    f[RHO] = uR[VN];
+    f[VX1] = uR[VX1] * vR[VN];
+    f[VX2] = uR[VX2] * vR[VN];
+    f[VX3] = uR[VX3] * vR[VN];
+    f[PRS] = (uR[PRS] + vR[PRS]) * vR[VN];
+    pr = vR[PRS];
+  } else if constexpr (SOLVER == HLL) {
+    double fL[NFLX], fR[NFLX];
+    fL[RHO] = uL[VN];
+    fL[VX1] = uL[VX1] * vL[VN];
+    fL[VX2] = uL[VX2] * vL[VN];
+    fL[VX3] = uL[VX3] * vL[VN];
+    fL[PRS] = (uL[PRS] + vL[PRS]) * vL[VN];
+    fR[RHO] = uR[VN];
+    fR[VX1] = uR[VX1] * vR[VN];
+    fR[VX2] = uR[VX2] * vR[VN];
+    fR[VX3] = uR[VX3] * vR[VN];
+    fR[PRS] = (uR[PRS] + vR[PRS]) * vR[VN];
+    const double scrh = 1.0 / (SR - SL);
+#pragma unroll
+    for (int nv = 0; nv < NFLX; nv++) {
+      double t = SL * SR * (uR[nv] - uL[nv]) + SR * fL[nv] - SL * fR[nv];
+      f[nv] = t * scrh;
+    }
+    pr = (SR * vL[PRS] - SL * vR[PRS]) * scrh;
+  } else {
+    // HLLC: only the star state on the side selected by the contact speed
+    // is formed; the reference forms both and discards one.
+    const double qL = vL[PRS] + uL[VN] * (vL[VN] - SL);
+    const double qR = vR[PRS] + uR[VN] * (vR[VN] - SR);
+    const double wL = vL[RHO] * (vL[VN] - SL);
+    const double wR = vR[RHO] * (vR[VN] - SR);
+    const double vs = (qR - qL) / (wR - wL);
+    const bool left = vs >= 0.0;
+    const double S = left ? SL : SR;
+    const double vx = left ? vL[VN] : vR[VN];
+    double v[NFLX], u[NFLX];
+#pragma unroll
+    for (int nv = 0; nv < NFLX; nv++) {
+      v[nv] = left ? vL[nv] : vR[nv];
+      u[nv] = left ? uL[nv] : uR[nv];
+    }
+    double fs[NFLX];
+    fs[RHO] = u[VN];
+    fs[VX1] = u[VX1] * v[VN];
+    fs[VX2] = u[VX2] * v[VN];
+    fs[VX3] = u[VX3] * v[VN];
+    fs[PRS] = (u[PRS] + v[PRS]) * v[VN];
+    double us[NFLX];
+    us[RHO] = u[RHO] * (S - vx) / (S - vs);
+#pragma unroll
+    for (int nv = VX1; nv <= VX3; nv++) us[nv] = (nv == VN) ? us[RHO] * vs : us[RHO] * v[nv];
+    us[PRS] = u[PRS] / v[RHO] + (vs - vx) * (vs + v[PRS] / (v[RHO] * (S - vx)));
+    us[PRS] *= us[RHO];
+#pragma unroll
+    for (int nv = 0; nv < NFLX; nv++) f[nv] = fs[nv] + S * (us[nv] - u[nv]);
+    pr = v[PRS];
+  }
+  if constexpr (NV > NFLX) {
+    const bool up = f[RHO] > 0.0;
+#pragma unroll
+    for (int nv = NFLX; nv < NV; nv++) f[nv] = f[RHO] * (up ? vL[nv] : vR[nv]);
+  }
+}
+
+}  // namespace ps

@@ -1,0 +1,57 @@
+// ps_stage3d.cu -- instantiations of the fused stage kernel for
+// DIMENSIONS == 3 (one translation unit per dimensionality so that the
+// build compiles them in parallel).
+#include "ps_stage.cuh"
+
+namespace ps {
+
+template <int NV, int LIM, int SOLVER>
+static const void *pick_3d(int stage)
+{
+  return stage == 1 ? reinterpret_cast<const void *>(&k_stage<3, NV, LIM, SOLVER, 1>)
+                    : reinterpret_cast<const void *>(&k_stage<3, NV, LIM, SOLVER, 2>);
+}
+
+template <int NV>
+static const void *pick_nv_3d(int lim, int solver, int stage)
+{
+  if (solver == HLL) {
+    if (lim == LIM_VL) return pick_3d<NV, LIM_VL, HLL>(stage);
+    if (lim == LIM_MM) return pick_3d<NV, LIM_MM, HLL>(stage);
+    return pick_3d<NV, LIM_MC, HLL>(stage);
+  }
+  if (lim == LIM_VL) return pick_3d<NV, LIM_VL, HLLC>(stage);
+  if (lim == LIM_MM) return pick_3d<NV, LIM_MM, HLLC>(stage);
+  return pick_3d<NV, LIM_MC, HLLC>(stage);
+}
+
+const void *stage_kernel_3d(int nv, int lim, int solver, int stage)
+{
+  if (nv == 5) return pick_nv_3d<5>(lim, solver, stage);
+  if (nv == 6) return pick_nv_3d<6>(lim, solver, stage);
+  return nullptr;
+}
+
+size_t stage_smem_3d(int nv)
+{
+  return nv == 5 ? stage_smem_bytes<5, TileT<3>>() : stage_smem_bytes<6, TileT<3>>();
+}
+
+void stage_tile_3d(int *t)
+{
+  t[0] = TileT<3>::X; t[1] = TileT<3>::Y; t[2] = TileT<3>::Z;
+  t[3] = TileT<3>::HX; t[4] = TileT<3>::HY; t[5] = TileT<3>::HZ;
+}
+
+void fill_ghosts_3d(double *V, const Params &p, cudaStream_t s)
+{
+  const long long n = (long long)p.nx[0] * p.nx[1] * p.nx[2];
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  if (p.nvar == 5)
+    k_fill_ghosts<3, 5><<<blocks, 256, 0, s>>>(V, p);
+  else
+    k_fill_ghosts<3, 6><<<blocks, 256, 0, s>>>(V, p);
+}
+
+}  // namespace ps

@@ -1,0 +1,223 @@
+"""ctypes binding of libps_gb300.so (include/ps_gb300.h) for Python callers.
+
+The library is the product; this module only marshals arrays.  It raises
+if the library is missing: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libps_gb300.so")
+
+CARTESIAN, SPHERICAL = 0, 3
+LIM = {"mc": 0, "vl": 1, "mm": 2}
+SOLVER = {"hllc": 0, "hll": 1}
+BC = {"outflow": 1, "reflective": 2, "axisymmetric": 3, "eqtsymmetric": 4,
+      "periodic": 5, "userdef": 8}
+GRID = {"uniform": 0, "log": 1, "ratio": 2}
+FLAGS = {0x01: "nan", 0x02: "cons2prim", 0x04: "negative_density", 0x08: "dt_too_small",
+         0x10: "tma_timeout"}
+
+# Exported entry points declared in include/ps_gb300.h.
+EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_destroy",
+           "ps_set_grid", "ps_set_state", "ps_get_state", "ps_set_time", "ps_get_time",
+           "ps_advance_step", "ps_run", "ps_sync", "ps_device_state", "ps_launch_count",
+           "ps_get_dt_history", "ps_set_stream", "ps_probe_fp64_flops", "ps_save_state",
+           "ps_restore_state", "ps_time_step_kernels"]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("dims", ctypes.c_int), ("nx", ctypes.c_int * 3), ("nvar", ctypes.c_int),
+                ("geometry", ctypes.c_int), ("limiter", ctypes.c_int), ("solver", ctypes.c_int),
+                ("bc", ctypes.c_int * 6), ("gamma", ctypes.c_double), ("cfl", ctypes.c_double),
+                ("cfl_max_var", ctypes.c_double), ("tstop", ctypes.c_double),
+                ("first_dt", ctypes.c_double), ("cooling", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the library (raises OSError if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} not built: run pluto-sirocco_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        D, I, P, DP = ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+        L.ps_last_error.restype = ctypes.c_char_p
+        L.ps_grid_build.argtypes = [I, I, I, D, D, D, DP, DP, DP, DP]
+        L.ps_init_blast.argtypes = [ctypes.POINTER(Config), DP, DP, DP, D, D, D, D,
+                                    ctypes.c_long, DP]
+        L.ps_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(P)]
+        L.ps_destroy.argtypes = [P]
+        L.ps_set_grid.argtypes = [P, I, DP, DP, DP, DP]
+        L.ps_set_state.argtypes = [P, DP]
+        L.ps_get_state.argtypes = [P, DP]
+        L.ps_set_time.argtypes = [P, D, D, ctypes.c_long]
+        L.ps_get_time.argtypes = [P, DP, DP, ctypes.POINTER(ctypes.c_long), DP]
+        L.ps_advance_step.argtypes = [P, D, DP]
+        L.ps_run.argtypes = [P, I]
+        L.ps_sync.argtypes = [P]
+        L.ps_device_state.argtypes = [P, ctypes.POINTER(I)]
+        L.ps_device_state.restype = ctypes.c_void_p
+        L.ps_launch_count.argtypes = [P]
+        L.ps_launch_count.restype = ctypes.c_long
+        L.ps_get_dt_history.argtypes = [P, DP, I]
+        L.ps_set_stream.argtypes = [P, P]
+        L.ps_probe_fp64_flops.argtypes = [I]
+        L.ps_probe_fp64_flops.restype = D
+        L.ps_save_state.argtypes = [P]
+        L.ps_restore_state.argtypes = [P]
+        L.ps_time_step_kernels.argtypes = [P, DP]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_config(dims=2, nx=(256, 256, 1), nvar=5, limiter="mc", solver="hllc",
+                bc="outflow", gamma=5.0 / 3.0, cfl=0.4, cfl_max_var=1.1, tstop=10.0,
+                first_dt=1e-4, cooling=0):
+    c = Config()
+    c.dims = dims
+    n = list(nx) + [1] * (3 - len(nx))
+    c.nx[:] = n[:3]
+    c.nvar = nvar
+    c.geometry = CARTESIAN
+    c.limiter = LIM[limiter]
+    c.solver = SOLVER[solver]
+    bcs = [bc] * 6 if isinstance(bc, str) else list(bc)
+    c.bc[:] = [BC[b] for b in bcs]
+    c.gamma = gamma
+    c.cfl = cfl
+    c.cfl_max_var = cfl_max_var
+    c.tstop = tstop
+    c.first_dt = first_dt
+    c.cooling = cooling
+    return c
+
+
+def check(rc, what):
+    if rc < 0:
+        raise RuntimeError(f"{what} failed ({rc}): {lib().ps_last_error().decode()}")
+    return rc
+
+
+def build_grid(n, ngh, xbeg=0.0, xend=1.0, kind="uniform", ratio=1.0):
+    nt = n + 2 * ngh
+    x, xl, xr, dx = (np.zeros(nt) for _ in range(4))
+    check(lib().ps_grid_build(GRID[kind], n, ngh, xbeg, xend, ratio, _dp(x), _dp(xl), _dp(xr),
+                              _dp(dx)), "ps_grid_build")
+    return x, xl, xr, dx
+
+
+class Grid:
+    """Grid arrays of the total box for every direction (as SetGrid builds them)."""
+
+    def __init__(self, cfg, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0)):
+        self.ngh = [2 if d < cfg.dims else 0 for d in range(3)]
+        self.ntot = [cfg.nx[d] + 2 * self.ngh[d] for d in range(3)]
+        self.arrays = [build_grid(cfg.nx[d], self.ngh[d], xbeg[d], xend[d]) for d in range(3)]
+
+    def x(self, d):
+        return self.arrays[d][0]
+
+
+def blast_state(cfg, grid, p_amb=0.1, p_in=10.0, r_in=0.1, noise=0.01, seed=1):
+    V = np.zeros((cfg.nvar, grid.ntot[2], grid.ntot[1], grid.ntot[0]))
+    check(lib().ps_init_blast(ctypes.byref(cfg), _dp(grid.x(0)), _dp(grid.x(1)), _dp(grid.x(2)),
+                              p_amb, p_in, r_in, noise, seed, _dp(V)), "ps_init_blast")
+    return V
+
+
+class Solver:
+    """One device context (ps_ctx) on the current CUDA device."""
+
+    def __init__(self, cfg, grid):
+        self.cfg = cfg
+        self.grid = grid
+        self.ctx = ctypes.c_void_p()
+        check(lib().ps_create(ctypes.byref(cfg), ctypes.byref(self.ctx)), "ps_create")
+        for d in range(cfg.dims):
+            x, xl, xr, dx = grid.arrays[d]
+            check(lib().ps_set_grid(self.ctx, d, _dp(x), _dp(xl), _dp(xr), _dp(dx)),
+                  "ps_set_grid")
+
+    def close(self):
+        if self.ctx:
+            lib().ps_destroy(self.ctx)
+            self.ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, V):
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        check(lib().ps_set_state(self.ctx, _dp(V)), "ps_set_state")
+
+    def get_state(self, out=None):
+        g = self.grid
+        shape = (self.cfg.nvar, g.ntot[2], g.ntot[1], g.ntot[0])
+        V = np.zeros(shape) if out is None else out
+        if V.shape != shape or V.dtype != np.float64 or not V.flags.c_contiguous:
+            raise ValueError("output array must be C-contiguous float64 of shape %s" % (shape,))
+        check(lib().ps_get_state(self.ctx, _dp(V)), "ps_get_state")
+        return V
+
+    def set_time(self, t, dt, step=0):
+        check(lib().ps_set_time(self.ctx, t, dt, step), "ps_set_time")
+
+    def time(self):
+        t, dt, inv = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        st = ctypes.c_long()
+        check(lib().ps_get_time(self.ctx, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(st),
+                                ctypes.byref(inv)), "ps_get_time")
+        return t.value, dt.value, st.value, inv.value
+
+    def run(self, nsteps):
+        check(lib().ps_run(self.ctx, nsteps), "ps_run")
+        return self.sync()
+
+    def advance_step(self, dt, inv_dt_hyp=0.0):
+        inv = ctypes.c_double(inv_dt_hyp)
+        rc = check(lib().ps_advance_step(self.ctx, dt, ctypes.byref(inv)), "ps_advance_step")
+        return rc, inv.value
+
+    def sync(self):
+        return check(lib().ps_sync(self.ctx), "ps_sync")
+
+    def dt_history(self, n):
+        out = np.zeros(n)
+        k = check(lib().ps_get_dt_history(self.ctx, _dp(out), n), "ps_get_dt_history")
+        return out[:k]
+
+    def launches(self):
+        return lib().ps_launch_count(self.ctx)
+
+    def save(self):
+        check(lib().ps_save_state(self.ctx), "ps_save_state")
+
+    def restore(self):
+        check(lib().ps_restore_state(self.ctx), "ps_restore_state")
+
+    def time_step_kernels(self):
+        ms = np.zeros(3)
+        check(lib().ps_time_step_kernels(self.ctx, _dp(ms)), "ps_time_step_kernels")
+        return ms
+
+    def set_stream(self, stream_handle):
+        check(lib().ps_set_stream(self.ctx, ctypes.c_void_p(stream_handle)), "ps_set_stream")
+
+    def device_state(self):
+        pitch = ctypes.c_int()
+        ptr = lib().ps_device_state(self.ctx, ctypes.byref(pitch))
+        return ptr, pitch.value

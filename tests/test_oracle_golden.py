@@ -1,0 +1,52 @@
+"""The CPU oracle against golden vectors produced by the reference's own
+serial build (tests/golden/make_golden.py).  Bit-exact: every variable of
+every active cell, plus the reference's printed time and next dt."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def _oracle_for(meta):
+    from oracle import Oracle
+    o = Oracle(dims=meta["dims"], nx=meta["n"], limiter=meta["limiter"], solver=meta["solver"],
+               bc=meta["bc"], cfl=meta["cfl"], cfl_max_var=meta["cfl_max_var"],
+               tstop=meta["tstop"], first_dt=meta["first_dt"])
+    o.init_blast(meta["p_amb"], meta["p_in"], meta["r_in"], meta["noise"], meta["seed"])
+    return o
+
+
+@pytest.mark.parametrize("meta", golden_cases(), ids=lambda m: m["name"])
+def test_oracle_matches_reference(built, meta):
+    o = _oracle_for(meta)
+    assert _digest(o.active()) == meta["ic_sha256"], "initial condition differs"
+    if meta["npz"]:
+        v0, v1 = load_golden(meta)
+        assert np.array_equal(o.active(), v0)
+    assert o.run(meta["steps"]) == 0
+    a = o.active()
+    if meta["npz"]:
+        assert np.array_equal(a, v1), f"max |diff| = {np.abs(a - v1).max()}"
+    assert _digest(a) == meta["final_sha256"]
+    t, dt, step = o.time()
+    assert step == meta["steps"]
+    assert float(f"{t:e}") == float(meta["t_final"])
+    assert float(f"{dt:e}") == float(meta["dt_next"])
+
+
+def test_oracle_detects_planted_error(built):
+    """A deliberately perturbed initial cell must break bit-exactness (the
+    comparison is not vacuous)."""
+    meta = [m for m in golden_cases(full_only=True) if m["dims"] == 2][0]
+    o = _oracle_for(meta)
+    V = o.V
+    V[0, 0, 10, 10] = np.nextafter(V[0, 0, 10, 10], 2.0)
+    o.run(meta["steps"])
+    _, v1 = load_golden(meta)
+    assert not np.array_equal(o.active(), v1)
