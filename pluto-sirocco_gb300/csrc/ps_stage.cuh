@@ -240,10 +240,14 @@ __global__ void __launch_bounds__(TileGeom<TileT<DIMS>>::NT)
     tma_load_4d(sv, &tm, ox + p.beg[0] - TL::HX, oy + p.beg[1] - TL::HY,
                 DIMS == 3 ? oz + p.beg[2] - TL::HZ : 0, 0, bar);
   }
-  if (!mbar_wait_bounded(bar, 0, 1u << 22)) {
-    atomicOr(&a.sc->flags, F_TMA_TIMEOUT);
-    // give the copy a last bounded chance to land before the CTA exits
-    mbar_wait_bounded(bar, 0, 1u << 22);
+  const bool landed = mbar_wait_bounded(bar, 0, 1u << 22);
+  if (!__syncthreads_and(landed)) {
+    // block-uniform exit; thread 0 gives the copy a last bounded chance to
+    // land before the CTA's shared memory is released
+    if (tid == 0) {
+      atomicOr(&a.sc->flags, F_TMA_TIMEOUT);
+      mbar_wait_bounded(bar, 0, 1u << 22);
+    }
     return;
   }
 
