@@ -168,6 +168,21 @@ int ps_restore_state(ps_ctx *ctx);
  * dt kernel.  Advances the state by one step. */
 int ps_time_step_kernels(ps_ctx *ctx, double *ms);
 
+/* No counterpart in the reference.  ps_advance_step() for callers that
+ * cannot allocate device memory: the caller owns the state (Vc_dev, a
+ * device buffer laid out like Data.Vc, [nv][k][j][i] over the total box,
+ * 16-byte aligned) and passes the host dx arrays of each direction; the
+ * stage scratch comes from a fixed array inside the library (3.3 MB per
+ * GPU, held until exit).  Limits: 32768 total-box cells per variable,
+ * 6 variables, 2048 cells per direction, even total-box row length;
+ * larger grids get PS_EINVAL.  Calls that overlap on the GPU share the
+ * scratch and race.  The first call on each device looks up the scratch
+ * address; make it before any stream capture.  stream may be NULL. */
+int ps_advance_step_noalloc(const ps_config *cfg, const double *dx1,
+                            const double *dx2, const double *dx3,
+                            double *Vc_dev, double dt, double *inv_dt_hyp,
+                            void *stream);
+
 /* Diagnostic with no reference counterpart: measured FP64 FMA throughput
  * of the current device in FLOP/s (2 per FMA), or < 0 on error. */
 double ps_probe_fp64_flops(int reps);

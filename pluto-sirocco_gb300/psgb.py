@@ -25,7 +25,7 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_set_grid", "ps_set_state", "ps_get_state", "ps_set_time", "ps_get_time",
            "ps_advance_step", "ps_run", "ps_sync", "ps_device_state", "ps_launch_count",
            "ps_get_dt_history", "ps_set_stream", "ps_probe_fp64_flops", "ps_save_state",
-           "ps_restore_state", "ps_time_step_kernels"]
+           "ps_restore_state", "ps_time_step_kernels", "ps_advance_step_noalloc"]
 
 
 class Config(ctypes.Structure):
@@ -73,6 +73,8 @@ def lib():
         L.ps_save_state.argtypes = [P]
         L.ps_restore_state.argtypes = [P]
         L.ps_time_step_kernels.argtypes = [P, DP]
+        L.ps_advance_step_noalloc.argtypes = [ctypes.POINTER(Config), DP, DP, DP,
+                                              ctypes.c_void_p, D, DP, ctypes.c_void_p]
         _lib = L
     return _lib
 
