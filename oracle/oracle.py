@@ -26,7 +26,15 @@ class OrConfig(ctypes.Structure):
                 ("ratio", ctypes.c_double * 3), ("gamma", ctypes.c_double),
                 ("cfl", ctypes.c_double), ("cfl_max_var", ctypes.c_double),
                 ("tstop", ctypes.c_double), ("first_dt", ctypes.c_double),
-                ("cooling", ctypes.c_int)]
+                ("cooling", ctypes.c_int), ("body_force", ctypes.c_int),
+                ("line_force", ctypes.c_int), ("floors", ctypes.c_int),
+                ("unit_density", ctypes.c_double), ("unit_length", ctypes.c_double),
+                ("unit_velocity", ctypes.c_double), ("mu", ctypes.c_double),
+                ("rho_0", ctypes.c_double), ("cent_mass", ctypes.c_double),
+                ("t_iso", ctypes.c_double), ("l_star", ctypes.c_double),
+                ("f_x", ctypes.c_double), ("f_uv", ctypes.c_double), ("t_x", ctypes.c_double),
+                ("krad", ctypes.c_double), ("alpharad", ctypes.c_double),
+                ("dfloor", ctypes.c_double)]
 
 
 _lib = None
@@ -57,27 +65,61 @@ def lib():
         L.or_time.argtypes = [P, DP, DP, ctypes.POINTER(ctypes.c_long)]
         L.or_set_time.argtypes = [P, D, D, ctypes.c_long]
         L.or_history.argtypes = [P, DP, DP, I]
+        L.or_init_wind.argtypes = [P]
+        L.or_set_flux.argtypes = [P, I, DP, DP, DP]
+        L.or_cooling.argtypes = [P, D, D]
+        L.or_sirocco_xi.restype = DP
+        L.or_sirocco_xi.argtypes = [P]
         _lib = L
     return _lib
+
+
+# Parameters of the line-driven disk-wind configuration (the [Parameters]
+# block of oracle/ref_cfg/wind2d/pluto.ini and the units of its
+# definitions.h).
+WIND = dict(mu=0.6, rho_0=1.0e-9, cent_mass=1.4e34, t_iso=4.0e4, l_star=1.0e37, f_x=1.0,
+            f_uv=1.0, t_x=5.6e7, krad=0.2, alpharad=-0.6, dfloor=1.0e-20,
+            unit_density=1e-14, unit_length=1e9, unit_velocity=1e9)
+WIND_GRID = dict(xbeg=(10.0, 0.0, 0.0), xend=(1000.0, 1.5707963267948966, 1.0),
+                 gridtype=("log", "uniform", "uniform"))
+NANGLES = 36
+
+
+def synthetic_flux(x1, x2, ntot, l_uv=1.0e37, unit_length=1e9, na=NANGLES):
+    """Synthetic directional UV flux: L_UV/(4 pi r^2) in the angle bin that
+    contains the radial direction of each active cell, zero elsewhere; the
+    values are rounded through the 13-significant-digit text of the
+    directional_flux_*.dat files the reference reads.  Arrays are
+    [angle][k][j][i] over the total box (ghost cells zero)."""
+    import math
+    fr = np.zeros((na, ntot[2], ntot[1], ntot[0]))
+    for j in range(2, ntot[1] - 2):
+        a = int(math.floor(x2[j] / (2 * 3.14159265358979 / 36)))
+        for i in range(2, ntot[0] - 2):
+            r = x1[i] * unit_length
+            fr[a, :, j, i] = float("%.12e" % (l_uv / (4 * math.pi * r * r)))
+    return fr, np.zeros_like(fr), np.zeros_like(fr)
 
 
 class Oracle:
     def __init__(self, dims=2, nx=(64, 64, 1), nvar=5, limiter="mc", solver="hllc",
                  bc="outflow", gamma=5.0 / 3.0, cfl=0.4, cfl_max_var=1.1, tstop=10.0,
-                 first_dt=1e-4, cooling=0):
+                 first_dt=1e-4, cooling=0, geometry=0, gridtype=("uniform",) * 3,
+                 xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), body_force=0, line_force=0,
+                 floors=0, params=None):
         c = OrConfig()
         c.dims = dims
         n = list(nx) + [1] * (3 - len(nx))
         c.nx[:] = n[:3]
         c.nvar = nvar
-        c.geometry = 0
+        c.geometry = geometry
         c.limiter = LIM[limiter]
         c.solver = SOLVER[solver]
         bcs = [bc] * 6 if isinstance(bc, str) else list(bc)
         c.bc[:] = [BC[b] for b in bcs]
-        c.gridtype[:] = [0, 0, 0]
-        c.xbeg[:] = [0.0, 0.0, 0.0]
-        c.xend[:] = [1.0, 1.0, 1.0]
+        c.gridtype[:] = [{"uniform": 0, "log": 1, "ratio": 2}[g] for g in gridtype]
+        c.xbeg[:] = list(xbeg)
+        c.xend[:] = list(xend)
         c.ratio[:] = [1.0, 1.0, 1.0]
         c.gamma = gamma
         c.cfl = cfl
@@ -85,6 +127,9 @@ class Oracle:
         c.tstop = tstop
         c.first_dt = first_dt
         c.cooling = cooling
+        c.body_force, c.line_force, c.floors = body_force, line_force, floors
+        for k, v in (params or {}).items():
+            setattr(c, k, v)
         self.cfg = c
         self.nvar = nvar
         self.dims = dims
@@ -115,6 +160,19 @@ class Oracle:
     def run(self, nsteps):
         return lib().or_run(self.s, nsteps)
 
+    def init_wind(self):
+        lib().or_init_wind(self.s)
+
+    def set_flux(self, fr, ft, fp):
+        fr, ft, fp = (np.ascontiguousarray(a, dtype=np.float64) for a in (fr, ft, fp))
+        self._flux = (fr, ft, fp)
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib().or_set_flux(self.s, fr.shape[0], fr.ctypes.data_as(dp), ft.ctypes.data_as(dp),
+                          fp.ctypes.data_as(dp))
+
+    def cooling(self, dt, t):
+        lib().or_cooling(self.s, dt, t)
+
     def time(self):
         t, dt = ctypes.c_double(), ctypes.c_double()
         st = ctypes.c_long()
@@ -133,3 +191,19 @@ class Oracle:
         g = [2 if d < self.dims else 0 for d in range(3)]
         a = V[:, g[2]:self.ntot[2] - g[2], g[1]:self.ntot[1] - g[1], g[0]:self.ntot[0] - g[0]]
         return a[:, 0] if self.dims == 2 else a
+
+
+def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4):
+    """The 2-D spherical line-driven disk wind (PLM van Leer, HLL, RK2,
+    userdef/outflow/axisymmetric/reflective boundaries, point-mass gravity,
+    floors, BLONDIN cooling and the line force), initialised."""
+    o = Oracle(dims=2, nx=(nr, nt, 1), nvar=6, limiter="vl", solver="hll",
+               bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
+               cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling,
+               geometry=3, gridtype=WIND_GRID["gridtype"], xbeg=WIND_GRID["xbeg"],
+               xend=WIND_GRID["xend"], body_force=1, line_force=line_force, floors=1,
+               params=WIND)
+    if line_force:
+        o.set_flux(*synthetic_flux(o.grid(0), o.grid(1), o.ntot))
+    o.init_wind()
+    return o

@@ -20,6 +20,14 @@
  *   RK2             Src/Time_Stepping/rk_step.c:18-20, 29-384
  *   boundaries      Src/boundary.c:56-760
  *   main loop / dt  Src/main.c:215-337, 383-497, 521-697
+ *   spherical geom. Src/set_geometry.c:62-250, Src/States/plm_coeffs.c:30-74
+ *   curvilinear RHS Src/MHD/rhs.c:234-351, 423-630, Src/MHD/rhs_source.c:101-420
+ *   line force      Src/LineDriven/line_connect.c:267-320 (xi init),
+ *                   504-777 (VGradCalc, bilinear), 815-903 (LineForce)
+ *   cooling         Src/Cooling/BLONDIN/cooling.c:50-319
+ *   split source    Src/split_source.c:28-79, Strang order Src/main.c:479-485
+ * The wind problem (Init, UserDefBoundary, BodyForceVector) follows the
+ * problem file oracle/ref_cfg/wind2d/init.c used for the reference build.
  */
 #include "ps_oracle.h"
 
@@ -43,6 +51,16 @@
 static const double small_density = 1.e-12;
 static const double small_pressure = 1.e-12;
 
+/* physical constants of Src/pluto.h:296-321 */
+#define C_AMU    1.66053886e-24
+#define C_C      2.99792458e10
+#define C_G      6.6726e-8
+#define C_KB     1.3806505e-16
+#define C_MP     1.67262171e-24
+#define C_PI     3.14159265358979
+#define C_RGAS   8.3144598e7
+#define C_SIGMAT 6.6524e-25
+
 struct or_sim {
   or_config c;
   int ngh[3], ntot[3], beg[3], end[3];
@@ -54,6 +72,19 @@ struct or_sim {
   /* row workspace, [i][nv] */
   double *rv, *rvp, *rvm, *rup, *rum, *rdv, *rflux, *rrhs, *rfL, *rfR;
   double *rpress, *rpL, *rpR, *ra2L, *ra2R, *rcmax, *rSL, *rSR;
+  /* curvilinear geometry and PLM weights (set_geometry.c, plm_coeffs.c) */
+  double *xgc[3], *rt, *sp, *sn, *dmu, *dVr;
+  double *pcp[3], *pcm[3], *pwp[3], *pwm[3], *pdp[3], *pdm[3];
+  double *dV;            /* [k][j][i]                      */
+  double *Ax1, *Ax2;     /* [k][j][i+1], [k][j+1][i] faces */
+  double *rvc;           /* row workspace: face-averaged / centred state */
+  /* line-driven wind */
+  int na;
+  double *Fr, *Ft, *Fp;            /* [a][k][j][i] */
+  double *xi_s, *tr_s;             /* sirocco_xi, sirocco_t_r */
+  double *dvds, *roff, *toff, *moff; /* [a][k][j][i] */
+  double *x11[2], *x22[2];
+  int dvds_ready;
   double g_time, g_dt;
   long step;
   double invDt_hyp, dt_cool;
@@ -124,6 +155,91 @@ static void build_grid(or_sim *s, int d)
   for (i = 0; i < nt; i++) s->inv_dx[d][i] = 1.0 / (dx[i]);
 }
 
+/* Geometry factors (Src/set_geometry.c:62-240) and PLM weights
+ * (Src/States/plm_coeffs.c:30-74, non-HIGH_ORDER branch). */
+static void build_geometry(or_sim *s)
+{
+  int i, j, k, d;
+  int n0 = s->ntot[0], n1 = s->ntot[1], n2 = s->ntot[2];
+  const int sph = s->c.geometry == OR_SPHERICAL;
+  double *x1 = s->x[0], *dx1 = s->dx[0], *x1p = s->xr[0], *x1m = s->xl[0];
+  double *x2 = s->x[1], *x2p = s->xr[1], *x2m = s->xl[1];
+  for (d = 0; d < 3; d++) s->xgc[d] = calloc(s->ntot[d], sizeof(double));
+  s->rt = calloc(n0, sizeof(double));
+  s->dVr = calloc(n0, sizeof(double));
+  s->sp = calloc(n1, sizeof(double));
+  s->sn = calloc(n1, sizeof(double));
+  s->dmu = calloc(n1, sizeof(double));
+  for (i = 0; i < n0; i++) {
+    double xL = x1m[i], xR = x1p[i];
+    if (sph) {
+      s->xgc[0][i] = x1[i] + 2.0 * x1[i] * dx1[i] * dx1[i] /
+                                (12.0 * x1[i] * x1[i] + dx1[i] * dx1[i]);
+      s->rt[i] = (xR * xR * xR - xL * xL * xL) / (xR * xR - xL * xL) / 1.5;
+    } else {
+      s->xgc[0][i] = x1[i];
+      s->rt[i] = x1[i];
+    }
+    s->dVr[i] = fabs(x1p[i] * x1p[i] * x1p[i] - x1m[i] * x1m[i] * x1m[i]) / 3.0;
+  }
+  for (j = 0; j < n1; j++) {
+    double xL = x2m[j], xR = x2p[j];
+    if (sph) {
+      s->xgc[1][j] = sin(xR) - sin(xL) + xL * cos(xL) - xR * cos(xR);
+      s->xgc[1][j] /= cos(xL) - cos(xR);
+      s->sp[j] = fabs(sin(xR));
+      s->sn[j] = fabs(sin(x2[j]));
+      s->dmu[j] = fabs(cos(xL) - cos(xR));
+    } else {
+      s->xgc[1][j] = x2[j];
+    }
+  }
+  for (k = 0; k < n2; k++) s->xgc[2][k] = s->x[2][k];
+  if (sph) {
+    /* 2-D spherical: dV = dVr*dmu, A1 = rp^2*dmu, A2 = |r|*dr*|sin(th_p)| */
+    s->dV = calloc((size_t)n2 * n1 * n0, sizeof(double));
+    s->Ax1 = calloc((size_t)n2 * n1 * (n0 + 1), sizeof(double));
+    s->Ax2 = calloc((size_t)n2 * (n1 + 1) * n0, sizeof(double));
+    for (k = 0; k < n2; k++)
+    for (j = 0; j < n1; j++) {
+      double dmu = fabs(cos(x2m[j]) - cos(x2p[j]));
+      for (i = 0; i < n0; i++) {
+        double dVr = fabs(x1p[i] * x1p[i] * x1p[i] - x1m[i] * x1m[i] * x1m[i]) / 3.0;
+        s->dV[((size_t)k * n1 + j) * n0 + i] = dVr * dmu;
+      }
+      for (i = -1; i < n0; i++) {
+        double a = (i == -1) ? x1m[0] * x1m[0] * dmu : x1p[i] * x1p[i] * dmu;
+        s->Ax1[((size_t)k * n1 + j) * (n0 + 1) + (i + 1)] = a;
+      }
+    }
+    for (k = 0; k < n2; k++)
+    for (j = -1; j < n1; j++)
+    for (i = 0; i < n0; i++) {
+      double a = (j == -1) ? fabs(x1[i]) * dx1[i] * fabs(sin(x2m[0]))
+                           : fabs(x1[i]) * dx1[i] * fabs(sin(x2p[j]));
+      s->Ax2[((size_t)k * (n1 + 1) + (j + 1)) * n0 + i] = a;
+    }
+  }
+  for (d = 0; d < 3; d++) {
+    int nt = s->ntot[d];
+    double *dx = s->dx[d], *xgc = s->xgc[d], *xr = s->xr[d];
+    s->pcp[d] = calloc(nt, sizeof(double));
+    s->pcm[d] = calloc(nt, sizeof(double));
+    s->pwp[d] = calloc(nt, sizeof(double));
+    s->pwm[d] = calloc(nt, sizeof(double));
+    s->pdp[d] = calloc(nt, sizeof(double));
+    s->pdm[d] = calloc(nt, sizeof(double));
+    for (i = 1; i <= nt - 2; i++) {
+      s->pwp[d][i] = dx[i] / (xgc[i + 1] - xgc[i]);
+      s->pwm[d][i] = dx[i] / (xgc[i] - xgc[i - 1]);
+      s->pcp[d][i] = (xgc[i + 1] - xgc[i]) / (xr[i] - xgc[i]);
+      s->pcm[d][i] = (xgc[i] - xgc[i - 1]) / (xgc[i] - xr[i - 1]);
+      s->pdp[d][i] = (xr[i] - xgc[i]) / dx[i];
+      s->pdm[d][i] = (xgc[i] - xr[i - 1]) / dx[i];
+    }
+  }
+}
+
 /* ------------------------------------------------------------------ */
 /* lifecycle                                                           */
 /* ------------------------------------------------------------------ */
@@ -156,6 +272,10 @@ or_sim *or_create(const or_config *cfg)
   ROW1(s->rpress); ROW1(s->rpL); ROW1(s->rpR); ROW1(s->ra2L); ROW1(s->ra2R);
   ROW1(s->rcmax); ROW1(s->rSL); ROW1(s->rSR);
 #undef ROW1
+  s->rvc = calloc((size_t)(nmax + 2) * NVMAX, sizeof(double));
+  build_geometry(s);
+  s->xi_s = calloc(ncell, sizeof(double));
+  s->tr_s = calloc(ncell, sizeof(double));
   s->g_time = 0.0;
   s->g_dt = cfg->first_dt;
   s->step = 0;
@@ -170,8 +290,15 @@ void or_destroy(or_sim *s)
   if (!s) return;
   for (d = 0; d < 3; d++) {
     free(s->x[d]); free(s->xl[d]); free(s->xr[d]); free(s->dx[d]);
-    free(s->inv_dx[d]);
+    free(s->inv_dx[d]); free(s->xgc[d]);
+    free(s->pcp[d]); free(s->pcm[d]); free(s->pwp[d]); free(s->pwm[d]);
+    free(s->pdp[d]); free(s->pdm[d]);
   }
+  free(s->rt); free(s->sp); free(s->sn); free(s->dmu); free(s->dVr);
+  free(s->dV); free(s->Ax1); free(s->Ax2); free(s->rvc);
+  free(s->Fr); free(s->Ft); free(s->Fp); free(s->xi_s); free(s->tr_s);
+  free(s->dvds); free(s->roff); free(s->toff); free(s->moff);
+  free(s->x11[0]); free(s->x11[1]); free(s->x22[0]); free(s->x22[1]);
   free(s->V); free(s->U); free(s->U0); free(s->Cdt);
   free(s->rv); free(s->rvp); free(s->rvm); free(s->rup); free(s->rum);
   free(s->rdv); free(s->rflux); free(s->rrhs); free(s->rfL); free(s->rfR);
@@ -191,9 +318,12 @@ const double *or_grid(const or_sim *s, int dir, int which)
     case 0: return s->x[dir];
     case 1: return s->xl[dir];
     case 2: return s->xr[dir];
+    case 4: return s->xgc[dir];
     default: return s->dx[dir];
   }
 }
+
+const double *or_sirocco_xi(const or_sim *s) { return s->xi_s; }
 
 void or_time(const or_sim *s, double *t, double *dt, long *step)
 {
@@ -317,10 +447,134 @@ void or_init_blast(or_sim *s, double p_amb, double p_in, double r_in,
 /* boundary conditions (Src/boundary.c:56-760)                          */
 /* ------------------------------------------------------------------ */
 
+/* prim_to_cons is defined below; the floors need it */
+static inline void prim_to_cons(const double *v, double *u, int nvar, double gmm1);
+
+#define UNIT_P(s) ((s)->c.unit_density * (s)->c.unit_velocity * (s)->c.unit_velocity)
+#define UNIT_T(s) ((s)->c.unit_length / (s)->c.unit_velocity)
+#define UNIT_A(s) ((s)->c.unit_velocity * (s)->c.unit_velocity / (s)->c.unit_length)
+#define KELVIN_OF(s) ((s)->c.unit_velocity * (s)->c.unit_velocity * C_AMU / C_KB)
+
+/* Init() of the wind problem at one point (oracle/ref_cfg/wind2d/init.c) */
+static void wind_init_point(const or_sim *s, double *v, double x1, double x2)
+{
+  double gm_cgs = C_G * s->c.cent_mass;
+  double mu = s->c.mu, T = s->c.t_iso;
+  double r = x1 * s->c.unit_length;
+  double cs2 = C_RGAS * T / mu;
+  double tt = tan(x2);
+  double rho_d = s->c.rho_0 * exp(-gm_cgs / (2.0 * cs2 * r * tt * tt)) / s->c.unit_density;
+  double rho_a = s->c.dfloor / s->c.unit_density;
+  v[VX1] = 0.0;
+  v[VX2] = 0.0;
+  if (rho_d > rho_a) {
+    v[RHO] = rho_d;
+    v[NFLX] = 1.0;
+  } else {
+    v[RHO] = rho_a;
+    v[NFLX] = 0.0;
+  }
+  v[VX3] = sqrt(gm_cgs / r) * sin(x2) / s->c.unit_velocity;
+  v[PRS] = v[RHO] * T / (KELVIN_OF(s) * mu);
+}
+
+void or_init_wind(or_sim *s)
+{
+  int i, j, k, nv;
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  double v[NVMAX];
+  /* Startup(): Init() on every cell of the total box at the centroids */
+  for (k = 0; k < s->ntot[2]; k++)
+  for (j = 0; j < s->ntot[1]; j++)
+  for (i = 0; i < s->ntot[0]; i++) {
+    for (nv = 0; nv < NVMAX; nv++) v[nv] = 0.0;
+    wind_init_point(s, v, s->xgc[0][i], s->xgc[1][j]);
+    for (nv = 0; nv < s->c.nvar; nv++) s->V[nv * nc + cidx(s, k, j, i)] = v[nv];
+  }
+  /* read_sirocco_heatcool(flag = 0): frozen xi and radiation temperature */
+  for (k = s->beg[2]; k <= s->end[2]; k++)
+  for (j = s->beg[1]; j <= s->end[1]; j++)
+  for (i = s->beg[0]; i <= s->end[0]; i++) {
+    size_t c = cidx(s, k, j, i);
+    double rho = s->V[RHO * nc + c] * s->c.unit_density;
+    double r = s->x[0][i] * s->c.unit_length;
+    double nH = rho / (1.43 * C_MP);
+    double lx = s->c.l_star * s->c.f_x;
+    s->xi_s[c] = lx / nH / (r * r);
+    s->tr_s[c] = s->c.t_x;
+  }
+  s->dvds_ready = 0;
+}
+
+void or_set_flux(or_sim *s, int nangles, const double *fr, const double *ft, const double *fp)
+{
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  size_t n = nc * (size_t)nangles;
+  free(s->Fr); free(s->Ft); free(s->Fp);
+  free(s->dvds); free(s->roff); free(s->toff); free(s->moff);
+  s->na = nangles;
+  s->Fr = malloc(n * sizeof(double));
+  s->Ft = malloc(n * sizeof(double));
+  s->Fp = malloc(n * sizeof(double));
+  memcpy(s->Fr, fr, n * sizeof(double));
+  memcpy(s->Ft, ft, n * sizeof(double));
+  memcpy(s->Fp, fp, n * sizeof(double));
+  s->dvds = calloc(n, sizeof(double));
+  s->roff = calloc(n, sizeof(double));
+  s->toff = calloc(n, sizeof(double));
+  s->moff = calloc(n, sizeof(double));
+  s->dvds_ready = 0;
+}
+
+/* UserDefBoundary(side == 0) of the wind problem: density and pressure
+ * floors on every cell, with the conservative state of a repaired cell
+ * rebuilt (PrimToCons3D on that cell). */
+static void wind_floors(or_sim *s)
+{
+  int i, j, k, nv, nvar = s->c.nvar;
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  double mu = s->c.mu, K = KELVIN_OF(s);
+  double dfloor = s->c.dfloor / s->c.unit_density;
+  double tfloor = 5.e2;
+  double pfloor = dfloor * tfloor / (K * mu);
+  double gmm1 = s->c.gamma - 1.0, v[NVMAX];
+  for (k = 0; k < s->ntot[2]; k++)
+  for (j = 0; j < s->ntot[1]; j++)
+  for (i = 0; i < s->ntot[0]; i++) {
+    size_t c = cidx(s, k, j, i);
+    double *V = s->V;
+    int convert = 0;
+    if (V[RHO * nc + c] < dfloor) {
+      double cs, dfact, temp;
+      if (V[RHO * nc + c] < 0.0) V[RHO * nc + c] = dfloor;
+      cs = sqrt(s->c.gamma * V[PRS * nc + c] / V[RHO * nc + c]);
+      dfact = V[RHO * nc + c] / dfloor;
+      V[RHO * nc + c] = dfloor;
+      V[VX1 * nc + c] = dfact * V[VX1 * nc + c];
+      V[VX2 * nc + c] = dfact * V[VX2 * nc + c];
+      V[VX3 * nc + c] = dfact * V[VX3 * nc + c];
+      V[PRS * nc + c] = cs * cs * V[RHO * nc + c] / s->c.gamma;
+      temp = V[PRS * nc + c] / V[RHO * nc + c] * K * mu;
+      if (temp < tfloor) V[PRS * nc + c] = V[RHO * nc + c] * tfloor / (K * mu);
+      V[NFLX * nc + c] = 0.0;
+      convert = 1;
+    }
+    if (V[PRS * nc + c] < pfloor) {
+      V[PRS * nc + c] = pfloor;
+      convert = 1;
+    }
+    if (convert) {
+      for (nv = 0; nv < nvar; nv++) v[nv] = V[nv * nc + c];
+      prim_to_cons(v, &s->U[c * nvar], nvar, gmm1);
+    }
+  }
+}
+
 static void boundary(or_sim *s)
 {
   int side, nv, i, j, k;
   int nvar = s->c.nvar;
+  if (s->c.floors) wind_floors(s);
   for (side = 0; side < 6; side++) {
     int d = side / 2, isend = side % 2;
     int type = s->c.bc[side];
@@ -355,8 +609,15 @@ static void boundary(or_sim *s)
                  type == OR_BC_EQTSYMMETRIC) {
         int i0 = isend ? 2 * s->end[d] + 1 : 2 * s->beg[d] - 1;
         src[d] = i0 - idx;
+      } else if (type == OR_BC_USERDEF && side == 0) {
+        /* wind problem, X1_BEG: copy the first active cell, inflow only */
+        src[0] = s->beg[0];
+        val = s->V[vidx(s, nv, src[2], src[1], src[0])];
+        if (nv == VX1) val = MIND(val, 0.0);
+        s->V[vidx(s, nv, k, j, i)] = val;
+        continue;
       } else {
-        continue; /* user-defined sides are filled by the caller */
+        continue;
       }
       val = s->V[vidx(s, nv, src[2], src[1], src[0])];
       if (type == OR_BC_OUTFLOW || type == OR_BC_PERIODIC)
@@ -437,6 +698,241 @@ static inline double limit(int lim, double dvp, double dvm)
   return dv;
 }
 
+/* Limiters on irregular or curvilinear grids (Src/States/plm_coeffs.h:128-150) */
+static inline double limit_general(int lim, double dvp, double dvm, double cp, double cm)
+{
+  double dv;
+  if (lim == OR_LIM_MC) {
+    if (dvp * dvm > 0.0) {
+      double qc = 0.5 * ((dvm) + (dvp)), scrh = ABS_MIN((dvp) * cp, (dvm) * cm);
+      dv = ABS_MIN(qc, scrh);
+    } else dv = 0.0;
+  } else if (lim == OR_LIM_VL) {
+    dv = (dvp * dvm > 0.0 ? (dvp) * (dvm) * (cp * (dvm) + cm * (dvp)) /
+                                ((dvp) * (dvp) + (dvm) * (dvm) + (cp + cm - 2.0) * (dvp) * (dvm))
+                          : 0.0);
+  } else {
+    dv = (dvp * dvm > 0.0 ? ABS_MIN(dvp, dvm) : 0.0);
+  }
+  return dv;
+}
+
+/* ------------------------------------------------------------------ */
+/* line force (Src/LineDriven/line_connect.c)                         */
+/* ------------------------------------------------------------------ */
+
+#define AIDX(s, a, c) ((size_t)(a) * (size_t)(s)->ntot[0] * (s)->ntot[1] * (s)->ntot[2] + (c))
+
+static void bilinear(const double x11[2], const double x22[2], const double v11[2],
+                     const double v12[2], const double v21[2], const double v22[2],
+                     const double test[2], double ans[2])
+{
+  double fracx1 = (test[0] - x11[0]) / (x22[0] - x11[0]);
+  double fracx2 = (test[1] - x11[1]) / (x22[1] - x11[1]);
+  double temp1 = (1.0 - fracx1) * v11[0] + fracx1 * v21[0];
+  double temp2 = (1.0 - fracx1) * v12[0] + fracx1 * v22[0];
+  ans[0] = (1.0 - fracx2) * temp1 + fracx2 * temp2;
+  temp1 = (1.0 - fracx1) * v11[1] + fracx1 * v21[1];
+  temp2 = (1.0 - fracx1) * v12[1] + fracx1 * v22[1];
+  ans[1] = (1.0 - fracx2) * temp1 + fracx2 * temp2;
+}
+
+/* VGradCalc (line_connect.c:504-742): dv/ds along every flux bin.  Returns
+ * nonzero if a NaN appears (the reference exits the program there). */
+static int vgrad_calc(or_sim *s)
+{
+  int i, j, k, a;
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  const double UL = s->c.unit_length, UV = s->c.unit_velocity;
+  double *x1 = s->x[0], *x2 = s->x[1];
+  double *V1 = s->V + VX1 * nc, *V2 = s->V + VX2 * nc;
+  if (!s->dvds_ready) {
+    for (a = 0; a < 2; a++) {
+      free(s->x11[a]); free(s->x22[a]);
+      s->x11[a] = calloc(nc, sizeof(double));
+      s->x22[a] = calloc(nc, sizeof(double));
+    }
+    for (a = 0; a < s->na; a++) {
+      for (k = s->beg[2]; k <= s->end[2]; k++)
+      for (j = s->beg[1]; j <= s->end[1]; j++)
+      for (i = s->beg[0]; i <= s->end[0]; i++) {
+        size_t c = cidx(s, k, j, i), q = AIDX(s, a, c);
+        double maxds, mod_flux;
+        s->x11[0][c] = (x1[i - 1] + x1[i]) / 2.0 * UL;
+        s->x11[1][c] = (x2[j - 1] + x2[j]) / 2.0;
+        s->x22[0][c] = (x1[i + 1] + x1[i]) / 2.0 * UL;
+        s->x22[1][c] = (x2[j + 1] + x2[j]) / 2.0;
+        maxds = fabs(s->x22[0][c] - s->x11[0][c]);
+        if (maxds > (x1[i] * UL * fabs(s->x22[1][c] - s->x11[1][c])))
+          maxds = x1[i] * UL * fabs(s->x22[1][c] - s->x11[1][c]);
+        maxds /= 2.0;
+        mod_flux = sqrt(pow(s->Fr[q], 2) + pow(s->Ft[q], 2) + pow(s->Fp[q], 2));
+        if (mod_flux == 0.0) {
+          s->moff[q] = -999;
+        } else {
+          double x = x1[i] * sin(x2[j]) * UL;
+          double z = x1[i] * cos(x2[j]) * UL;
+          double th = (a + 0.5) * (2.0 * C_PI) / 36.0;
+          double dx1 = maxds * sin(th), dx2 = maxds * cos(th);
+          double ds = sqrt(dx1 * dx1 + dx2 * dx2);
+          s->roff[q] = sqrt((x + dx1) * (x + dx1) + (z + dx2) * (z + dx2));
+          s->toff[q] = atan((x + dx1) / (z + dx2));
+          s->moff[q] = ds;
+        }
+      }
+    }
+    s->dvds_ready = 1;
+  }
+  for (a = 0; a < s->na; a++) {
+    for (k = s->beg[2]; k <= s->end[2]; k++)
+    for (j = s->beg[1]; j <= s->end[1]; j++)
+    for (i = s->beg[0]; i <= s->end[0]; i++) {
+      size_t c = cidx(s, k, j, i), q = AIDX(s, a, c);
+      size_t cjm = cidx(s, k, j - 1, i), cjp = cidx(s, k, j + 1, i);
+      double v11[2], v12[2], v21[2], v22[2], x11[2], x22[2], loc[2], ans1[2], ans2[2];
+      double vx1, vz1, ds;
+      v11[0] = (V1[cjm - 1] + V1[cjm] + V1[c - 1] + V1[c]) / 4.0;
+      v11[1] = (V2[cjm - 1] + V2[cjm] + V2[c - 1] + V2[c]) / 4.0;
+      v12[0] = (V1[cjp - 1] + V1[c - 1] + V1[cjp] + V1[c]) / 4.0;
+      v12[1] = (V2[cjp - 1] + V2[c - 1] + V2[cjp] + V2[c]) / 4.0;
+      v22[0] = (V1[cjp] + V1[cjp + 1] + V1[c + 1] + V1[c]) / 4.0;
+      v22[1] = (V2[cjp] + V2[cjp + 1] + V2[c + 1] + V2[c]) / 4.0;
+      v21[0] = (V1[c + 1] + V1[cjm + 1] + V1[cjm] + V1[c]) / 4.0;
+      v21[1] = (V2[c + 1] + V2[cjm + 1] + V2[cjm] + V2[c]) / 4.0;
+      x11[0] = s->x11[0][c]; x11[1] = s->x11[1][c];
+      x22[0] = s->x22[0][c]; x22[1] = s->x22[1][c];
+      loc[0] = x1[i] * UL;
+      loc[1] = x2[j];
+      bilinear(x11, x22, v11, v12, v21, v22, loc, ans1);
+      vx1 = (ans1[0] * UV * sin(x2[j]) + ans1[1] * UV * cos(x2[j]));
+      vz1 = (ans1[0] * UV * cos(x2[j]) - ans1[1] * UV * sin(x2[j]));
+      loc[0] = s->roff[q];
+      loc[1] = s->toff[q];
+      ds = s->moff[q];
+      if (ds == -999) {
+        s->dvds[q] = -999;
+      } else {
+        double vx2, vz2, th, v1, v2;
+        bilinear(x11, x22, v11, v12, v21, v22, loc, ans2);
+        vx2 = (ans2[0] * UV * sin(loc[1]) + ans2[1] * UV * cos(loc[1]));
+        vz2 = (ans2[0] * UV * cos(loc[1]) - ans2[1] * UV * sin(loc[1]));
+        th = (a + 0.5) * (2.0 * C_PI) / 36.0;
+        v1 = sin(th) * vx1 + cos(th) * vz1;
+        v2 = sin(th) * vx2 + cos(th) * vz2;
+        s->dvds[q] = fabs((v2 - v1) / ds);
+      }
+      if (s->dvds[q] != s->dvds[q]) return 1;
+    }
+  }
+  return 0;
+}
+
+/* LineForce (line_connect.c:815-903), power-law force multiplier */
+static void line_force(const or_sim *s, const double *v, size_t c, double *grad)
+{
+  const double sigma_e = C_SIGMAT / C_AMU / 1.18;
+  double rho = v[RHO] * s->c.unit_density;
+  double mu = s->c.mu, krad = s->c.krad, alpharad = s->c.alpharad;
+  double M_max = 4400.;
+  double T = v[PRS] / v[RHO] * KELVIN_OF(s) * mu;
+  double v_th = sqrt((2.0 * C_KB * T) / C_MP);
+  double UA = UNIT_A(s);
+  int a;
+  grad[0] = 0.0;
+  grad[1] = 0.0;
+  grad[2] = 0.0;
+  for (a = 0; a < s->na; a++) {
+    size_t q = AIDX(s, a, c);
+    double flux_r = s->Fr[q], flux_t = s->Ft[q], M_UV;
+    if (s->dvds[q] > 0.0) {
+      double t_UV = sigma_e * rho * v_th / s->dvds[q];
+      M_UV = krad * pow(t_UV, alpharad);
+      if (M_UV > M_max) M_UV = M_max;
+    } else {
+      M_UV = 0.0;
+    }
+    grad[0] += ((1.0 + M_UV) * sigma_e * flux_r / C_C) / UA;
+    grad[1] += ((1.0 + M_UV) * sigma_e * flux_t / C_C) / UA;
+  }
+}
+
+/* Curvilinear right-hand side of one row: total flux times area, flux
+ * difference over the volume, pressure gradient, angular-momentum form of
+ * the phi momentum (rhs.c:234-351, 423-630), then the geometric, gravity
+ * and line-force sources (rhs_source.c:101-420) with the face-averaged
+ * state in x1 and the cell-centred state in x2. */
+static void sph_rhs(or_sim *s, int d, int k0, int j0, int i0, double dt)
+{
+  int nvar = s->c.nvar, nbeg = s->beg[d], nend = s->end[d], i, nv;
+  int n0 = s->ntot[0], n1 = s->ntot[1];
+  double *fl = s->rflux, *rhs = s->rrhs, *pr = s->rpress, *vp = s->rvp, *vm = s->rvm;
+  double *v = s->rv;
+  double fA[2][NVMAX];
+  double gm_code = C_G * s->c.cent_mass /
+                   (s->c.unit_length * s->c.unit_velocity * s->c.unit_velocity);
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  (void)nc;
+  for (i = nbeg; i <= nend; i++) {
+    int ii = d == 0 ? i : i0, jj = d == 1 ? i : j0;
+    size_t c = cidx(s, k0, jj, ii);
+    double dtdV = dt / s->dV[c], dtdl, vc[NVMAX], grad[3], g0;
+    for (int side = 0; side < 2; side++) {
+      int f = i - 1 + side; /* face f+1/2 */
+      double A;
+      if (d == 0) A = s->Ax1[((size_t)k0 * n1 + j0) * (n0 + 1) + (f + 1)];
+      else        A = s->Ax2[((size_t)k0 * (n1 + 1) + (f + 1)) * n0 + i0];
+      for (nv = 0; nv < nvar; nv++) fA[side][nv] = R(fl, f, nv) * A;
+      if (d == 0) fA[side][VX3] *= fabs(s->xr[0][f]);
+      else        fA[side][VX3] *= fabs(s->sp[f]);
+    }
+    if (d == 0) dtdl = dt / s->dx[0][i];
+    else        dtdl = dt / s->dx[1][i] * (1.0 / s->rt[i0]);
+    for (nv = 0; nv < nvar; nv++) R(rhs, i, nv) = -dtdV * (fA[1][nv] - fA[0][nv]);
+    R(rhs, i, VX1 + d) -= dtdl * (pr[i] - pr[i - 1]);
+    if (d == 0) R(rhs, i, VX3) /= fabs(s->x[0][i]);
+    else        R(rhs, i, VX3) /= fabs(s->sn[i]);
+
+    if (d == 0) {
+      double r_1 = 1.0 / s->x[0][i], vphi, Sm;
+      for (nv = 0; nv < nvar; nv++) vc[nv] = 0.5 * (R(vp, i, nv) + R(vm, i, nv));
+      vphi = vc[VX3];
+      Sm = vc[RHO] * (vc[VX2] * vc[VX2] + vphi * vphi);
+      R(rhs, i, VX1) += dt * Sm * r_1;
+      if (s->c.body_force) {
+        g0 = -1.0 * gm_code / (s->x[0][i] * s->x[0][i]);
+        R(rhs, i, VX1) += dt * vc[RHO] * g0;
+        R(rhs, i, PRS) += dt * 0.5 * (R(fl, i, RHO) + R(fl, i - 1, RHO)) * g0;
+      }
+      if (s->c.line_force) {
+        line_force(s, vc, c, grad);
+        R(rhs, i, VX1) += dt * vc[RHO] * grad[0];
+        R(rhs, i, PRS) += dt * 0.5 * (R(fl, i, RHO) + R(fl, i - 1, RHO)) * grad[0];
+      }
+    } else {
+      double r_1 = 1.0 / s->rt[i0], ct = 1.0 / tan(s->x[1][i]), vphi, Sm;
+      for (nv = 0; nv < nvar; nv++) vc[nv] = R(v, i, nv);
+      vphi = vc[VX3];
+      Sm = vc[RHO] * (-vc[VX2] * vc[VX1] + ct * vphi * vphi);
+      Sm += 0.0 - ct * 0.0;
+      R(rhs, i, VX2) += dt * Sm * r_1;
+      if (s->c.body_force) {
+        double g1 = 0.0, g2 = 0.0;
+        R(rhs, i, VX2) += dt * vc[RHO] * g1;
+        R(rhs, i, PRS) += dt * 0.5 * (R(fl, i, RHO) + R(fl, i - 1, RHO)) * g1;
+        R(rhs, i, VX3) += dt * vc[RHO] * g2;
+        R(rhs, i, PRS) += dt * vc[RHO] * vc[VX3] * g2;
+      }
+      if (s->c.line_force) {
+        line_force(s, vc, c, grad);
+        R(rhs, i, VX2) += dt * vc[RHO] * grad[1];
+        R(rhs, i, PRS) += dt * 0.5 * (R(fl, i, RHO) + R(fl, i - 1, RHO)) * grad[1];
+        R(rhs, i, VX3) += dt * vc[RHO] * grad[2];
+        R(rhs, i, PRS) += dt * vc[RHO] * vc[VX3] * grad[2];
+      }
+    }
+  }
+}
+
 static void row_sweep(or_sim *s, int d, int k0, int j0, int i0, int stage,
                       double dt)
 {
@@ -466,11 +962,22 @@ static void row_sweep(or_sim *s, int d, int k0, int j0, int i0, int stage,
   for (i = beg - 1; i <= end; i++)
     for (nv = 0; nv < nvar; nv++) R(dvv, i, nv) = R(v, i + 1, nv) - R(v, i, nv);
   for (i = beg; i <= end; i++) {
-    for (nv = 0; nv < nvar; nv++) {
-      double dvp = R(dvv, i, nv), dvm = R(dvv, i - 1, nv);
-      double dvl = limit(s->c.limiter, dvp, dvm);
-      R(vp, i, nv) = R(v, i, nv) + dvl * 0.5;
-      R(vm, i, nv) = R(v, i, nv) - dvl * 0.5;
+    if (s->c.geometry == OR_CARTESIAN) {
+      for (nv = 0; nv < nvar; nv++) {
+        double dvp = R(dvv, i, nv), dvm = R(dvv, i - 1, nv);
+        double dvl = limit(s->c.limiter, dvp, dvm);
+        R(vp, i, nv) = R(v, i, nv) + dvl * 0.5;
+        R(vm, i, nv) = R(v, i, nv) - dvl * 0.5;
+      }
+    } else {
+      double cp = s->pcp[d][i], cm = s->pcm[d][i], wp = s->pwp[d][i], wm = s->pwm[d][i];
+      double dp = s->pdp[d][i], dm = s->pdm[d][i];
+      for (nv = 0; nv < nvar; nv++) {
+        double dvp = R(dvv, i, nv) * wp, dvm = R(dvv, i - 1, nv) * wm;
+        double dvl = limit_general(s->c.limiter, dvp, dvm, cp, cm);
+        R(vp, i, nv) = R(v, i, nv) + dvl * dp;
+        R(vm, i, nv) = R(v, i, nv) - dvl * dm;
+      }
     }
     prim_to_cons(&R(vp, i, 0), &R(up, i, 0), nvar, gmm1);
     prim_to_cons(&R(vm, i, 0), &R(um, i, 0), nvar, gmm1);
@@ -553,12 +1060,16 @@ static void row_sweep(or_sim *s, int d, int k0, int j0, int i0, int stage,
     }
   }
 
-  /* right-hand side (rhs.c:188-209, Cartesian) and update */
-  for (i = nbeg; i <= nend; i++) {
-    double scrh = dt / s->dx[d][i];
-    for (nv = 0; nv < nvar; nv++)
-      R(rhs, i, nv) = -scrh * (R(fl, i, nv) - R(fl, i - 1, nv));
-    R(rhs, i, vn) -= scrh * (pr[i] - pr[i - 1]);
+  if (s->c.geometry == OR_CARTESIAN) {
+    /* right-hand side (rhs.c:188-209, Cartesian) */
+    for (i = nbeg; i <= nend; i++) {
+      double scrh = dt / s->dx[d][i];
+      for (nv = 0; nv < nvar; nv++)
+        R(rhs, i, nv) = -scrh * (R(fl, i, nv) - R(fl, i - 1, nv));
+      R(rhs, i, vn) -= scrh * (pr[i] - pr[i - 1]);
+    }
+  } else {
+    sph_rhs(s, d, k0, j0, i0, dt);
   }
   for (i = nbeg; i <= nend; i++) {
     size_t c = base + i * stride;
@@ -568,9 +1079,13 @@ static void row_sweep(or_sim *s, int d, int k0, int j0, int i0, int stage,
   /* inverse time step (update_stage.c:303-324) */
   if (stage == 1) {
     if (s->c.dims > 1) {
+      double r_1 = 1.0;
+      if (s->c.geometry == OR_SPHERICAL && d == 1) r_1 = 1.0 / s->x[0][i0];
       for (i = nbeg; i <= nend; i++) {
         size_t c = base + i * stride;
-        s->Cdt[c] += 0.5 * (cmax[i - 1] + cmax[i]) * s->inv_dx[d][i] * 1.0;
+        double inv_dl = (s->c.geometry == OR_SPHERICAL && d == 1) ? s->inv_dx[d][i] * r_1
+                                                                  : s->inv_dx[d][i];
+        s->Cdt[c] += 0.5 * (cmax[i - 1] + cmax[i]) * inv_dl * 1.0;
       }
     } else {
       for (i = nbeg - 1; i <= nend; i++)
@@ -584,6 +1099,7 @@ static void update_stage(or_sim *s, int stage, double dt)
   int d, i, j, k;
   size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
   if (stage == 1) memset(s->Cdt, 0, nc * sizeof(double));
+  if (s->c.line_force && vgrad_calc(s)) s->fail |= 1024;
   for (d = 0; d < s->c.dims; d++) {
     int lo[3], hi[3];
     for (int q = 0; q < 3; q++) { lo[q] = s->beg[q]; hi[q] = s->end[q]; }
@@ -629,6 +1145,175 @@ static int cons_to_prim_dom(or_sim *s)
     for (nv = 0; nv < nvar; nv++) s->V[nv * nc + c] = v[nv];
   }
   return flags;
+}
+
+/* ------------------------------------------------------------------ */
+/* BLONDIN heating/cooling (Src/Cooling/BLONDIN/cooling.c:50-319)      */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+  double xi, sqxi, sqsqxi, nH, n, tx, E, hc_init, dt_share;
+  double comp_c_pre, comp_h_pre, line_c_pre, brem_c_pre, xray_h_pre;
+} bl_ctx;
+
+static double bl_ne_rat(double T)
+{
+  double ne_ratio;
+  if (T < 1.5e4) {
+    ne_ratio = 1e-2 + pow(10, (-51.59417133 + 12.27740153 * log10(T)));
+  } else if (T >= 1.5e4 && T < 3.3e4) {
+    ne_ratio = pow(10, (-3.80749689 + 0.86092628 * log10(T)));
+  } else {
+    ne_ratio = 1.21;
+  }
+  return ne_ratio;
+}
+
+static double bl_heatcool(const bl_ctx *b, double T)
+{
+  double sqT = sqrt(T);
+  double ne = b->nH * bl_ne_rat(T);
+  double comp_heat = b->comp_h_pre * (8.9e-36 * b->xi * b->tx);
+  double comp_cool = b->comp_c_pre * (8.9e-36 * b->xi * (4.0 * T));
+  double xray_heat = b->xray_h_pre * (1.5e-21 * (b->sqsqxi / sqT));
+  double line_cool = b->line_c_pre * ((1e-16 * exp(-1.3e5 / T) / b->sqxi / T) +
+                                      fmin(fmin(1e-24, 5e-27 * sqT), 1.5e-17 / T));
+  double brem_cool = b->brem_c_pre * (3.3e-27 * sqT);
+  return b->nH * (ne * comp_heat + b->nH * xray_heat - ne * comp_cool - ne * line_cool -
+                  ne * brem_cool);
+}
+
+static double bl_zfunc(const bl_ctx *b, double temp)
+{
+  return (temp * b->n * C_KB / (2.0 / 3.0)) - b->E -
+         b->dt_share * (b->hc_init + bl_heatcool(b, temp)) / 2.0;
+}
+
+/* which: 0 = zfunc, 1 = heatcool */
+static double bl_func(const bl_ctx *b, int which, double x)
+{
+  return which == 0 ? bl_zfunc(b, x) : bl_heatcool(b, x);
+}
+
+/* Brent's method as in the reference (ITMAX 100, EPS 3e-8) */
+static double bl_zbrent(const bl_ctx *bc, int which, double x1, double x2, double tol)
+{
+  const double EPS = 3.0e-8;
+  int iter;
+  double a = x1, b = x2, c = x2;
+  double d = 0.0, e = 0.0;
+  double fa = bl_func(bc, which, a), fb = bl_func(bc, which, b), fc = fb;
+  double p, q, r, sv, tol1, xm;
+  if (fb * fa > 0.0) return b;
+  for (iter = 1; iter <= 100; iter++) {
+    if (fb * fc > 0.0) {
+      c = a;
+      fc = fa;
+      e = d = b - a;
+    }
+    if (fabs(fc) < fabs(fb)) {
+      a = b;
+      b = c;
+      c = a;
+      fa = fb;
+      fb = fc;
+      fc = fa;
+    }
+    tol1 = 2.0 * EPS * fabs(b) + 0.5 * tol;
+    xm = 0.5 * (c - b);
+    if (fabs(xm) <= tol1 || fb == 0.0) return b;
+    if (fabs(e) >= tol1 && fabs(fa) > fabs(fb)) {
+      sv = fb / fa;
+      if (a == c) {
+        p = 2.0 * xm * sv;
+        q = 1.0 - sv;
+      } else {
+        q = fa / fc;
+        r = fb / fc;
+        p = sv * (2.0 * xm * q * (q - r) - (b - a) * (r - 1.0));
+        q = (q - 1.0) * (r - 1.0) * (sv - 1.0);
+      }
+      if (p > 0.0) q = -q;
+      p = fabs(p);
+      double min1 = 3.0 * xm * q - fabs(tol1 * q);
+      double min2 = fabs(e * q);
+      if (2.0 * p < (min1 < min2 ? min1 : min2)) {
+        e = d;
+        d = p / q;
+      } else {
+        d = xm;
+        e = d;
+      }
+    } else {
+      d = xm;
+      e = d;
+    }
+    a = b;
+    fa = fb;
+    if (fabs(d) > tol1)
+      b += d;
+    else
+      b += (xm > 0.0 ? fabs(tol1) : -fabs(tol1));
+    fb = bl_func(bc, which, b);
+  }
+  return b;
+}
+
+void or_cooling(or_sim *s, double dt, double t)
+{
+  int i, j, k;
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  double lx = s->c.l_star * s->c.f_x, mu = s->c.mu;
+  double g_minCoolingTemp = 1.e4;
+  bl_ctx b;
+  memset(&b, 0, sizeof(b));
+  b.dt_share = dt * UNIT_T(s);
+  b.comp_c_pre = b.comp_h_pre = b.line_c_pre = b.brem_c_pre = b.xray_h_pre = 1.0;
+  for (k = s->beg[2]; k <= s->end[2]; k++)
+  for (j = s->beg[1]; j <= s->end[1]; j++)
+  for (i = s->beg[0]; i <= s->end[0]; i++) {
+    size_t c = cidx(s, k, j, i);
+    double r = s->x[0][i] * s->c.unit_length;
+    double rho = s->V[RHO * nc + c] * s->c.unit_density;
+    double p = s->V[PRS * nc + c], T, T_f, t_l, t_u, test, E_f, p_f;
+    T = p / s->V[RHO * nc + c] * KELVIN_OF(s) * mu;
+    (void)T;
+    b.E = (p * UNIT_P(s)) / (s->c.gamma - 1);
+    b.nH = rho / (1.43 * C_MP);
+    if (t <= 3.0) {
+      b.xi = lx / b.nH / r / r;
+      b.tx = s->c.t_x;
+    } else {
+      b.xi = s->xi_s[c];
+      b.tx = s->tr_s[c];
+    }
+    b.n = rho / (mu * C_MP);
+    T = b.E * (2.0 / 3.0) / (b.n * C_KB);
+    if (T < g_minCoolingTemp) continue;
+    b.sqxi = sqrt(b.xi);
+    b.sqsqxi = pow(b.xi, 0.25);
+    b.hc_init = bl_heatcool(&b, T);
+    t_l = T * 0.9;
+    t_u = T * 1.1;
+    test = bl_zfunc(&b, t_l) * bl_zfunc(&b, t_u);
+    while (test > 0 && test == test) {
+      t_l *= 0.9;
+      t_u *= 1.1;
+      test = bl_zfunc(&b, t_l) * bl_zfunc(&b, t_u);
+    }
+    if (test != test) {
+      T_f = T;
+    } else {
+      double hc_final;
+      T_f = bl_zbrent(&b, 0, t_l, t_u, 1.0);
+      hc_final = bl_heatcool(&b, T_f);
+      if (hc_final * b.hc_init < 0.0) T_f = bl_zbrent(&b, 1, fmin(T_f, T), fmax(T_f, T), 1.0);
+    }
+    T_f = MAXD(T_f, g_minCoolingTemp);
+    E_f = T_f / (2.0 / 3.0) * (b.n * C_KB);
+    p_f = E_f * (s->c.gamma - 1) / UNIT_P(s);
+    s->V[PRS * nc + c] = p_f;
+  }
 }
 
 /* RK2 AdvanceStep (rk_step.c:29-384) */
@@ -693,8 +1378,12 @@ int or_run(or_sim *s, int nsteps)
       s->invDt_hyp = 0.0;
       s->dt_cool = 1.e38;
     }
+    /* Strang alternation of the split source (main.c:479-485) */
+    if (s->c.cooling && s->step % 2 != 0) or_cooling(s, s->g_dt, s->g_time);
     flags = advance_step(s);
     if (flags & 64) s->fail |= flags;
+    if (s->c.cooling && s->step % 2 == 0) or_cooling(s, s->g_dt, s->g_time);
+    if (s->fail & 1024) return 3;
     s->hist_dt[s->nhist] = s->g_dt;
     s->hist_inv[s->nhist] = s->invDt_hyp;
     s->nhist++;

@@ -43,6 +43,13 @@ typedef struct {
   double gamma;
   double cfl, cfl_max_var, tstop, first_dt;
   int    cooling;       /* 0: none; 1: BLONDIN split source (Strang rules)  */
+  /* line-driven disk wind (all zero for the plain hydro configurations) */
+  int    body_force;    /* point-mass gravity (BodyForceVector)            */
+  int    line_force;    /* VGradCalc + LineForce                           */
+  int    floors;        /* internal-boundary density/pressure floors       */
+  double unit_density, unit_length, unit_velocity;
+  double mu, rho_0, cent_mass, t_iso, l_star, f_x, f_uv, t_x;
+  double krad, alpharad, dfloor;
 } or_config;
 
 typedef struct or_sim or_sim;
@@ -53,7 +60,7 @@ void    or_destroy(or_sim *s);
 /* Geometry of the total box (ngh ghosts each side of active dirs). */
 int     or_ntot(const or_sim *s, int dir);
 int     or_nghost(const or_sim *s, int dir);
-/* which: 0 = x (centre), 1 = xl, 2 = xr, 3 = dx */
+/* which: 0 = x (centre), 1 = xl, 2 = xr, 3 = dx, 4 = xgc (centroid) */
 const double *or_grid(const or_sim *s, int dir, int which);
 
 /* Primitive state [nv][k][j][i] over the total box (read/write). */
@@ -66,9 +73,20 @@ double *or_state(or_sim *s);
 void    or_init_blast(or_sim *s, double p_amb, double p_in, double r_in,
                       double noise, long seed);
 
+/* Line-driven wind: initial condition of the wind problem (Init() called
+ * on every cell of the total box at the volume centroids, as Startup does)
+ * followed by read_sirocco_heatcool(flag = 0): frozen xi and T_r. */
+void    or_init_wind(or_sim *s);
+
+/* Directional UV fluxes, [angle][k][j][i] over the total box, for the
+ * line force (flux_r_UV / flux_t_UV / flux_p_UV, Src/globals.h:191-210). */
+void    or_set_flux(or_sim *s, int nangles, const double *fr, const double *ft,
+                    const double *fp);
+
 /* Run `nsteps` steps of the main loop (Src/main.c:215-337 semantics).
  * Returns 0 on success, 1 if dt became too small (NextTimeStep abort),
- * 2 if a ConsToPrim failure flag was raised. */
+ * 2 if a ConsToPrim failure flag was raised, 3 if dv/ds became NaN
+ * (the reference exits there). */
 int     or_run(or_sim *s, int nsteps);
 
 void    or_time(const or_sim *s, double *t, double *dt, long *step);
@@ -77,6 +95,14 @@ void    or_set_time(or_sim *s, double t, double dt, long step);
 /* Per-step record of the last or_run: dt used by each step and the
  * invDt_hyp the stage-1 reduction produced.  Returns count copied. */
 int     or_history(const or_sim *s, double *dt_used, double *inv_dt, int max);
+
+/* One BLONDIN cooling pass over the active cells with the given dt and
+ * simulation time (BlondinCooling, Src/Cooling/BLONDIN/cooling.c:50-165). */
+void    or_cooling(or_sim *s, double dt, double t);
+
+/* Frozen ionisation parameter and radiation temperature per cell
+ * ([k][j][i], total box). */
+const double *or_sirocco_xi(const or_sim *s);
 
 #ifdef __cplusplus
 }
