@@ -28,10 +28,12 @@ def built():
     return True
 
 
-def golden_cases(full_only=False):
+def golden_cases(full_only=False, kind="blast"):
     out = []
     for f in sorted(glob.glob(os.path.join(GOLDEN, "*.json"))):
         meta = json.load(open(f))
+        if meta.get("kind", "blast") != kind:
+            continue
         npz = f[:-5] + ".npz"
         meta["npz"] = npz if os.path.exists(npz) else None
         if full_only and meta["npz"] is None:

@@ -26,6 +26,67 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 ORACLE = os.path.join(ROOT, "oracle")
+sys.path.insert(0, ORACLE)
+sys.path.insert(0, os.path.join(ROOT, "pluto-sirocco_gb300"))
+
+WIND_INI = """[Grid]
+
+X1-grid    1    10.0   {nr}    l+   1000.0
+X2-grid    1    0.0    {nt}    u    1.5707963267948966
+X3-grid    1    0.0    1     u    1.0
+
+[Time]
+
+CFL              0.4
+CFL_max_var      1.1
+tstop            1.e10
+first_dt         1.e-4
+
+[Solver]
+
+Solver         hll
+
+[Boundary]
+
+X1-beg        userdef
+X1-end        outflow
+X2-beg        axisymmetric
+X2-end        reflective
+X3-beg        outflow
+X3-end        outflow
+
+[Static Grid Output]
+
+uservar    0
+dbl       -1.0  {every}   single_file
+flt       -1.0  -1   single_file
+vtk       -1.0  -1   single_file
+dbl.h5    -1.0  -1
+flt.h5    -1.0  -1
+tab       -1.0  -1
+ppm       -1.0  -1
+png       -1.0  -1
+log        {every}
+analysis  -1.0  -1
+
+[Parameters]
+
+MU                          0.6
+RHO_0                       1.0e-9
+R_0                         1.0e10
+RHO_ALPHA                   1.5
+CENT_MASS                   1.4e34
+DISK_MDOT                   1.0e-8
+T_ISO                       4.0e4
+L_star                      1.0e37
+f_x                         1.0
+f_uv                        1.0
+T_x                         5.6e7
+KRAD                        0.2
+ALPHARAD                    -0.6
+DFLOOR                      1.0e-20
+GAMMA                       1.6666666666666667
+"""
 
 INI = """[Grid]
 
@@ -126,14 +187,77 @@ def run_case(ref, name, cfg, dims, n, solver, bc, steps, full):
     print(name, "t =", t_s, "dt =", dt_s)
 
 
+def write_flux_files(wd, nr, nt):
+    """directional_flux_{r,theta,phi}.dat in the format read by
+    read_sirocco_fluxes (Src/LineDriven/line_connect.c:84-165): two header
+    lines (the second holds the angle count as its third token), then one
+    row per active cell: i j k r[cm] theta[rad] F_0 .. F_35."""
+    import psgb
+    from oracle import synthetic_flux, NANGLES, WIND
+    x1 = psgb.build_grid(nr, 2, 10.0, 1000.0, "log")[0]
+    x2 = psgb.build_grid(nt, 2, 0.0, 1.5707963267948966, "uniform")[0]
+    fl = synthetic_flux(x1, x2, (nr + 4, nt + 4, 1))
+    for ax, name in enumerate(("r", "theta", "phi")):
+        with open(os.path.join(wd, f"directional_flux_{name}.dat"), "w") as f:
+            f.write("# synthetic directional UV flux\n")
+            f.write(f"# nangles {NANGLES}\n")
+            for j in range(2, nt + 2):
+                for i in range(2, nr + 2):
+                    vals = " ".join("%.12e" % v for v in fl[ax][:, 0, j, i])
+                    f.write(f"{i - 2} {j - 2} 0 {x1[i] * WIND['unit_length']:.12e} "
+                            f"{x2[j]:.12e} {vals}\n")
+
+
+# name, ref config, (nr, nt), steps, snapshot every, with flux files
+WIND_CASES = [
+    ("wind2d_full_64x32", "wind2d", (64, 32), 200, 20, True),
+    ("wind2d_hydro_64x32", "wind2d_hydro", (64, 32), 100, 20, False),
+]
+
+
+def run_wind_case(ref, name, cfg, n, steps, every, flux):
+    subprocess.run(["make", "-s", "-f", os.path.join(ORACLE, "ref.mk"), f"CFG={cfg}",
+                    f"REF={ref}", "-j8"], check=True)
+    exe = os.path.join(ORACLE, "_ref", cfg, "pluto")
+    wd = os.path.join(ORACLE, "_ref", "runs", name)
+    shutil.rmtree(wd, ignore_errors=True)
+    os.makedirs(wd)
+    with open(os.path.join(wd, "pluto.ini"), "w") as f:
+        f.write(WIND_INI.format(nr=n[0], nt=n[1], every=every))
+    if flux:
+        write_flux_files(wd, n[0], n[1])
+    subprocess.run([exe, "-maxsteps", str(steps - 1)], cwd=wd, check=True,
+                   stdout=subprocess.DEVNULL)
+    snaps = []
+    for k in range(steps // every + 1):
+        a = np.fromfile(os.path.join(wd, f"data.{k:04d}.dbl"), dtype="<f8")
+        snaps.append(a.reshape(6, n[1], n[0]))
+    lines = [l.split() for l in open(os.path.join(wd, "dbl.out")).read().split("\n") if l]
+    keep = sorted({0, 1, len(snaps) // 2, len(snaps) - 1})
+    meta = dict(name=name, ref_config=cfg, kind="wind", dims=2, n=[n[0], n[1], 1],
+                steps=steps, snap_steps=[k * every for k in keep], cooling=int(flux),
+                line_force=int(flux), t=[lines[k][1] for k in keep],
+                dt=[lines[k][2] for k in keep], final_sha256=digest(snaps[-1]))
+    snaps = np.stack([snaps[k] for k in keep])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), snaps=snaps)
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print(name, "t =", meta["t"][-1])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
     args = ap.parse_args()
     if not os.path.isdir(os.path.join(args.ref, "Src")):
         sys.exit("reference sources not found at " + args.ref)
     for c in CASES:
-        run_case(args.ref, *c)
+        if args.only is None or args.only in c[0]:
+            run_case(args.ref, *c)
+    for c in WIND_CASES:
+        if args.only is None or args.only in c[0]:
+            run_wind_case(args.ref, *c)
 
 
 if __name__ == "__main__":

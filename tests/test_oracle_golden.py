@@ -50,3 +50,26 @@ def test_oracle_detects_planted_error(built):
     o.run(meta["steps"])
     _, v1 = load_golden(meta)
     assert not np.array_equal(o.active(), v1)
+
+
+@pytest.mark.parametrize("meta", golden_cases(kind="wind"), ids=lambda m: m["name"])
+def test_wind_oracle_matches_reference(built, meta):
+    """2-D spherical line-driven disk wind: geometry, general-grid PLM, HLL,
+    tracer, userdef boundary and floors, gravity and (full case) BLONDIN
+    cooling with the Strang alternation and the line force: bit-exact at
+    every stored snapshot."""
+    from oracle import wind_oracle
+    snaps = np.load(meta["npz"])["snaps"]
+    nr, nt = meta["n"][0], meta["n"][1]
+    o = wind_oracle(nr, nt, cooling=meta["cooling"], line_force=meta["line_force"])
+    done = 0
+    for k, step in enumerate(meta["snap_steps"]):
+        if step > done:
+            o.run(step - done)
+            done = step
+        a = o.active()
+        assert np.array_equal(a, snaps[k]), f"step {step}: max |diff| {np.abs(a - snaps[k]).max()}"
+        t, dt, _ = o.time()
+        assert float(f"{t:e}") == float(meta["t"][k])
+        assert float(f"{dt:e}") == float(meta["dt"][k])
+    assert _digest(o.active()) == meta["final_sha256"]
