@@ -74,6 +74,26 @@ typedef struct ps_config {
 
 typedef struct ps_ctx ps_ctx;
 
+/* Line-driven disk wind terms of a 2-D spherical context: units
+ * (definitions.h UNIT_*), the [Parameters] of the sirocco wind problem,
+ * and which source terms are on. */
+typedef struct ps_wind {
+  double unit_density, unit_length, unit_velocity;
+  double mu;           /* MU: mean molecular weight                        */
+  double rho_0;        /* RHO_0: disk-plane density [g cm^-3]              */
+  double cent_mass;    /* CENT_MASS: central point mass [g]                 */
+  double t_iso;        /* T_ISO: initial isothermal temperature [K]        */
+  double l_star;       /* L_star [erg s^-1]                                 */
+  double f_x, f_uv;    /* X-ray and UV fractions of L_star                  */
+  double t_x;          /* T_x: X-ray (Compton) temperature [K]              */
+  double krad, alpharad; /* force multiplier M = krad * t^alpharad          */
+  double dfloor;       /* DFLOOR: density floor [g cm^-3]                   */
+  int    body_force;   /* BodyForceVector: point-mass gravity               */
+  int    line_force;   /* VGradCalc + LineForce                             */
+  int    floors;       /* UserDefBoundary(side 0) density/pressure floors   */
+  int    nangles;      /* NFLUX_ANGLES (36 for SIROCCO), at most 64         */
+} ps_wind;
+
 const char *ps_last_error(void);
 
 /* ---------------------------------------------------------------- */
@@ -99,6 +119,27 @@ int ps_init_blast(const ps_config *cfg, const double *x1, const double *x2,
                   const double *x3, double p_amb, double p_in, double r_in,
                   double noise, long seed, double *Vc);
 
+/* Initial condition of the line-driven disk wind on a 2-D spherical grid:
+ * Init() evaluated on every cell of the total box at the volume centroids
+ * (Src/startup.c:70-100, Src/set_geometry.c:81-104): an isothermal
+ * (t_iso) disk-plane layer rho_0 exp(-G M / (2 cs^2 r tan^2 theta)) above a
+ * halo at dfloor, Keplerian v_phi, tracer 1 in the layer.  Grid arrays are
+ * those of ps_grid_build for x1 and x2; Vc is [nv][j][i] with nv = 6. */
+int ps_init_wind(const ps_config *cfg, const ps_wind *w, const double *x1,
+                 const double *xl1, const double *xr1, const double *dx1,
+                 const double *x2, const double *xl2, const double *xr2,
+                 double *Vc);
+
+/* Synthetic directional UV flux for the line force: l_star*f_uv/(4 pi r^2)
+ * in the angle bin that contains the radial direction of each active cell
+ * (bins (a + 1/2) 2 pi / 36 from the polar axis), zero elsewhere, rounded
+ * through the 13-significant-digit text of the directional_flux_*.dat
+ * files that read_sirocco_fluxes parses (Src/LineDriven/line_connect.c:
+ * 84-165).  fr/ft/fp are [angle][j][i] over the total box. */
+int ps_wind_synthetic_flux(const ps_config *cfg, const ps_wind *w,
+                           const double *x1, const double *x2,
+                           double *fr, double *ft, double *fp);
+
 /* ---------------------------------------------------------------- */
 /* device context                                                    */
 /* ---------------------------------------------------------------- */
@@ -121,6 +162,17 @@ int ps_set_grid(ps_ctx *ctx, int dir, const double *x, const double *xl,
 int ps_set_state(ps_ctx *ctx, const double *Vc);
 int ps_get_state(ps_ctx *ctx, double *Vc);
 
+/* Turns a 2-D spherical context into the line-driven disk wind: point-mass
+ * gravity (BodyForceVector), the problem's UserDefBoundary (floors on every
+ * cell; X1_BEG copies the first active cell with inflow only), VGradCalc +
+ * LineForce with the fluxes flux_* ([angle][j][i] over the total box, i.e.
+ * flux_r_UV / flux_t_UV / flux_p_UV of Src/globals.h:191-210), and the
+ * BLONDIN split source when cfg.cooling is set.  Call after ps_set_grid and
+ * ps_set_state: sirocco_xi and sirocco_t_r are initialised from the state
+ * as read_sirocco_heatcool(flag = 0) does (line_connect.c:287-306). */
+int ps_set_wind(ps_ctx *ctx, const ps_wind *w, const double *flux_r,
+                const double *flux_t, const double *flux_p);
+
 /* g_time, g_dt, g_stepNumber of the main loop (Src/globals.h:104-110). */
 int ps_set_time(ps_ctx *ctx, double t, double dt, long step);
 int ps_get_time(ps_ctx *ctx, double *t, double *dt, long *step,
@@ -131,6 +183,12 @@ int ps_get_time(ps_ctx *ctx, double *t, double *dt, long *step,
  * *inv_dt_hyp holds Dts->invDt_hyp as UpdateStage leaves it
  * (update_stage.c:389-394), ready for PLUTO's own NextTimeStep(). */
 int ps_advance_step(ps_ctx *ctx, double dt, double *inv_dt_hyp);
+
+/* SplitSource (Src/split_source.c:28-79) with COOLING == BLONDIN: one
+ * BlondinCooling pass (Src/Cooling/BLONDIN/cooling.c:50-165) over the
+ * active cells with the given dt at simulation time t.  No-op without
+ * cooling. */
+int ps_split_source(ps_ctx *ctx, double dt, double t);
 
 /* The main loop of Src/main.c:215-337 (Integrate + NextTimeStep and the
  * tstop clamp) for nsteps steps, entirely on the device and replayed

@@ -123,27 +123,7 @@ static int cuda_fail(cudaError_t e, const char *where)
 // context
 // ------------------------------------------------------------------
 
-struct ps_ctx {
-  ps_config cfg;
-  ps::Params p;
-  int tile[6];
-  dim3 grid, block;
-  size_t smem;
-  const void *k1, *k2;
-  double *V, *Vs, *Us;
-  double *Vsave;            // device checkpoint of V (ps_save_state)
-  ps::Scalars *sc_save;
-  double *dx[3], *inv_dx[3], *dtdx[3];
-  ps::Scalars *sc;
-  double *hist;
-  CUtensorMap tmV, tmVs;
-  cudaStream_t stream;      // stream the work is issued on
-  cudaStream_t own_stream;  // stream created by the context
-  cudaGraphExec_t g1, gN;
-  int nG;
-  long launches;
-  int grid_mask;
-};
+#include "ps_ctx.cuh"
 
 namespace ps {
 static void launch_fill_ghosts(const ps_ctx *c, double *V, cudaStream_t s)
@@ -190,9 +170,25 @@ static int encode_map(ps_ctx *c, double *base, CUtensorMap *tm)
   return 0;
 }
 
+void ps_wind_free(ps::WindDev *w);
+int ps_wind_step_launches(ps_ctx *c, int odd, int (*finish)(ps_ctx *, int));
+int ps_wind_hydro_launches(ps_ctx *c);
+int ps_wind_cool_launch(ps_ctx *c);
+int ps_wind_bnd_launch(ps_ctx *c, int stage);
+int ps_wind_stage_launch(ps_ctx *c, int stage);
+
 static void free_ctx(ps_ctx *c)
 {
   if (!c) return;
+  if (c->wind) ps_wind_free(c->wind);
+  for (int k = 0; k < 3; k++)
+    if (c->gw[k]) cudaGraphExecDestroy(c->gw[k]);
+  for (int d = 0; d < 3; d++) {
+    std::free(c->hx[d]);
+    std::free(c->hxl[d]);
+    std::free(c->hxr[d]);
+    std::free(c->hdx[d]);
+  }
   if (c->g1) cudaGraphExecDestroy(c->g1);
   if (c->gN) cudaGraphExecDestroy(c->gN);
   cudaFree(c->V);
@@ -218,11 +214,13 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
     return PS_EINVAL;
   }
   *out = nullptr;
+  const bool sph = cfg->geometry == PS_SPHERICAL;
   if ((cfg->dims != 2 && cfg->dims != 3) || (cfg->nvar != 5 && cfg->nvar != 6) ||
-      cfg->geometry != PS_CARTESIAN || cfg->limiter < 0 || cfg->limiter > 2 ||
+      (cfg->geometry != PS_CARTESIAN && !sph) || (sph && (cfg->dims != 2 || cfg->nvar != 6)) ||
+      cfg->limiter < 0 || cfg->limiter > 2 ||
       (cfg->solver != PS_HLLC && cfg->solver != PS_HLL) || cfg->gamma <= 1.0) {
-    ps_set_error_msg("ps_create: unsupported configuration (dims 2/3, nvar 5/6, Cartesian, "
-                     "MC/VL/MM limiter, HLLC/HLL)");
+    ps_set_error_msg("ps_create: unsupported configuration (Cartesian: dims 2/3, nvar 5/6; "
+                     "spherical: dims 2, nvar 6; MC/VL/MM limiter, HLLC/HLL)");
     return PS_EINVAL;
   }
   for (int d = 0; d < 3; d++) {
@@ -237,8 +235,9 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   }
   for (int s = 0; s < 2 * cfg->dims; s++) {
     int b = cfg->bc[s];
+    const bool userdef_ok = sph && s == 0 && b == PS_BC_USERDEF;
     if (b != PS_BC_OUTFLOW && b != PS_BC_PERIODIC && b != PS_BC_REFLECTIVE &&
-        b != PS_BC_AXISYM && b != PS_BC_EQTSYM) {
+        b != PS_BC_AXISYM && b != PS_BC_EQTSYM && !userdef_ok) {
       ps_set_error_msg("ps_create: boundary type not supported on this path");
       return PS_EINVAL;
     }
@@ -275,8 +274,8 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   if (cfg->dims == 2) {
     ps::stage_tile_2d(c->tile);
     c->smem = ps::stage_smem_2d(p.nvar);
-    c->k1 = ps::stage_kernel_2d(p.nvar, p.limiter, p.solver, 1);
-    c->k2 = ps::stage_kernel_2d(p.nvar, p.limiter, p.solver, 2);
+    c->k1 = sph ? nullptr : ps::stage_kernel_2d(p.nvar, p.limiter, p.solver, 1);
+    c->k2 = sph ? nullptr : ps::stage_kernel_2d(p.nvar, p.limiter, p.solver, 2);
   } else {
     ps::stage_tile_3d(c->tile);
     c->smem = ps::stage_smem_3d(p.nvar);
@@ -317,8 +316,10 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   TRY(cudaMalloc(&c->sc, sizeof(ps::Scalars)));
   TRY(cudaMalloc(&c->hist, ps::kHist * sizeof(double)));
   TRY(cudaMemset(c->hist, 0, ps::kHist * sizeof(double)));
-  TRY(cudaFuncSetAttribute(c->k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
-  TRY(cudaFuncSetAttribute(c->k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+  if (c->k1) {
+    TRY(cudaFuncSetAttribute(c->k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+    TRY(cudaFuncSetAttribute(c->k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->smem));
+  }
 #undef TRY
   ps::Scalars s0;
   std::memset(&s0, 0, sizeof(s0));
@@ -349,16 +350,30 @@ extern "C" int ps_destroy(ps_ctx *c)
 extern "C" int ps_set_grid(ps_ctx *c, int dir, const double *x, const double *xl,
                            const double *xr, const double *dx)
 {
-  (void)x;
-  (void)xl;
-  (void)xr;
   if (!c || dir < 0 || dir >= c->p.dims || !dx) {
     ps_set_error_msg("ps_set_grid: bad arguments");
     return PS_EINVAL;
   }
   const int n = c->p.ntot[dir];
+  if (c->cfg.geometry == PS_SPHERICAL && (!x || !xl || !xr)) {
+    ps_set_error_msg("ps_set_grid: spherical geometry needs x, xl, xr and dx");
+    return PS_EINVAL;
+  }
   double *inv = (double *)std::malloc(n * sizeof(double));
   if (!inv) return PS_ENOMEM;
+  const double *src[4] = {x, xl, xr, dx};
+  double **dst[4] = {&c->hx[dir], &c->hxl[dir], &c->hxr[dir], &c->hdx[dir]};
+  for (int k = 0; k < 4; k++) {
+    std::free(*dst[k]);
+    *dst[k] = nullptr;
+    if (!src[k]) continue;
+    *dst[k] = (double *)std::malloc(n * sizeof(double));
+    if (!*dst[k]) {
+      std::free(inv);
+      return PS_ENOMEM;
+    }
+    std::memcpy(*dst[k], src[k], n * sizeof(double));
+  }
   for (int i = 0; i < n; i++) inv[i] = 1.0 / (dx[i]);  // Src/set_geometry.c:243-245
   cudaError_t e = cudaMemcpy(c->dx[dir], dx, n * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -462,6 +477,7 @@ extern "C" int ps_set_time(ps_ctx *c, double t, double dt, long step)
   s.t = t;
   s.dt = dt;
   s.step = step;
+  c->host_step = step;
   s.last = 0;
   s.done = 0;
   s.inv_dt_hyp = 0.0;
@@ -501,6 +517,10 @@ extern "C" int ps_advance_step(ps_ctx *c, double dt, double *inv_dt_hyp)
 {
   int r = check_ready(c, "ps_advance_step");
   if (r) return r;
+  if (c->cfg.geometry == PS_SPHERICAL && !c->wind) {
+    ps_set_error_msg("ps_advance_step: a spherical context needs ps_set_wind first");
+    return PS_ESTATE;
+  }
   ps::Scalars s;
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
@@ -510,8 +530,13 @@ extern "C" int ps_advance_step(ps_ctx *c, double dt, double *inv_dt_hyp)
   s.last = 0;
   CK(cudaMemcpy(c->sc, &s, sizeof(s), cudaMemcpyHostToDevice));
   launch_finish(c, ps::MODE_PREP);
-  CK(launch_stage(c, 1));
-  CK(launch_stage(c, 2));
+  if (c->wind) {
+    r = ps_wind_hydro_launches(c);
+    if (r) return r;
+  } else {
+    CK(launch_stage(c, 1));
+    CK(launch_stage(c, 2));
+  }
   launch_finish(c, ps::MODE_INV);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->stream));
@@ -539,11 +564,66 @@ static int build_graph(ps_ctx *c, int nsteps, cudaGraphExec_t *out)
   return 0;
 }
 
+static int finish_step(ps_ctx *c, int) { return launch_finish(c, ps::MODE_STEP); }
+
+// CUDA graphs of the wind step: [0] even step, [1] odd step, [2] even+odd
+static int build_wind_graph(ps_ctx *c, int kind, cudaGraphExec_t *out)
+{
+  cudaGraph_t g;
+  long before = c->launches;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int r = 0;
+  if (kind == 0 || kind == 2) r = ps_wind_step_launches(c, 0, finish_step);
+  if (!r && (kind == 1 || kind == 2)) r = ps_wind_step_launches(c, 1, finish_step);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->launches = before;
+  if (r) return r;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture (wind)");
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate (wind)");
+  return 0;
+}
+
+static int run_wind(ps_ctx *c, int nsteps)
+{
+  long per_step = 7 + (c->p.cooling ? 1 : 0);
+  for (int k = 0; k < 3; k++)
+    if (!c->gw[k]) {
+      int r = build_wind_graph(c, k, &c->gw[k]);
+      if (r) return r;
+    }
+  int left = nsteps;
+  while (left > 0) {
+    const int odd = (int)(c->host_step & 1);
+    if (!odd && left >= 2) {
+      CK(cudaGraphLaunch(c->gw[2], c->stream));
+      c->launches += 2 * per_step;
+      c->host_step += 2;
+      left -= 2;
+    } else {
+      CK(cudaGraphLaunch(c->gw[odd], c->stream));
+      c->launches += per_step;
+      c->host_step += 1;
+      left -= 1;
+    }
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
 extern "C" int ps_run(ps_ctx *c, int nsteps)
 {
   int r = check_ready(c, "ps_run");
   if (r) return r;
   if (nsteps < 0) return PS_EINVAL;
+  if (c->cfg.geometry == PS_SPHERICAL) {
+    if (!c->wind) {
+      ps_set_error_msg("ps_run: a spherical context needs ps_set_wind first");
+      return PS_ESTATE;
+    }
+    return run_wind(c, nsteps);
+  }
   const int G = 16;
   if (!c->g1) {
     r = build_graph(c, 1, &c->g1);
@@ -608,6 +688,7 @@ extern "C" int ps_save_state(ps_ctx *c)
   CK(cudaMemcpyAsync(c->Vsave, c->V, nbytes, cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemcpyAsync(c->sc_save, c->sc, sizeof(ps::Scalars), cudaMemcpyDeviceToDevice,
                      c->stream));
+  c->host_step_save = c->host_step;
   return 0;
 }
 
@@ -621,6 +702,7 @@ extern "C" int ps_restore_state(ps_ctx *c)
   CK(cudaMemcpyAsync(c->V, c->Vsave, nbytes, cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemcpyAsync(c->sc, c->sc_save, sizeof(ps::Scalars), cudaMemcpyDeviceToDevice,
                      c->stream));
+  c->host_step = c->host_step_save;
   return 0;
 }
 
@@ -632,21 +714,73 @@ extern "C" int ps_time_step_kernels(ps_ctx *c, double *ms)
   int r = check_ready(c, "ps_time_step_kernels");
   if (r) return r;
   if (!ms) return PS_EINVAL;
-  cudaEvent_t ev[4];
-  for (int i = 0; i < 4; i++) CK(cudaEventCreate(&ev[i]));
-  CK(cudaEventRecord(ev[0], c->stream));
-  CK(launch_stage(c, 1));
-  CK(cudaEventRecord(ev[1], c->stream));
-  CK(launch_stage(c, 2));
-  CK(cudaEventRecord(ev[2], c->stream));
-  launch_finish(c, ps::MODE_STEP);
-  CK(cudaEventRecord(ev[3], c->stream));
-  CK(cudaEventSynchronize(ev[3]));
-  for (int i = 0; i < 3; i++) {
-    float t = 0.f;
-    CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
-    ms[i] = t;
+  if (c->cfg.geometry == PS_SPHERICAL && !c->wind) {
+    ps_set_error_msg("ps_time_step_kernels: a spherical context needs ps_set_wind first");
+    return PS_ESTATE;
   }
-  for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
-  return 0;
+  cudaEvent_t ev[8];
+  for (int i = 0; i < 8; i++) CK(cudaEventCreate(&ev[i]));
+  if (c->wind) {
+    // ms[0], ms[1]: the two stage kernels; ms[2]: the rest of the step
+    // (boundary kernels, split source, dt kernel)
+    const int odd = (int)(c->host_step & 1);
+    CK(cudaEventRecord(ev[0], c->stream));
+    if (odd) r = ps_wind_cool_launch(c);
+    if (!r) r = ps_wind_bnd_launch(c, 1);
+    CK(cudaEventRecord(ev[1], c->stream));
+    if (!r) r = ps_wind_stage_launch(c, 1);
+    CK(cudaEventRecord(ev[2], c->stream));
+    if (!r) r = ps_wind_bnd_launch(c, 2);
+    CK(cudaEventRecord(ev[3], c->stream));
+    if (!r) r = ps_wind_stage_launch(c, 2);
+    CK(cudaEventRecord(ev[4], c->stream));
+    if (!r && !odd) r = ps_wind_cool_launch(c);
+    launch_finish(c, ps::MODE_STEP);
+    CK(cudaEventRecord(ev[5], c->stream));
+    CK(cudaEventSynchronize(ev[5]));
+    c->host_step++;
+    float t[5];
+    for (int i = 0; i < 5; i++) CK(cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]));
+    ms[0] = t[1];
+    ms[1] = t[3];
+    ms[2] = t[0] + t[2] + t[4];
+  } else {
+    CK(cudaEventRecord(ev[0], c->stream));
+    CK(launch_stage(c, 1));
+    CK(cudaEventRecord(ev[1], c->stream));
+    CK(launch_stage(c, 2));
+    CK(cudaEventRecord(ev[2], c->stream));
+    launch_finish(c, ps::MODE_STEP);
+    CK(cudaEventRecord(ev[3], c->stream));
+    CK(cudaEventSynchronize(ev[3]));
+    for (int i = 0; i < 3; i++) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+      ms[i] = t;
+    }
+  }
+  for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
+  return r;
+}
+
+// SplitSource (Src/split_source.c:28-79): the BLONDIN pass with dt at time t.
+extern "C" int ps_split_source(ps_ctx *c, double dt, double t)
+{
+  int r = check_ready(c, "ps_split_source");
+  if (r) return r;
+  if (!c->wind || !c->p.cooling) return 0;
+  ps::Scalars s;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
+  s.dt = dt;
+  s.t = t;
+  s.done = 0;
+  CK(cudaMemcpy(c->sc, &s, sizeof(s), cudaMemcpyHostToDevice));
+  r = ps_wind_cool_launch(c);
+  if (r) return r;
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  unsigned flags = 0;
+  CK(cudaMemcpy(&flags, &c->sc->flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  return (int)flags;
 }

@@ -1,0 +1,66 @@
+// ps_wind.cuh -- device data of the 2-D spherical line-driven disk wind:
+// geometry factors, the sparse per-cell list of flux bins used by the line
+// force, and the problem parameters (units, gravity, floors, cooling).
+#pragma once
+
+#include "ps_hydro.cuh"
+
+namespace ps {
+
+// 1-D geometry arrays over the total box; every product the reference
+// forms per cell (volumes, areas) is rebuilt from these with the same
+// rounding: dV = dVr[i]*dmu[j], A1 = A1f[i]*dmu[j], A2 = rdr[i]*sxp[j].
+struct SphGeom {
+  // x1 direction (ntot[0] entries)
+  const double *x1, *dx1, *inv_dx1;
+  const double *rinv;    // 1/x1                    (r_1 of the x1 sources)
+  const double *absx1;   // |x1|                    (phi-momentum divisor)
+  const double *absx1p;  // |x1p|                   (phi-momentum flux factor)
+  const double *A1f;     // x1p*x1p
+  const double *dVr;     // |x1p^3 - x1m^3| / 3
+  const double *rdr;     // |x1|*dx1
+  const double *rtinv;   // 1/rt                    (dx/dl in x2, r_1 of the x2 sources)
+  const double *g0;      // -1*GM/(x1*x1)            (BodyForceVector)
+  const double *x11a, *x22a, *locr;  // VGradCalc interpolation corners / centre (cm)
+  // x2 direction (ntot[1] entries)
+  const double *x2, *dx2, *inv_dx2;
+  const double *dmu;     // |cos(x2m) - cos(x2p)|
+  const double *sxp;     // |sin(x2p)|
+  const double *spabs;   // |sp|
+  const double *sn;      // |sin(x2)|
+  const double *ct;      // 1/tan(x2)
+  const double *sin2, *cos2;
+  const double *x11b, *x22b;
+  // PLM weights per direction
+  const double *cp[2], *cm[2], *wp[2], *wm[2], *dp[2], *dm[2];
+};
+
+// Flux bins with a nonzero (F_r, F_theta) per active cell, in increasing
+// bin order (the order the reference sums them in), as a CSR list.
+struct LineList {
+  const int *off;        // [nx0*nx1 + 1], active cell (i, j) -> (j*nx0 + i)
+  const int *ang;        // bin index
+  const double *Fr, *Ft;
+  const double *roff, *toff, *sinto, *costo, *ds;
+  double *dvds;          // per-entry dv/ds of the current stage
+};
+
+struct WindParams {
+  int body_force, line_force, floors, cooling;
+  double unit_density, unit_length, unit_velocity;
+  double mu, kelvin;     // KELVIN = UNIT_VELOCITY^2 * amu / kB
+  double dfloor, tfloor, pfloor;
+  double krad, alpharad, sigma_e, unit_acc;
+  double lx, t_x;        // L_star*f_x, T_x
+  double unit_pressure, unit_time;
+  double sin_a[64], cos_a[64];  // sin/cos of the bin directions
+};
+
+struct WindStageArgs {
+  StageArgs s;
+  SphGeom g;
+  LineList L;
+  WindParams w;
+};
+
+}  // namespace ps

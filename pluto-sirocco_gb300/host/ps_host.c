@@ -11,6 +11,7 @@
 
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -153,5 +154,102 @@ int ps_init_blast(const ps_config *cfg, const double *x1, const double *x2,
     Vc[4 * nc + c] = (sqrt(r2) < r_in) ? p_in : p_amb;
   }
   free(g);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* line-driven disk wind                                               */
+/* ------------------------------------------------------------------ */
+
+#define W_AMU  1.66053886e-24
+#define W_G    6.6726e-8
+#define W_KB   1.3806505e-16
+#define W_PI   3.14159265358979
+#define W_RGAS 8.3144598e7
+
+int ps_init_wind(const ps_config *cfg, const ps_wind *w, const double *x1,
+                 const double *xl1, const double *xr1, const double *dx1,
+                 const double *x2, const double *xl2, const double *xr2,
+                 double *Vc)
+{
+  int n0, n1, i, j;
+  size_t nc;
+  double gm_cgs, kelvin, rho_a;
+  if (!cfg || !w || !x1 || !xl1 || !xr1 || !dx1 || !x2 || !xl2 || !xr2 || !Vc ||
+      cfg->dims != 2 || cfg->nvar != 6 || cfg->geometry != PS_SPHERICAL) {
+    ps_set_error_msg("ps_init_wind: needs a 2-D spherical configuration with nvar = 6");
+    return PS_EINVAL;
+  }
+  n0 = cfg->nx[0] + 4;
+  n1 = cfg->nx[1] + 4;
+  nc = (size_t)n0 * n1;
+  gm_cgs = W_G * w->cent_mass;
+  kelvin = w->unit_velocity * w->unit_velocity * W_AMU / W_KB;
+  rho_a = w->dfloor / w->unit_density;
+  (void)xl1;
+  (void)xr1;
+  for (j = 0; j < n1; j++) {
+    /* theta centroid (Src/set_geometry.c:97-99) */
+    double xL = xl2[j], xR = xr2[j];
+    double th = sin(xR) - sin(xL) + xL * cos(xL) - xR * cos(xR);
+    th /= cos(xL) - cos(xR);
+    for (i = 0; i < n0; i++) {
+      /* radial centroid (Src/set_geometry.c:81-84) */
+      double r1 = x1[i] + 2.0 * x1[i] * dx1[i] * dx1[i] /
+                              (12.0 * x1[i] * x1[i] + dx1[i] * dx1[i]);
+      double r = r1 * w->unit_length;
+      double cs2 = W_RGAS * w->t_iso / w->mu;
+      double tt = tan(th);
+      double rho_d = w->rho_0 * exp(-gm_cgs / (2.0 * cs2 * r * tt * tt)) / w->unit_density;
+      size_t c = (size_t)j * n0 + i;
+      double rho, trc;
+      if (rho_d > rho_a) {
+        rho = rho_d;
+        trc = 1.0;
+      } else {
+        rho = rho_a;
+        trc = 0.0;
+      }
+      Vc[0 * nc + c] = rho;
+      Vc[1 * nc + c] = 0.0;
+      Vc[2 * nc + c] = 0.0;
+      Vc[3 * nc + c] = sqrt(gm_cgs / r) * sin(th) / w->unit_velocity;
+      Vc[4 * nc + c] = rho * w->t_iso / (kelvin * w->mu);
+      Vc[5 * nc + c] = trc;
+    }
+  }
+  return 0;
+}
+
+int ps_wind_synthetic_flux(const ps_config *cfg, const ps_wind *w,
+                           const double *x1, const double *x2,
+                           double *fr, double *ft, double *fp)
+{
+  int n0, n1, na, i, j, a;
+  size_t nc;
+  char buf[64];
+  double l_uv;
+  if (!cfg || !w || !x1 || !x2 || !fr || !ft || !fp || cfg->dims != 2 || w->nangles < 1 ||
+      w->nangles > 64) {
+    ps_set_error_msg("ps_wind_synthetic_flux: bad arguments");
+    return PS_EINVAL;
+  }
+  n0 = cfg->nx[0] + 4;
+  n1 = cfg->nx[1] + 4;
+  nc = (size_t)n0 * n1;
+  na = w->nangles;
+  memset(fr, 0, (size_t)na * nc * sizeof(double));
+  memset(ft, 0, (size_t)na * nc * sizeof(double));
+  memset(fp, 0, (size_t)na * nc * sizeof(double));
+  l_uv = w->l_star * w->f_uv;
+  for (j = 2; j < n1 - 2; j++) {
+    a = (int)floor(x2[j] / (2 * W_PI / 36));
+    if (a < 0 || a >= na) continue;
+    for (i = 2; i < n0 - 2; i++) {
+      double r = x1[i] * w->unit_length;
+      snprintf(buf, sizeof(buf), "%.12e", l_uv / (4 * 3.141592653589793 * r * r));
+      fr[(size_t)a * nc + (size_t)j * n0 + i] = strtod(buf, NULL);
+    }
+  }
   return 0;
 }

@@ -25,7 +25,8 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_set_grid", "ps_set_state", "ps_get_state", "ps_set_time", "ps_get_time",
            "ps_advance_step", "ps_run", "ps_sync", "ps_device_state", "ps_launch_count",
            "ps_get_dt_history", "ps_set_stream", "ps_probe_fp64_flops", "ps_save_state",
-           "ps_restore_state", "ps_time_step_kernels", "ps_advance_step_noalloc"]
+           "ps_restore_state", "ps_time_step_kernels", "ps_advance_step_noalloc",
+           "ps_init_wind", "ps_wind_synthetic_flux", "ps_set_wind", "ps_split_source"]
 
 
 class Config(ctypes.Structure):
@@ -35,6 +36,30 @@ class Config(ctypes.Structure):
                 ("cfl_max_var", ctypes.c_double), ("tstop", ctypes.c_double),
                 ("first_dt", ctypes.c_double), ("cooling", ctypes.c_int),
                 ("reserved", ctypes.c_int)]
+
+
+class Wind(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("unit_density", "unit_length", "unit_velocity", "mu", "rho_0", "cent_mass",
+                 "t_iso", "l_star", "f_x", "f_uv", "t_x", "krad", "alpharad", "dfloor")] + \
+               [(n, ctypes.c_int) for n in ("body_force", "line_force", "floors", "nangles")]
+
+
+# The line-driven disk wind problem: 512 x 256 (r, theta) by default,
+# r log-spaced 1e10..1e12 cm, theta uniform 0..pi/2; 7 solar masses;
+# halo 1e-20 g/cm^3; disk-plane layer 1e-9 g/cm^3 at 4e4 K; L_x = 1e37 erg/s;
+# M = 0.2 t^-0.6, M_max = 4400.
+WIND_PARAMS = dict(unit_density=1e-14, unit_length=1e9, unit_velocity=1e9, mu=0.6,
+                   rho_0=1.0e-9, cent_mass=1.4e34, t_iso=4.0e4, l_star=1.0e37, f_x=1.0,
+                   f_uv=1.0, t_x=5.6e7, krad=0.2, alpharad=-0.6, dfloor=1.0e-20)
+
+
+def make_wind(line_force=1, body_force=1, floors=1, nangles=36, **over):
+    w = Wind()
+    for k, v in dict(WIND_PARAMS, **over).items():
+        setattr(w, k, v)
+    w.body_force, w.line_force, w.floors, w.nangles = body_force, line_force, floors, nangles
+    return w
 
 
 _lib = None
@@ -75,6 +100,12 @@ def lib():
         L.ps_time_step_kernels.argtypes = [P, DP]
         L.ps_advance_step_noalloc.argtypes = [ctypes.POINTER(Config), DP, DP, DP,
                                               ctypes.c_void_p, D, DP, ctypes.c_void_p]
+        L.ps_init_wind.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Wind), DP, DP, DP, DP,
+                                   DP, DP, DP, DP]
+        L.ps_wind_synthetic_flux.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Wind), DP,
+                                             DP, DP, DP, DP]
+        L.ps_set_wind.argtypes = [P, ctypes.POINTER(Wind), DP, DP, DP]
+        L.ps_split_source.argtypes = [P, D, D]
         _lib = L
     return _lib
 
@@ -109,6 +140,47 @@ def check(rc, what):
     if rc < 0:
         raise RuntimeError(f"{what} failed ({rc}): {lib().ps_last_error().decode()}")
     return rc
+
+
+def make_wind_config(nr=512, nt=256, cooling=1, limiter="vl", solver="hll", cfl=0.4,
+                     first_dt=1e-4):
+    c = make_config(dims=2, nx=(nr, nt, 1), nvar=6, limiter=limiter, solver=solver,
+                    bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
+                    cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling)
+    c.geometry = SPHERICAL
+    return c
+
+
+class WindGrid:
+    """r log-spaced on [10, 1000] x UNIT_LENGTH, theta uniform on [0, pi/2]."""
+
+    def __init__(self, cfg):
+        self.ngh = [2, 2, 0]
+        self.ntot = [cfg.nx[0] + 4, cfg.nx[1] + 4, 1]
+        self.arrays = [build_grid(cfg.nx[0], 2, 10.0, 1000.0, "log"),
+                       build_grid(cfg.nx[1], 2, 0.0, 1.5707963267948966, "uniform"),
+                       build_grid(1, 0, 0.0, 1.0, "uniform")]
+
+    def x(self, d):
+        return self.arrays[d][0]
+
+
+def wind_state(cfg, wind, grid):
+    V = np.zeros((6, 1, grid.ntot[1], grid.ntot[0]))
+    a1, a2 = grid.arrays[0], grid.arrays[1]
+    check(lib().ps_init_wind(ctypes.byref(cfg), ctypes.byref(wind), _dp(a1[0]), _dp(a1[1]),
+                             _dp(a1[2]), _dp(a1[3]), _dp(a2[0]), _dp(a2[1]), _dp(a2[2]),
+                             _dp(V)), "ps_init_wind")
+    return V
+
+
+def wind_flux(cfg, wind, grid):
+    shape = (wind.nangles, 1, grid.ntot[1], grid.ntot[0])
+    fr, ft, fp = np.zeros(shape), np.zeros(shape), np.zeros(shape)
+    check(lib().ps_wind_synthetic_flux(ctypes.byref(cfg), ctypes.byref(wind), _dp(grid.x(0)),
+                                       _dp(grid.x(1)), _dp(fr), _dp(ft), _dp(fp)),
+          "ps_wind_synthetic_flux")
+    return fr, ft, fp
 
 
 def build_grid(n, ngh, xbeg=0.0, xend=1.0, kind="uniform", ratio=1.0):
@@ -175,6 +247,14 @@ class Solver:
         check(lib().ps_get_state(self.ctx, _dp(V)), "ps_get_state")
         return V
 
+    def set_wind(self, wind, flux=None):
+        if flux is None:
+            shape = (max(wind.nangles, 1), 1, self.grid.ntot[1], self.grid.ntot[0])
+            flux = (np.zeros(shape),) * 3
+        self._flux = [np.ascontiguousarray(f, dtype=np.float64) for f in flux]
+        check(lib().ps_set_wind(self.ctx, ctypes.byref(wind), *(_dp(f) for f in self._flux)),
+              "ps_set_wind")
+
     def set_time(self, t, dt, step=0):
         check(lib().ps_set_time(self.ctx, t, dt, step), "ps_set_time")
 
@@ -193,6 +273,9 @@ class Solver:
         inv = ctypes.c_double(inv_dt_hyp)
         rc = check(lib().ps_advance_step(self.ctx, dt, ctypes.byref(inv)), "ps_advance_step")
         return rc, inv.value
+
+    def split_source(self, dt, t):
+        return check(lib().ps_split_source(self.ctx, dt, t), "ps_split_source")
 
     def sync(self):
         return check(lib().ps_sync(self.ctx), "ps_sync")

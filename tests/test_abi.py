@@ -92,3 +92,28 @@ def test_bad_config_rejected_without_gpu(built, bad):
     assert rc == -1
     assert psgb.lib().ps_last_error()
     assert not ctx.value
+
+
+def test_wind_host_helpers_match_oracle(built):
+    """ps_init_wind (Init() at the volume centroids) and the synthetic
+    flux-file values equal the oracle's, which equal the reference's."""
+    import psgb
+    from oracle import wind_oracle, synthetic_flux
+    cfg = psgb.make_wind_config(48, 24)
+    w = psgb.make_wind()
+    g = psgb.WindGrid(cfg)
+    V = psgb.wind_state(cfg, w, g)
+    o = wind_oracle(48, 24)
+    assert np.array_equal(V, o.V)
+    fr, ft, fp = psgb.wind_flux(cfg, w, g)
+    ofr, oft, ofp = synthetic_flux(o.grid(0), o.grid(1), o.ntot)
+    assert np.array_equal(fr, ofr) and np.array_equal(ft, oft) and np.array_equal(fp, ofp)
+    assert np.count_nonzero(fr) == 48 * 24  # one bin per active cell
+
+
+def test_wind_requires_spherical_nvar6(built):
+    import psgb
+    cfg = psgb.make_config(dims=2, nx=(32, 32, 1), nvar=5)
+    cfg.geometry = psgb.SPHERICAL
+    ctx = ctypes.c_void_p()
+    assert psgb.lib().ps_create(ctypes.byref(cfg), ctypes.byref(ctx)) == -1
