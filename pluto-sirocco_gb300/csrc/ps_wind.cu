@@ -434,7 +434,9 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
     const int ix = q % PX, iy = q / PX;
     const int sx = ix + TL::HX - (D == 0), sy = iy + TL::HY - (D == 1);
     const int s0 = sy * G::SX + sx;
-    const int gc = D == 0 ? p.beg[0] + ox + ix - 1 : p.beg[1] + oy + iy - 1;
+    // cells past the end of the grid (partial last tile) read the last
+    // weights; their states are never used
+    const int gc = min(D == 0 ? p.beg[0] + ox + ix - 1 : p.beg[1] + oy + iy - 1, p.ntot[D] - 1);
     const double cp = g.cp[D][gc], cm = g.cm[D][gc], wp = g.wp[D][gc], wm = g.wm[D][gc];
     const double dp = g.dp[D][gc], dm = g.dm[D][gc];
 #pragma unroll
