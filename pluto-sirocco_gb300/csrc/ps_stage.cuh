@@ -31,6 +31,10 @@ template <> struct TileT<2> {
 template <> struct TileT<3> {
   static constexpr int X = 16, Y = 4, Z = 4, HX = 2, HY = 2, HZ = 2;
 };
+// 2-D tiles of other shapes (chosen per grid size by the batch autotuner)
+template <int TX, int TY> struct Tile2D {
+  static constexpr int X = TX, Y = TY, Z = 1, HX = 2, HY = 2, HZ = 0;
+};
 
 template <class TL> struct TileGeom {
   static constexpr int SX = TL::X + 2 * TL::HX, SY = TL::Y + 2 * TL::HY, SZ = TL::Z + 2 * TL::HZ;

@@ -32,287 +32,35 @@
 
 extern "C" void ps_set_error_msg(const char *msg);
 
+#include "ps_wind_dev.cuh"
+
 namespace ps {
 
-constexpr double kAmu = 1.66053886e-24, kC = 2.99792458e10, kG = 6.6726e-8, kKB = 1.3806505e-16,
-                 kMP = 1.67262171e-24, kPI = 3.14159265358979, kSigmaT = 6.6524e-25;
-constexpr int kMaxCoolIter = 10000;  // the bracket search of the reference ends far earlier
-
-struct WindDev {
-  WindStageArgs a;       // geometry, line list, parameters (stage part filled per launch)
-  double *geo = nullptr; // all 1-D geometry arrays in one allocation
-  int *off = nullptr, *ang = nullptr;
-  double *ent = nullptr; // Fr, Ft, roff, toff, sinto, costo, ds (SoA, nent each)
-  double *dvds = nullptr;
-  double *xi = nullptr, *tr = nullptr;
-  long nent = 0;
-  const void *k1 = nullptr, *k2 = nullptr;
-  size_t smem = 0;
-};
-
-// ------------------------------------------------------------------
-// device helpers
-// ------------------------------------------------------------------
-
-template <int LIM>
-__device__ __forceinline__ double limited_slope_general(double dvp, double dvm, double cp,
-                                                        double cm)
-{
-  if constexpr (LIM == LIM_MC) {
-    double dv = 0.0;
-    if (dvp * dvm > 0.0) {
-      double qc = 0.5 * (dvm + dvp), scrh = abs_min(dvp * cp, dvm * cm);
-      dv = abs_min(qc, scrh);
-    }
-    return dv;
-  } else if constexpr (LIM == LIM_VL) {
-    return dvp * dvm > 0.0 ? dvp * dvm * (cp * dvm + cm * dvp) /
-                                 (dvp * dvp + dvm * dvm + (cp + cm - 2.0) * dvp * dvm)
-                           : 0.0;
-  } else {
-    return dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0;
-  }
-}
-
-__device__ __forceinline__ long long vcell(const Params &p, int gj, int gi)
-{
-  return (long long)gj * p.px + gi;
-}
-
-// density / pressure floors of the problem's UserDefBoundary(side 0);
-// returns true if the cell was repaired.
-template <int NV>
-__device__ __forceinline__ bool apply_floors(double (&v)[NV], const WindParams &w, double gamma)
-{
-  bool convert = false;
-  const double K = w.kelvin, mu = w.mu;
-  if (v[RHO] < w.dfloor) {
-    if (v[RHO] < 0.0) v[RHO] = w.dfloor;
-    const double cs = sqrt(gamma * v[PRS] / v[RHO]);
-    const double dfact = v[RHO] / w.dfloor;
-    v[RHO] = w.dfloor;
-    v[VX1] = dfact * v[VX1];
-    v[VX2] = dfact * v[VX2];
-    v[VX3] = dfact * v[VX3];
-    v[PRS] = cs * cs * v[RHO] / gamma;
-    const double temp = v[PRS] / v[RHO] * K * mu;
-    if (temp < w.tfloor) v[PRS] = v[RHO] * w.tfloor / (K * mu);
-    if constexpr (NV > NFLX) v[NFLX] = 0.0;
-    convert = true;
-  }
-  if (v[PRS] < w.pfloor) {
-    v[PRS] = w.pfloor;
-    convert = true;
-  }
-  return convert;
-}
-
-// Boundary() part 1: floors on the active cells, then the x1 ghost cells
-// of the active rows, each written by the active cell it comes from.
 template <int NV>
 __global__ void k_wind_bnd_x1(double *V, double *Us, const Params p, const WindParams w,
                               Scalars *sc, int stage)
 {
   if (sc->done) return;
   const int n = p.nx[0] * p.nx[1];
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int i = q % p.nx[0], j = q / p.nx[0];
-    const int gi = i + p.beg[0], gj = j + p.beg[1];
-    const long long c = vcell(p, gj, gi);
-    double v[NV];
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) v[nv] = V[nv * p.vstride + c];
-    if (w.floors && apply_floors<NV>(v, w, p.gamma)) {
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) V[nv * p.vstride + c] = v[nv];
-      if (stage == 2) {
-        double u[NV];
-        prim_to_cons<NV>(v, u, p.gmm1);
-#pragma unroll
-        for (int nv = 0; nv < NV; nv++) Us[nv * p.vstride + c] = u[nv];
-      }
-    }
-    const int b = p.beg[0], e = p.beg[0] + p.nx[0] - 1, nn = p.nx[0];
-#pragma unroll
-    for (int side = 0; side < 2; side++) {
-      const int type = p.bc[side];
-      int t0 = -1, t1 = -1;
-      bool flip = false, inflow = false;
-      if (type == BC_OUTFLOW || type == PS_BC_USERDEF) {
-        if (side == 0 && gi == b) { t0 = b - 1; t1 = b - 2; }
-        if (side == 1 && gi == e) { t0 = e + 1; t1 = e + 2; }
-        inflow = (type == PS_BC_USERDEF) && side == 0;
-      } else if (type == BC_PERIODIC) {
-        if (side == 0 && gi >= e - 1) t0 = gi - nn;
-        if (side == 1 && gi <= b + 1) t0 = gi + nn;
-      } else if (type == BC_REFLECTIVE || type == BC_AXISYM || type == BC_EQTSYM) {
-        flip = true;
-        if (side == 0 && gi <= b + 1) t0 = 2 * b - 1 - gi;
-        if (side == 1 && gi >= e - 1) t0 = 2 * e + 1 - gi;
-      }
-#pragma unroll
-      for (int wi = 0; wi < 2; wi++) {
-        const int t = wi == 0 ? t0 : t1;
-        if (t < 0) continue;
-        const long long g = vcell(p, gj, t);
-#pragma unroll
-        for (int nv = 0; nv < NV; nv++) {
-          double val = v[nv];
-          if (flip && (nv == VX1 || (type == BC_AXISYM && nv == VX3))) val = -1 * val;
-          if (inflow && nv == VX1) val = dmin(val, 0.0);
-          V[nv * p.vstride + g] = val;
-        }
-      }
-    }
-  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    bnd_x1_cell<NV>(V, Us, p, w, stage, q);
 }
 
-// Boundary() part 2: the x2 ghost rows over every column (x1 ghosts
-// included), after part 1 -- the side order of Boundary().
 template <int NV>
 __global__ void k_wind_bnd_x2(double *V, const Params p, Scalars *sc)
 {
   if (sc->done) return;
   const int n = p.ntot[0] * 4;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int gi = q % p.ntot[0], r = q / p.ntot[0];
-    const int side = r / 2;
-    const int b = p.beg[1], e = p.beg[1] + p.nx[1] - 1, nn = p.nx[1];
-    const int gj = side == 0 ? b - 1 - (r & 1) : e + 1 + (r & 1);
-    const int type = p.bc[2 + side];
-    int src;
-    bool flip = false;
-    if (type == BC_OUTFLOW)
-      src = side == 0 ? b : e;
-    else if (type == BC_PERIODIC)
-      src = side == 0 ? gj + nn : gj - nn;
-    else {
-      flip = true;
-      src = side == 0 ? 2 * b - 1 - gj : 2 * e + 1 - gj;
-    }
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      double val = V[nv * p.vstride + vcell(p, src, gi)];
-      if (flip && (nv == VX2 || (type == BC_AXISYM && nv == VX3))) val = -1 * val;
-      V[nv * p.vstride + vcell(p, gj, gi)] = val;
-    }
-  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    bnd_x2_item<NV>(V, p, q);
 }
 
-// read_sirocco_heatcool(flag = 0): xi = L_x / n_H / r^2 from the state.
 __global__ void k_wind_init_xi(const double *V, double *xi, double *tr, const Params p,
                                const WindParams w, const double *x1)
 {
   const int n = p.nx[0] * p.nx[1];
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int gi = q % p.nx[0] + p.beg[0], gj = q / p.nx[0] + p.beg[1];
-    const long long c = vcell(p, gj, gi);
-    const double rho = V[RHO * p.vstride + c] * w.unit_density;
-    const double r = x1[gi] * w.unit_length;
-    const double nH = rho / (1.43 * kMP);
-    xi[c] = w.lx / nH / (r * r);
-    tr[c] = w.t_x;
-  }
-}
-
-// ---------------------------------------------------------------
-// BLONDIN heating/cooling, one thread per active cell
-// ---------------------------------------------------------------
-
-struct BlCtx {
-  double xi, sqxi, sqsqxi, nH, n, tx, E, hc_init, dt_share;
-};
-
-__device__ __forceinline__ double bl_ne_rat(double T)
-{
-  if (T < 1.5e4) return 1e-2 + pow(10.0, (-51.59417133 + 12.27740153 * log10(T)));
-  if (T >= 1.5e4 && T < 3.3e4) return pow(10.0, (-3.80749689 + 0.86092628 * log10(T)));
-  return 1.21;
-}
-
-__device__ __forceinline__ double bl_heatcool(const BlCtx &b, double T)
-{
-  const double sqT = sqrt(T);
-  const double ne = b.nH * bl_ne_rat(T);
-  const double comp_heat = 1.0 * (8.9e-36 * b.xi * b.tx);
-  const double comp_cool = 1.0 * (8.9e-36 * b.xi * (4.0 * T));
-  const double xray_heat = 1.0 * (1.5e-21 * (b.sqsqxi / sqT));
-  const double line_cool =
-      1.0 * ((1e-16 * exp(-1.3e5 / T) / b.sqxi / T) + fmin(fmin(1e-24, 5e-27 * sqT), 1.5e-17 / T));
-  const double brem_cool = 1.0 * (3.3e-27 * sqT);
-  return b.nH *
-         (ne * comp_heat + b.nH * xray_heat - ne * comp_cool - ne * line_cool - ne * brem_cool);
-}
-
-__device__ __forceinline__ double bl_zfunc(const BlCtx &b, double temp)
-{
-  return (temp * b.n * kKB / (2.0 / 3.0)) - b.E - b.dt_share * (b.hc_init + bl_heatcool(b, temp)) / 2.0;
-}
-
-__device__ __forceinline__ double bl_func(const BlCtx &b, int which, double x)
-{
-  return which == 0 ? bl_zfunc(b, x) : bl_heatcool(b, x);
-}
-
-__device__ double bl_zbrent(const BlCtx &bc, int which, double x1, double x2, double tol)
-{
-  const double EPS = 3.0e-8;
-  double a = x1, b = x2, c = x2, d = 0.0, e = 0.0;
-  double fa = bl_func(bc, which, a), fb = bl_func(bc, which, b), fc = fb;
-  if (fb * fa > 0.0) return b;
-  for (int iter = 1; iter <= 100; iter++) {
-    if (fb * fc > 0.0) {
-      c = a;
-      fc = fa;
-      e = d = b - a;
-    }
-    if (fabs(fc) < fabs(fb)) {
-      a = b;
-      b = c;
-      c = a;
-      fa = fb;
-      fb = fc;
-      fc = fa;
-    }
-    const double tol1 = 2.0 * EPS * fabs(b) + 0.5 * tol;
-    const double xm = 0.5 * (c - b);
-    if (fabs(xm) <= tol1 || fb == 0.0) return b;
-    if (fabs(e) >= tol1 && fabs(fa) > fabs(fb)) {
-      double p, q, r;
-      const double s = fb / fa;
-      if (a == c) {
-        p = 2.0 * xm * s;
-        q = 1.0 - s;
-      } else {
-        q = fa / fc;
-        r = fb / fc;
-        p = s * (2.0 * xm * q * (q - r) - (b - a) * (r - 1.0));
-        q = (q - 1.0) * (r - 1.0) * (s - 1.0);
-      }
-      if (p > 0.0) q = -q;
-      p = fabs(p);
-      const double min1 = 3.0 * xm * q - fabs(tol1 * q);
-      const double min2 = fabs(e * q);
-      if (2.0 * p < (min1 < min2 ? min1 : min2)) {
-        e = d;
-        d = p / q;
-      } else {
-        d = xm;
-        e = d;
-      }
-    } else {
-      d = xm;
-      e = d;
-    }
-    a = b;
-    fa = fb;
-    if (fabs(d) > tol1)
-      b += d;
-    else
-      b += (xm > 0.0 ? fabs(tol1) : -fabs(tol1));
-    fb = bl_func(bc, which, b);
-  }
-  return b;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    init_xi_cell(V, xi, tr, p, w, x1, q);
 }
 
 __global__ void k_blondin(double *V, const double *xi_s, const double *tr_s, const Params p,
@@ -321,399 +69,16 @@ __global__ void k_blondin(double *V, const double *xi_s, const double *tr_s, con
   if (sc->done) return;
   const double dt = sc->dt, t = sc->t;
   const int n = p.nx[0] * p.nx[1];
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int gi = q % p.nx[0] + p.beg[0], gj = q / p.nx[0] + p.beg[1];
-    const long long c = vcell(p, gj, gi);
-    BlCtx b;
-    b.dt_share = dt * w.unit_time;
-    const double r = x1[gi] * w.unit_length;
-    const double rho = V[RHO * p.vstride + c] * w.unit_density;
-    const double pr = V[PRS * p.vstride + c];
-    b.E = (pr * w.unit_pressure) / (p.gamma - 1);
-    b.nH = rho / (1.43 * kMP);
-    if (t <= 3.0) {
-      b.xi = w.lx / b.nH / r / r;
-      b.tx = w.t_x;
-    } else {
-      b.xi = xi_s[c];
-      b.tx = tr_s[c];
-    }
-    b.n = rho / (w.mu * kMP);
-    const double T = b.E * (2.0 / 3.0) / (b.n * kKB);
-    if (T < 1.e4) continue;
-    b.sqxi = sqrt(b.xi);
-    b.sqsqxi = pow(b.xi, 0.25);
-    b.hc_init = bl_heatcool(b, T);
-    double t_l = T * 0.9, t_u = T * 1.1;
-    double test = bl_zfunc(b, t_l) * bl_zfunc(b, t_u);
-    int it = 0;
-    while (test > 0 && test == test && it < kMaxCoolIter) {
-      t_l *= 0.9;
-      t_u *= 1.1;
-      test = bl_zfunc(b, t_l) * bl_zfunc(b, t_u);
-      it++;
-    }
-    if (it >= kMaxCoolIter) atomicOr(&sc->flags, F_NAN);
-    double T_f;
-    if (test != test) {
-      T_f = T;
-    } else {
-      T_f = bl_zbrent(b, 0, t_l, t_u, 1.0);
-      const double hc_final = bl_heatcool(b, T_f);
-      if (hc_final * b.hc_init < 0.0) T_f = bl_zbrent(b, 1, fmin(T_f, T), fmax(T_f, T), 1.0);
-    }
-    T_f = dmax(T_f, 1.e4);
-    const double E_f = T_f / (2.0 / 3.0) * (b.n * kKB);
-    V[PRS * p.vstride + c] = E_f * (p.gamma - 1) / w.unit_pressure;
-  }
-}
-
-// ---------------------------------------------------------------
-// spherical stage kernel
-// ---------------------------------------------------------------
-
-__device__ __forceinline__ void bilinear(double x110, double x111, double x220, double x221,
-                                         const double (&v11)[2], const double (&v12)[2],
-                                         const double (&v21)[2], const double (&v22)[2],
-                                         double t0, double t1, double (&ans)[2])
-{
-  const double fracx1 = (t0 - x110) / (x220 - x110);
-  const double fracx2 = (t1 - x111) / (x221 - x111);
-  double temp1 = (1.0 - fracx1) * v11[0] + fracx1 * v21[0];
-  double temp2 = (1.0 - fracx1) * v12[0] + fracx1 * v22[0];
-  ans[0] = (1.0 - fracx2) * temp1 + fracx2 * temp2;
-  temp1 = (1.0 - fracx1) * v11[1] + fracx1 * v21[1];
-  temp2 = (1.0 - fracx1) * v12[1] + fracx1 * v22[1];
-  ans[1] = (1.0 - fracx2) * temp1 + fracx2 * temp2;
-}
-
-// LineForce component `comp` (0: r, 1: theta) for the state vg of one cell.
-template <int NV>
-__device__ __forceinline__ double line_force(const double (&vg)[NV], const LineList &L,
-                                             const WindParams &w, int e0, int e1, int comp)
-{
-  const double rho = vg[RHO] * w.unit_density;
-  const double T = vg[PRS] / vg[RHO] * w.kelvin * w.mu;
-  const double v_th = sqrt((2.0 * kKB * T) / kMP);
-  double g = 0.0;
-  for (int e = e0; e < e1; e++) {
-    const double dvds = L.dvds[e];
-    double M = 0.0;
-    if (dvds > 0.0) {
-      const double t_UV = w.sigma_e * rho * v_th / dvds;
-      M = w.krad * pow(t_UV, w.alpharad);
-      if (M > 4400.) M = 4400.;
-    }
-    const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
-    g += ((1.0 + M) * w.sigma_e * F / kC) / w.unit_acc;
-  }
-  return g;
-}
-
-template <int D, int NV, int LIM, int SOLVER, class TL>
-__device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double *__restrict__ svp,
-                                          double *__restrict__ svm, double *__restrict__ sf,
-                                          double *__restrict__ spr, double *__restrict__ scm,
-                                          double (&U)[NV], double &cdt, bool own, int cx, int cy,
-                                          int gi, int gj, double dt, double dtdV, int e0, int e1,
-                                          const WindStageArgs &A, bool stage1)
-{
-  using G = TileGeom<TL>;
-  constexpr int PX = G::ext(0, D, 2), PY = G::ext(1, D, 2);
-  constexpr int FX = G::ext(0, D, 1), FY = G::ext(1, D, 1);
-  constexpr int NP = PX * PY, NF = FX * FY;
-  constexpr int SST = D == 0 ? 1 : G::SX;
-  constexpr int VN = VX1 + D;
-  const Params &p = A.s.p;
-  const SphGeom &g = A.g;
-  const double gam = p.gamma, gmm1 = p.gmm1;
-  const int ox = blockIdx.x * TL::X, oy = blockIdx.y * TL::Y;
-
-  // (1) PLM with the general-grid weights of the cell
-  for (int q = threadIdx.x; q < NP; q += G::NT) {
-    const int ix = q % PX, iy = q / PX;
-    const int sx = ix + TL::HX - (D == 0), sy = iy + TL::HY - (D == 1);
-    const int s0 = sy * G::SX + sx;
-    // cells past the end of the grid (partial last tile) read the last
-    // weights; their states are never used
-    const int gc = min(D == 0 ? p.beg[0] + ox + ix - 1 : p.beg[1] + oy + iy - 1, p.ntot[D] - 1);
-    const double cp = g.cp[D][gc], cm = g.cm[D][gc], wp = g.wp[D][gc], wm = g.wm[D][gc];
-    const double dp = g.dp[D][gc], dm = g.dm[D][gc];
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      const double vm1 = sv[nv * G::VS + s0 - SST], v0 = sv[nv * G::VS + s0],
-                   vp1 = sv[nv * G::VS + s0 + SST];
-      const double dvp = (vp1 - v0) * wp, dvm = (v0 - vm1) * wm;
-      const double dv = limited_slope_general<LIM>(dvp, dvm, cp, cm);
-      svp[nv * G::NPMAX + q] = v0 + dv * dp;
-      svm[nv * G::NPMAX + q] = v0 - dv * dm;
-    }
-  }
-  __syncthreads();
-
-  // (2) Riemann problem at every face of the tile line
-  for (int q = threadIdx.x; q < NF; q += G::NT) {
-    const int fx = q % FX, fy = q / FX;
-    const int pl = fy * PX + fx;
-    constexpr int PST = D == 0 ? 1 : PX;
-    double vL[NV], vR[NV], f[NV], pr, cmx;
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      vL[nv] = svp[nv * G::NPMAX + pl];
-      vR[nv] = svm[nv * G::NPMAX + pl + PST];
-    }
-    riemann<NV, SOLVER, VN>(vL, vR, gam, gmm1, f, pr, cmx);
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) sf[nv * G::NFMAX + q] = f[nv];
-    spr[q] = pr;
-    scm[q] = cmx;
-  }
-  __syncthreads();
-
-  // (3) curvilinear flux difference, sources, update
-  if (own) {
-    const int ql = cy * FX + cx;
-    constexpr int FST = D == 0 ? 1 : FX;
-    const int qr = ql + FST;
-    double Al, Ar, fl_phi, fr_phi, dtdl;
-    if (D == 0) {
-      Al = g.A1f[gi - 1] * g.dmu[gj];
-      Ar = g.A1f[gi] * g.dmu[gj];
-      fl_phi = g.absx1p[gi - 1];
-      fr_phi = g.absx1p[gi];
-      dtdl = A.s.dtdx[0][gi];
-    } else {
-      Al = g.rdr[gi] * g.sxp[gj - 1];
-      Ar = g.rdr[gi] * g.sxp[gj];
-      fl_phi = g.spabs[gj - 1];
-      fr_phi = g.spabs[gj];
-      dtdl = A.s.dtdx[1][gj] * g.rtinv[gi];
-    }
-    double rhs[NV];
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      double fAl = sf[nv * G::NFMAX + ql] * Al, fAr = sf[nv * G::NFMAX + qr] * Ar;
-      if (nv == VX3) {
-        fAl *= fl_phi;
-        fAr *= fr_phi;
-      }
-      rhs[nv] = -dtdV * (fAr - fAl);
-    }
-    rhs[VN] -= dtdl * (spr[qr] - spr[ql]);
-    rhs[VX3] /= D == 0 ? g.absx1[gi] : g.sn[gj];
-    const double mflux = sf[RHO * G::NFMAX + qr] + sf[RHO * G::NFMAX + ql];
-    double vc[NV];
-    if (D == 0) {
-      // face-averaged state of the cell: mean of its own + and - states
-      constexpr int PSTC = 1;
-      const int pc = cy * PX + cx + PSTC;
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++)
-        vc[nv] = 0.5 * (svp[nv * G::NPMAX + pc] + svm[nv * G::NPMAX + pc]);
-      const double r_1 = g.rinv[gi];
-      const double vphi = vc[VX3];
-      const double Sm = vc[RHO] * (vc[VX2] * vc[VX2] + vphi * vphi);
-      rhs[VX1] += dt * Sm * r_1;
-      if (A.w.body_force) {
-        const double g0 = g.g0[gi];
-        rhs[VX1] += dt * vc[RHO] * g0;
-        rhs[PRS] += dt * 0.5 * mflux * g0;
-      }
-      if (A.w.line_force) {
-        const double gr = line_force<NV>(vc, A.L, A.w, e0, e1, 0);
-        rhs[VX1] += dt * vc[RHO] * gr;
-        rhs[PRS] += dt * 0.5 * mflux * gr;
-      }
-    } else {
-      const int s0 = (cy + TL::HY) * G::SX + cx + TL::HX;
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) vc[nv] = sv[nv * G::VS + s0];
-      const double r_1 = g.rtinv[gi], ct = g.ct[gj];
-      const double vphi = vc[VX3];
-      double Sm = vc[RHO] * (-vc[VX2] * vc[VX1] + ct * vphi * vphi);
-      Sm += 0.0 - ct * 0.0;
-      rhs[VX2] += dt * Sm * r_1;
-      if (A.w.body_force) {
-        const double g1 = 0.0, g2 = 0.0;
-        rhs[VX2] += dt * vc[RHO] * g1;
-        rhs[PRS] += dt * 0.5 * mflux * g1;
-        rhs[VX3] += dt * vc[RHO] * g2;
-        rhs[PRS] += dt * vc[RHO] * vc[VX3] * g2;
-      }
-      if (A.w.line_force) {
-        const double gt = line_force<NV>(vc, A.L, A.w, e0, e1, 1), gz = 0.0;
-        rhs[VX2] += dt * vc[RHO] * gt;
-        rhs[PRS] += dt * 0.5 * mflux * gt;
-        rhs[VX3] += dt * vc[RHO] * gz;
-        rhs[PRS] += dt * vc[RHO] * vc[VX3] * gz;
-      }
-    }
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) U[nv] += rhs[nv];
-    if (stage1) {
-      const double inv_dl = D == 0 ? g.inv_dx1[gi] : g.inv_dx2[gj] * g.rinv[gi];
-      cdt += 0.5 * (scm[ql] + scm[qr]) * inv_dl;
-    }
-  }
-  __syncthreads();
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    blondin_cell(V, xi_s, tr_s, p, w, x1, sc, dt, t, q);
 }
 
 template <int NV, int LIM, int SOLVER, int STAGE>
 __global__ void __launch_bounds__(TileGeom<TileT<2>>::NT)
     k_stage_sph(const __grid_constant__ CUtensorMap tm, const WindStageArgs A)
 {
-  using TL = TileT<2>;
-  using G = TileGeom<TL>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  double *sv = reinterpret_cast<double *>(smem_raw);
-  double *svp = sv + NV * G::VS;
-  double *svm = svp + NV * G::NPMAX;
-  double *sf = svm + NV * G::NPMAX;
-  double *spr = sf + NV * G::NFMAX;
-  double *scm = spr + G::NFMAX;
-  uint64_t *bar = reinterpret_cast<uint64_t *>(scm + G::NFMAX);
-  unsigned &s_flags = *reinterpret_cast<unsigned *>(bar + 1);
-  unsigned long long *s_red = reinterpret_cast<unsigned long long *>(bar + 2);
-
-  const StageArgs &a = A.s;
-  if (a.sc->done) return;
-  const Params &p = a.p;
-  const int tid = threadIdx.x;
-  const int ox = blockIdx.x * TL::X, oy = blockIdx.y * TL::Y;
-  if (tid == 0) {
-    s_flags = 0;
-    mbar_init(bar, 1);
-  }
-  __syncthreads();
-  if (tid == 0) {
-    mbar_expect_tx(bar, (uint32_t)(NV * G::VS * sizeof(double)));
-    tma_load_4d(sv, &tm, ox + p.beg[0] - TL::HX, oy + p.beg[1] - TL::HY, 0, 0, bar);
-  }
-  const bool landed = mbar_wait_bounded(bar, 0, 1u << 22);
-  if (!__syncthreads_and(landed)) {
-    if (tid == 0) {
-      atomicOr(&a.sc->flags, F_TMA_TIMEOUT);
-      mbar_wait_bounded(bar, 0, 1u << 22);
-    }
-    return;
-  }
-
-  const int cx = tid % TL::X, cy = tid / TL::X;
-  const bool own = (ox + cx < p.nx[0]) && (oy + cy < p.nx[1]);
-  const int gi = p.beg[0] + ox + cx, gj = p.beg[1] + oy + cy;
-  const long long cell = (long long)gj * p.px + gi;
-  const double dt = a.sc->dt;
-  const SphGeom &g = A.g;
-
-  double U[NV];
-  double cdt = 0.0, dtdV = 0.0;
-  int e0 = 0, e1 = 0;
-  unsigned flags = 0;
-  if (own) {
-    if constexpr (STAGE == 1) {
-      double v[NV];
-      const int s0 = (cy + TL::HY) * G::SX + cx + TL::HX;
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) v[nv] = sv[nv * G::VS + s0];
-      prim_to_cons<NV>(v, U, p.gmm1);
-    } else {
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) U[nv] = a.Us[nv * p.vstride + cell];
-    }
-    dtdV = dt / (g.dVr[gi] * g.dmu[gj]);
-    if (A.w.line_force) {
-      // VGradCalc for the bins of this cell (line_connect.c:628-738)
-      const int dc = (oy + cy) * p.nx[0] + (ox + cx);
-      e0 = A.L.off[dc];
-      e1 = A.L.off[dc + 1];
-      const int sc0 = (cy + TL::HY) * G::SX + cx + TL::HX;
-      const double *V1 = sv + VX1 * G::VS, *V2 = sv + VX2 * G::VS;
-      const int jm = sc0 - G::SX, jp = sc0 + G::SX;
-      double v11[2], v12[2], v21[2], v22[2], ans1[2];
-      v11[0] = (V1[jm - 1] + V1[jm] + V1[sc0 - 1] + V1[sc0]) / 4.0;
-      v11[1] = (V2[jm - 1] + V2[jm] + V2[sc0 - 1] + V2[sc0]) / 4.0;
-      v12[0] = (V1[jp - 1] + V1[sc0 - 1] + V1[jp] + V1[sc0]) / 4.0;
-      v12[1] = (V2[jp - 1] + V2[sc0 - 1] + V2[jp] + V2[sc0]) / 4.0;
-      v22[0] = (V1[jp] + V1[jp + 1] + V1[sc0 + 1] + V1[sc0]) / 4.0;
-      v22[1] = (V2[jp] + V2[jp + 1] + V2[sc0 + 1] + V2[sc0]) / 4.0;
-      v21[0] = (V1[sc0 + 1] + V1[jm + 1] + V1[jm] + V1[sc0]) / 4.0;
-      v21[1] = (V2[sc0 + 1] + V2[jm + 1] + V2[jm] + V2[sc0]) / 4.0;
-      const double x110 = g.x11a[gi], x111 = g.x11b[gj], x220 = g.x22a[gi], x221 = g.x22b[gj];
-      bilinear(x110, x111, x220, x221, v11, v12, v21, v22, g.locr[gi], g.x2[gj], ans1);
-      const double UV = A.w.unit_velocity;
-      const double vx1 = (ans1[0] * UV * g.sin2[gj] + ans1[1] * UV * g.cos2[gj]);
-      const double vz1 = (ans1[0] * UV * g.cos2[gj] - ans1[1] * UV * g.sin2[gj]);
-      for (int e = e0; e < e1; e++) {
-        const double ds = A.L.ds[e];
-        double dvds;
-        if (ds == -999) {
-          dvds = -999;
-        } else {
-          double ans2[2];
-          bilinear(x110, x111, x220, x221, v11, v12, v21, v22, A.L.roff[e], A.L.toff[e], ans2);
-          const double st = A.L.sinto[e], ctt = A.L.costo[e];
-          const double vx2 = (ans2[0] * UV * st + ans2[1] * UV * ctt);
-          const double vz2 = (ans2[0] * UV * ctt - ans2[1] * UV * st);
-          const int an = A.L.ang[e];
-          const double sa = A.w.sin_a[an], ca = A.w.cos_a[an];
-          const double v1 = sa * vx1 + ca * vz1;
-          const double v2 = sa * vx2 + ca * vz2;
-          dvds = fabs((v2 - v1) / ds);
-        }
-        if (is_nan_bits(dvds)) flags |= F_NAN;
-        A.L.dvds[e] = dvds;
-      }
-    }
-  }
-
-  sweep_sph<0, NV, LIM, SOLVER, TL>(sv, svp, svm, sf, spr, scm, U, cdt, own, cx, cy, gi, gj, dt,
-                                    dtdV, e0, e1, A, STAGE == 1);
-  sweep_sph<1, NV, LIM, SOLVER, TL>(sv, svp, svm, sf, spr, scm, U, cdt, own, cx, cy, gi, gj, dt,
-                                    dtdV, e0, e1, A, STAGE == 1);
-
-  if (own) {
-    double v[NV];
-    if constexpr (STAGE == 2) {
-      double v0[NV], U0[NV];
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
-      prim_to_cons<NV>(v0, U0, p.gmm1);
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) U[nv] = 0.5 * U0[nv] + 0.5 * U[nv];
-    }
-    flags |= cons_to_prim<NV>(U, v, p.gmm1);
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++)
-      if (is_nan_bits(v[nv])) flags |= F_NAN;
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      if constexpr (STAGE == 1) a.Us[nv * p.vstride + cell] = U[nv];
-      a.Vout[nv * p.vstride + cell] = v[nv];
-    }
-  }
-  if (flags) atomicOr(&s_flags, flags);
-  if constexpr (STAGE == 1) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(cdt);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      unsigned long long ob = __shfl_xor_sync(0xffffffffu, b, o);
-      b = ob > b ? ob : b;
-    }
-    if ((tid & 31) == 0) s_red[tid >> 5] = b;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    if constexpr (STAGE == 1) {
-      unsigned long long b = 0;
-#pragma unroll
-      for (int w = 0; w < G::NT / 32; w++) b = s_red[w] > b ? s_red[w] : b;
-      atomicMax(&a.sc->cdt_bits, b);
-    }
-    if (s_flags) {
-      atomicOr(&a.sc->flags, s_flags);
-      if (s_flags & F_NAN) a.sc->done = 1;
-    }
-  }
+  stage_sph_tile<NV, LIM, SOLVER, STAGE, TileT<2>>(&tm, A, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 template <int NV, int LIM, int SOLVER>
