@@ -1,7 +1,7 @@
 """Benchmark of the GB300 hydro path: cell-updates per second, FP64.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
-                    [--workload wind|blast]
+                    [--workload wind|blast|batch]
 
 Workloads (synthetic inputs of the reference's configurations):
   wind   2-D spherical (r, theta) line-driven disk wind, 512 x 256 cells
@@ -12,6 +12,9 @@ Workloads (synthetic inputs of the reference's configurations):
          UV flux, PLM van Leer, HLL, RK2, CFL 0.4; 1000 steps.  Default.
   blast  2-D Cartesian ideal-gas blast wave, 256 x 256, PLM MC, HLLC, RK2,
          CFL 0.4, outflow, seeded 1% density noise; 100 steps.
+  batch  64 independent wind models (grids 128x64 .. 512x256, L_x, k and
+         alpha drawn with seed 4) advanced together by ps_batch_run, timed
+         beside the plain form (each model's ps_run in turn); 100 steps.
 One benchmark step is one time step of the whole grid (split source +
 AdvanceStep + NextTimeStep); the default K is the configured run length,
 restarted from the initial condition after the warm-up.
@@ -61,6 +64,18 @@ class Workload:
             self.desc = ("wind2d-512x256: 2-D spherical line-driven disk wind, PLM-VL, HLL, RK2, "
                          "CFL 0.4, BLONDIN cooling, line force (36 bins), 7 Msun, L_x 1e37")
             self.profile = "stage_kernel_wind_512x256.md"
+        elif name == "batch":
+            import psgb
+            self.specs = psgb.batch_models(64, seed=4)
+            self.nx = self.ny = None
+            self.nvar = 6
+            self.steps = 100
+            self.cpu_steps = 6
+            self.desc = ("wind-batch-64: 64 independent 2-D line-driven disk-wind models (grids "
+                         "drawn from 128x64, 256x128, 384x192, 512x256; L_x log-uniform "
+                         "1e36..1e38 erg/s, k U(0.1,0.4), alpha U(0.5,0.7); seed 4), each as "
+                         "the wind2d workload, all advanced together")
+            self.profile = "stage_kernel_wind_512x256.md"
         else:
             self.nx, self.ny, self.nvar = 256, 256, 5
             self.steps = 100
@@ -68,8 +83,11 @@ class Workload:
             self.desc = ("blast2d-256x256: 2-D Cartesian HD blast, PLM-MC, HLLC, RK2, CFL 0.4, "
                          "outflow, gamma 5/3, seeded 1% density noise")
             self.profile = "stage_kernel_blast2d_256.md"
-        self.cells = self.nx * self.ny
-        self.cooling = name == "wind"
+        if name == "batch":
+            self.cells = sum(sp["grid"][0] * sp["grid"][1] for sp in self.specs)
+        else:
+            self.cells = self.nx * self.ny
+        self.cooling = name in ("wind", "batch")
 
     def solver(self):
         """Device context with the initial state loaded."""
@@ -112,16 +130,25 @@ def _env_rank():
 # ----------------------------------------------------------------------
 
 def _cpu_worker(args):
-    name, steps = args
+    name, steps, idx = args
     wl = Workload(name)
-    o = wl.oracle()
+    if name == "batch":
+        from oracle import wind_oracle
+        sp = wl.specs[idx % len(wl.specs)]
+        o = wind_oracle(sp["grid"][0], sp["grid"][1], l_star=sp["l_star"], krad=sp["krad"],
+                        alpharad=sp["alpharad"])
+        cells = sp["grid"][0] * sp["grid"][1]
+    else:
+        o = wl.oracle()
+        cells = wl.cells
     t0 = time.perf_counter()
     o.run(steps)
-    return time.perf_counter() - t0
+    return time.perf_counter() - t0, cells * steps
 
 
 def cpu_throughput(wl, steps, procs=None):
-    """Independent oracle runs of the workload, one per host core."""
+    """Independent oracle runs of the workload, one per host core (for the
+    batch workload, worker i runs model i of the batch)."""
     import multiprocessing as mp
     import oracle
     oracle.lib()  # build/load before starting workers
@@ -129,16 +156,19 @@ def cpu_throughput(wl, steps, procs=None):
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(n) as pool:
-        per = pool.map(_cpu_worker, [(wl.name, steps)] * n)
+        res = pool.map(_cpu_worker, [(wl.name, steps, i) for i in range(n)])
     wall = time.perf_counter() - t0
-    cells = wl.cells * steps * n
+    per = [r[0] for r in res]
+    cells = sum(r[1] for r in res)
     slowest = max(per)
+    what = (f"models 0..{n - 1} of the batch" if wl.name == "batch"
+            else wl.desc.split(':')[0])
     return {"value": cells / slowest, "unit": "cell-updates/s", "cores": n, "kind": "port",
             "wall_s": slowest,
             "sample": f"{n} concurrent independent runs of the first {steps} steps of "
-                      f"{wl.desc.split(':')[0]} (one per core); time = slowest run's step loop "
+                      f"{what} (one per core); time = slowest run's step loop "
                       f"({slowest:.2f} s; {sum(per):.1f} s of CPU work; set-up excluded)",
-            "single_core_cell_updates_per_s": wl.cells * steps / statistics.median(per)}
+            "single_core_cell_updates_per_s": statistics.median(r[1] / r[0] for r in res)}
 
 
 # ----------------------------------------------------------------------
@@ -317,33 +347,189 @@ def gpu_bench(wl, steps, warmup, rank, world):
         "clocks": clk.summary(),
     }
     if rank == 0:
-        peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
-        hbm_peak = peaks.get("hbm_gbs", 6800.0)
-        alg_bytes_launch = 40 * wl.nvar / 2 * wl.cells
-        achieved = alg_bytes_launch / (stage_ms * 1e-3) / 1e9
-        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                           "frac": achieved / hbm_peak,
-                           "traffic": _profile_value(wl, "traffic_bytes_per_launch"),
-                           "kernel": "stage kernel (fused PLM/Riemann/sources/update), per launch",
-                           "stage_ms": [per_kernel[0], per_kernel[1]],
-                           "other_ms_per_step": per_kernel[2],
-                           "alg_bytes_per_launch": alg_bytes_launch,
-                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"
-                           if "hbm_gbs" in peaks else "fallback 6.8 TB/s (of fallback)"}
-        fp64 = psgb.lib().ps_probe_fp64_flops(5)
-        ops = _profile_value(wl, "fp64_ops_per_cell_stage")
-        out["roofline_fp64"] = {"peak": fp64 / 1e9, "unit": "GFLOP/s",
-                                "peak_source": "ps_probe_fp64_flops (dependent FMA chains, "
-                                               "measured on this GPU; 2 flops per FMA)"}
-        if fp64 > 0 and ops:
-            ach = ops * wl.cells / (stage_ms * 1e-3)
-            out["roofline_fp64"].update({"achieved": ach / 1e9, "frac": ach / fp64,
-                                         "ops_per_cell_stage": ops})
+        _rooflines(out, wl, stage_ms, per_kernel)
         if world == 1:
             out["cpu_baseline"] = cpu_throughput(wl, wl.cpu_steps)
         print(json.dumps(out), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def _batch_e2e(solvers, batch, V0s, steps):
+    """Batch through the C ABI with host arrays: per step every model's
+    Data.Vc copied in from pinned host memory, one ps_batch_run step, every
+    model's Data.Vc copied back."""
+    import torch
+    host = [torch.from_numpy(v.copy()).pin_memory().numpy() for v in V0s]
+    for s in solvers:
+        s.restore()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for s, v in zip(solvers, host):
+            s.set_state(v)
+        batch.run(1)
+        for s, v in zip(solvers, host):
+            s.get_state(out=v)
+    return time.perf_counter() - t0, int(sum(v.nbytes for v in V0s))
+
+
+def batch_bench(wl, steps, warmup, rank, world):
+    """64 wind models: the plain GPU form (each model's ps_run in turn, one
+    graph replay per model and step) against the batched form (ps_batch_run:
+    one launch per phase for all models, one graph replay per step)."""
+    import numpy as np
+    import torch
+    import psgb
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def make():
+        out, V0s = [], []
+        for sp in wl.specs:
+            s = psgb.wind_model_solver(sp)
+            s.set_stream(stream.cuda_stream)
+            s.save()
+            out.append(s)
+            V0s.append(s.get_state())
+        return out, V0s
+
+    def timed(step_fn, restore):
+        for _ in range(warmup):
+            flush.zero_()
+            step_fn()
+        torch.cuda.synchronize()
+        restore()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            torch.cuda.synchronize()
+            for a, b in ev:
+                flush.zero_()
+                a.record(stream)
+                step_fn()
+                b.record(stream)
+            torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        if dist:
+            tt = torch.tensor([ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+            dist.barrier()
+        return ms, clk.summary()
+
+    # plain GPU form
+    plain, _ = make()
+
+    def plain_step():
+        for s in plain:
+            s.run(1)
+
+    def plain_restore():
+        for s in plain:
+            s.restore()
+
+    ms_plain, _ = timed(plain_step, plain_restore)
+    plain_end = [s.get_state() for s in plain[:4]]
+    for s in plain:
+        s.close()
+
+    # batched form
+    solvers, V0s = make()
+    batch = psgb.Batch(solvers)
+    batch.set_stream(stream.cuda_stream)
+    t_tune = time.perf_counter()
+    batch.autotune(reps=5)
+    t_tune = time.perf_counter() - t_tune
+    for s in solvers:
+        s.restore()
+    launches0 = batch.launches()
+    ms, clocks = timed(lambda: batch.run(1), lambda: [s.restore() for s in solvers])
+    launches = batch.launches() - launches0
+    flags = batch.sync()
+    same = all(np.array_equal(a, s.get_state()) for a, s in zip(plain_end, solvers[:4]))
+    value = wl.cells * steps * world / (ms * 1e-3)
+    value_plain = wl.cells * steps * world / (ms_plain * 1e-3)
+    shapes = {}
+    for m, sp in enumerate(wl.specs):
+        shapes["%dx%d" % tuple(sp["grid"])] = "%dx%d" % batch.shape(m)
+
+    for s in solvers:
+        s.restore()
+    per_kernel = np.zeros(3)
+    reps = 10
+    for _ in range(reps):
+        per_kernel += batch.time_step_kernels()
+    per_kernel /= reps
+    stage_ms = 0.5 * (per_kernel[0] + per_kernel[1])
+
+    e2e_steps = min(steps, 20)
+    e2e_wall, bytes_state = _batch_e2e(solvers, batch, V0s, e2e_steps)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (the reference configuration's initial condition, generated)",
+        "config": {"workload": wl.desc, "cells": wl.cells, "models": len(wl.specs),
+                   "method": "batched GPU form (ps_batch_run, one CUDA graph per step)",
+                   "plain_value": value_plain, "plain_ms_per_step": ms_plain / steps,
+                   "speedup_vs_plain": value / value_plain,
+                   "identical_to_plain": same,
+                   "tile_shapes": shapes, "autotune_s": t_tune,
+                   "l2": "256 MiB buffer written before every timed step (L2 flushed)",
+                   "parallelism": "replicas only" if world > 1 else "single GPU"},
+        "e2e": {"value": wl.cells * e2e_steps / e2e_wall, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
+                "steps": e2e_steps,
+                "path": "per step: H2D of every model's Data.Vc, ps_batch_run(1), D2H of every "
+                        "model's Data.Vc (pinned host memory)"},
+        "gpu_launches": int(launches),
+        "device_flags": int(flags),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        _rooflines(out, wl, stage_ms, per_kernel)
+        if world == 1:
+            out["cpu_baseline"] = cpu_throughput(wl, wl.cpu_steps)
+        print(json.dumps(out), flush=True)
+    batch.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def _rooflines(out, wl, stage_ms, per_kernel):
+    import psgb
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    alg_bytes_launch = 40 * wl.nvar / 2 * wl.cells
+    achieved = alg_bytes_launch / (stage_ms * 1e-3) / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                       "frac": achieved / hbm_peak,
+                       "traffic": _profile_value(wl, "traffic_bytes_per_launch"),
+                       "kernel": "stage kernel (fused PLM/Riemann/sources/update), per launch",
+                       "stage_ms": [per_kernel[0], per_kernel[1]],
+                       "other_ms_per_step": per_kernel[2],
+                       "alg_bytes_per_launch": alg_bytes_launch,
+                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"
+                       if "hbm_gbs" in peaks else "fallback 6.8 TB/s (of fallback)"}
+    fp64 = psgb.lib().ps_probe_fp64_flops(5)
+    ops = _profile_value(wl, "fp64_ops_per_cell_stage")
+    out["roofline_fp64"] = {"peak": fp64 / 1e9, "unit": "GFLOP/s",
+                            "peak_source": "ps_probe_fp64_flops (dependent FMA chains, "
+                                           "measured on this GPU; 2 flops per FMA)"}
+    if fp64 > 0 and ops:
+        ach = ops * wl.cells / (stage_ms * 1e-3)
+        out["roofline_fp64"].update({"achieved": ach / 1e9, "frac": ach / fp64,
+                                     "ops_per_cell_stage": ops})
 
 
 def reference_bench(wl, steps, warmup, rank, world):
@@ -360,7 +546,8 @@ def reference_bench(wl, steps, warmup, rank, world):
            "ms_per_step": base["wall_s"] / per_core * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (the reference configuration's initial condition, generated)",
-           "config": {"workload": wl.desc, "cells": wl.cells, "grid": [wl.nx, wl.ny]},
+           "config": {"workload": wl.desc, "cells": wl.cells, "grid": [wl.nx, wl.ny]}
+           if wl.nx else {"workload": wl.desc, "cells": wl.cells, "models": len(wl.specs)},
            "impl": "reference",
            "cpu_baseline": base,
            "e2e": {"value": base["value"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
@@ -374,13 +561,15 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="wind", choices=["wind", "blast"])
+    ap.add_argument("--workload", default="wind", choices=["wind", "blast", "batch"])
     a = ap.parse_args()
     wl = Workload(a.workload)
     steps = a.steps if a.steps is not None else wl.steps
     rank, world = _env_rank()
     if a.impl == "reference":
         reference_bench(wl, steps, a.warmup, rank, world)
+    elif a.workload == "batch":
+        batch_bench(wl, steps, max(a.warmup, 3), rank, world)
     else:
         gpu_bench(wl, steps, max(a.warmup, 3), rank, world)
 

@@ -215,6 +215,37 @@ int ps_get_dt_history(ps_ctx *ctx, double *out, int max);
  * counterpart: lets a host framework order the path with its own work. */
 int ps_set_stream(ps_ctx *ctx, void *stream);
 
+/* ---------------------------------------------------------------- */
+/* batches of independent wind models                                */
+/* ---------------------------------------------------------------- */
+
+/* No reference counterpart (the reference runs one model per process).
+ * Advances n independent line-driven wind contexts (each already set up
+ * with ps_set_grid, ps_set_state, ps_set_time and ps_set_wind; uneven grid
+ * sizes and parameters allowed; same limiter, solver, cooling switch and
+ * step number) together: every phase of a step is one launch over all
+ * models and each step is one CUDA-graph replay; every model keeps its
+ * own dt (its own C_dt reduction and NextTimeStep).  Results are
+ * identical to ps_run on each context.  The contexts stay owned by the
+ * caller and must outlive the batch. */
+typedef struct ps_batch ps_batch;
+int  ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out);
+int  ps_batch_destroy(ps_batch *b);
+int  ps_batch_run(ps_batch *b, int nsteps);
+int  ps_batch_sync(ps_batch *b);      /* OR of every model's PS_F_* flags */
+int  ps_batch_set_stream(ps_batch *b, void *stream);
+long ps_batch_launch_count(const ps_batch *b);
+/* Tile shape of the stage kernels per model: 0 = 32x8, 1 = 16x16,
+ * 2 = 64x4 (model = -1: all models).  ps_batch_autotune times the stage
+ * kernel of every distinct grid size with each shape and keeps the fastest
+ * (`reps` timed launches each); the state is left unchanged. */
+int  ps_batch_set_shape(ps_batch *b, int model, int shape);
+int  ps_batch_get_shape(const ps_batch *b, int model, int *tx, int *ty);
+int  ps_batch_autotune(ps_batch *b, int reps);
+/* One step launched kernel by kernel, timed with CUDA events: ms[0] the
+ * stage-1 launches, ms[1] the stage-2 launches, ms[2] everything else. */
+int  ps_batch_time_step_kernels(ps_batch *b, float ms[3]);
+
 /* Device-side checkpoint / restore of Data.Vc and the main-loop scalars:
  * the backup that FAILSAFE keeps before a step (Src/failsafe.c:5-160),
  * held on the GPU so that a step can be retried or a run replayed. */

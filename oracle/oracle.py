@@ -193,7 +193,7 @@ class Oracle:
         return a[:, 0] if self.dims == 2 else a
 
 
-def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4):
+def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, **params):
     """The 2-D spherical line-driven disk wind (PLM van Leer, HLL, RK2,
     userdef/outflow/axisymmetric/reflective boundaries, point-mass gravity,
     floors, BLONDIN cooling and the line force), initialised."""
@@ -202,8 +202,10 @@ def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4):
                cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling,
                geometry=3, gridtype=WIND_GRID["gridtype"], xbeg=WIND_GRID["xbeg"],
                xend=WIND_GRID["xend"], body_force=1, line_force=line_force, floors=1,
-               params=WIND)
+               params=dict(WIND, **params))
     if line_force:
-        o.set_flux(*synthetic_flux(o.grid(0), o.grid(1), o.ntot))
+        prm = dict(WIND, **params)
+        o.set_flux(*synthetic_flux(o.grid(0), o.grid(1), o.ntot,
+                                   l_uv=prm["l_star"] * prm["f_uv"]))
     o.init_wind()
     return o

@@ -1,0 +1,612 @@
+// ps_batch.cu -- many independent line-driven wind models (uneven grid
+// sizes, own parameters, own dt) advanced together: every phase of a step
+// (split source, boundaries, the two stages, the dt kernel) is ONE launch
+// covering all models, and a whole step (or step pair) is one CUDA graph.
+// The tile shape of the stage kernels is chosen per grid size by a
+// measuring autotuner (ps_batch_autotune).
+//
+// Each model keeps its own context (state, scratch, geometry, flux-bin
+// lists, scalars); the batch holds a device table of per-model arguments
+// and TMA descriptors and the work lists that map CTAs to (model, tile) or
+// (model, cell block).  Results are identical to advancing each model on
+// its own (the per-cell arithmetic does not depend on the tile shape).
+#include "ps_finish.cuh"
+#include "ps_wind_dev.cuh"
+
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <vector>
+
+extern "C" void ps_set_error_msg(const char *msg);
+
+namespace ps {
+
+struct BatchModel {
+  CUtensorMap tm[2];     // V (stage-1 input) and V* (stage-2 input), tile box of the model
+  WindStageArgs st[2];   // stage 1 and stage 2 arguments
+  FinishArgs fin;        // dt kernel arguments (MODE_STEP)
+};
+
+struct TileItem {
+  int m, bx, by, pad;
+};
+struct BlockItem {
+  int m, b;
+};
+
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap *tm)
+{
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm) : "memory");
+}
+
+template <int NV, int LIM, int SOLVER, int STAGE, class TL>
+__global__ void __launch_bounds__(TileGeom<TL>::NT)
+    k_batch_stage(const BatchModel *__restrict__ models, const TileItem *__restrict__ items)
+{
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const TileItem it = items[blockIdx.x];
+  const BatchModel &M = models[it.m];
+  const CUtensorMap *tm = &M.tm[STAGE - 1];
+  if (threadIdx.x == 0) tensormap_acquire(tm);
+  stage_sph_tile<NV, LIM, SOLVER, STAGE, TL>(tm, M.st[STAGE - 1], it.bx, it.by, smem_raw);
+}
+
+template <int NV>
+__global__ void k_batch_bnd_x1(const BatchModel *__restrict__ models,
+                               const BlockItem *__restrict__ blocks, int stage)
+{
+  const BlockItem bi = blocks[blockIdx.x];
+  const WindStageArgs &A = models[bi.m].st[0];
+  if (A.s.sc->done) return;
+  const int q = bi.b * blockDim.x + threadIdx.x;
+  if (q < A.s.p.nx[0] * A.s.p.nx[1])
+    bnd_x1_cell<NV>(stage == 1 ? const_cast<double *>(A.s.Vn) : A.s.Vout, A.s.Us, A.s.p, A.w,
+                    stage, q);
+}
+
+template <int NV>
+__global__ void k_batch_bnd_x2(const BatchModel *__restrict__ models,
+                               const BlockItem *__restrict__ blocks, int stage)
+{
+  const BlockItem bi = blocks[blockIdx.x];
+  const WindStageArgs &A = models[bi.m].st[0];
+  if (A.s.sc->done) return;
+  const int q = bi.b * blockDim.x + threadIdx.x;
+  if (q < A.s.p.ntot[0] * 4)
+    bnd_x2_item<NV>(stage == 1 ? const_cast<double *>(A.s.Vn) : A.s.Vout, A.s.p, q);
+}
+
+__global__ void k_batch_blondin(const BatchModel *__restrict__ models,
+                                const BlockItem *__restrict__ blocks, const double *const *xi,
+                                const double *const *tr)
+{
+  const BlockItem bi = blocks[blockIdx.x];
+  const WindStageArgs &A = models[bi.m].st[0];
+  Scalars *sc = A.s.sc;
+  if (sc->done) return;
+  const int q = bi.b * blockDim.x + threadIdx.x;
+  if (q < A.s.p.nx[0] * A.s.p.nx[1])
+    blondin_cell(const_cast<double *>(A.s.Vn), xi[bi.m], tr[bi.m], A.s.p, A.w, A.g.x1, sc, sc->dt,
+                 sc->t, q);
+}
+
+__global__ void k_batch_finish(const BatchModel *__restrict__ models)
+{
+  finish_block(models[blockIdx.x].fin);
+}
+
+// ------------------------------------------------------------------
+// kernel tables for the tile shapes the autotuner chooses from
+// ------------------------------------------------------------------
+
+constexpr int kNumShapes = 3;
+const int kShapeX[kNumShapes] = {32, 16, 64};
+const int kShapeY[kNumShapes] = {8, 16, 4};
+
+template <int LIM, int SOLVER, class TL>
+static const void *pick_batch(int stage)
+{
+  return stage == 1 ? reinterpret_cast<const void *>(&k_batch_stage<6, LIM, SOLVER, 1, TL>)
+                    : reinterpret_cast<const void *>(&k_batch_stage<6, LIM, SOLVER, 2, TL>);
+}
+
+template <class TL>
+static const void *pick_batch_shape(int lim, int solver, int stage)
+{
+  if (solver == HLL) {
+    if (lim == LIM_VL) return pick_batch<LIM_VL, HLL, TL>(stage);
+    if (lim == LIM_MM) return pick_batch<LIM_MM, HLL, TL>(stage);
+    return pick_batch<LIM_MC, HLL, TL>(stage);
+  }
+  if (lim == LIM_VL) return pick_batch<LIM_VL, HLLC, TL>(stage);
+  if (lim == LIM_MM) return pick_batch<LIM_MM, HLLC, TL>(stage);
+  return pick_batch<LIM_MC, HLLC, TL>(stage);
+}
+
+static const void *batch_kernel(int shape, int lim, int solver, int stage)
+{
+  switch (shape) {
+    case 1: return pick_batch_shape<Tile2D<16, 16>>(lim, solver, stage);
+    case 2: return pick_batch_shape<Tile2D<64, 4>>(lim, solver, stage);
+    default: return pick_batch_shape<Tile2D<32, 8>>(lim, solver, stage);
+  }
+}
+
+static size_t batch_smem(int shape)
+{
+  switch (shape) {
+    case 1: return stage_smem_bytes<6, Tile2D<16, 16>>();
+    case 2: return stage_smem_bytes<6, Tile2D<64, 4>>();
+    default: return stage_smem_bytes<6, Tile2D<32, 8>>();
+  }
+}
+
+}  // namespace ps
+
+// ------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------
+
+struct ps_batch {
+  int n = 0;
+  std::vector<ps_ctx *> ctx;
+  ps::BatchModel *d_models = nullptr;
+  std::vector<ps::BatchModel> h_models;
+  std::vector<int> shape;              // chosen tile shape per model
+  // per shape group: work list of tiles
+  ps::TileItem *d_items[ps::kNumShapes] = {nullptr, nullptr, nullptr};
+  int nitems[ps::kNumShapes] = {0, 0, 0};
+  ps::BlockItem *d_cells = nullptr, *d_x2 = nullptr;
+  int ncells_blocks = 0, nx2_blocks = 0;
+  const double **d_xi = nullptr, **d_tr = nullptr;
+  int lim = 0, solver = 0, cooling = 0;
+  cudaStream_t stream = nullptr;      // stream the work is issued on
+  cudaStream_t own_stream = nullptr;  // stream created by the batch
+  cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};
+  long long host_step = 0;
+  long launches = 0;
+};
+
+static int batch_fail(const char *msg)
+{
+  ps_set_error_msg(msg);
+  return PS_EINVAL;
+}
+
+static int batch_cuda(cudaError_t e, const char *where)
+{
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
+  ps_set_error_msg(buf);
+  return PS_ECUDA;
+}
+
+#define BCK(call)                                          \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return batch_cuda(e_, #call);   \
+  } while (0)
+
+static int encode_box(const ps::Params &p, double *base, int tx, int ty, CUtensorMap *tm)
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    void *fn = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+      return batch_fail("cuTensorMapEncodeTiled entry point not available");
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  cuuint64_t dims[4] = {(cuuint64_t)p.ntot[0], (cuuint64_t)p.ntot[1], (cuuint64_t)p.ntot[2],
+                        (cuuint64_t)p.nvar};
+  cuuint64_t strides[3] = {(cuuint64_t)p.px * 8, (cuuint64_t)p.px * p.ntot[1] * 8,
+                           (cuuint64_t)p.vstride * 8};
+  cuuint32_t box[4] = {(cuuint32_t)(tx + 4), (cuuint32_t)(ty + 4), 1u, (cuuint32_t)p.nvar};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, base, dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return batch_fail("ps_batch: tensor map rejected");
+  return 0;
+}
+
+// Rebuilds the per-model descriptors and the work lists for the current
+// shape choice and uploads them.
+static int batch_upload(ps_batch *b)
+{
+  std::vector<ps::TileItem> items[ps::kNumShapes];
+  std::vector<ps::BlockItem> cells, x2;
+  for (int m = 0; m < b->n; m++) {
+    ps_ctx *c = b->ctx[m];
+    ps::BatchModel &M = b->h_models[m];
+    const ps::Params &p = c->p;
+    const int sh = b->shape[m], tx = ps::kShapeX[sh], ty = ps::kShapeY[sh];
+    int r = encode_box(p, c->V, tx, ty, &M.tm[0]);
+    if (!r) r = encode_box(p, c->Vs, tx, ty, &M.tm[1]);
+    if (r) return r;
+    for (int st = 0; st < 2; st++) {
+      ps::WindStageArgs A = c->wind->a;
+      A.s.Vn = c->V;
+      A.s.Vout = st == 0 ? c->Vs : c->V;
+      A.s.Us = c->Us;
+      for (int d = 0; d < 3; d++) {
+        A.s.dtdx[d] = c->dtdx[d];
+        A.s.inv_dx[d] = c->inv_dx[d];
+      }
+      A.s.sc = c->sc;
+      A.s.p = p;
+      M.st[st] = A;
+    }
+    std::memset(&M.fin, 0, sizeof(M.fin));
+    M.fin.sc = c->sc;
+    M.fin.hist_dt = c->hist;
+    for (int d = 0; d < 3; d++) {
+      M.fin.dtdx[d] = c->dtdx[d];
+      M.fin.dx[d] = c->dx[d];
+    }
+    M.fin.p = p;
+    M.fin.mode = ps::MODE_STEP;
+    const int ntx = (p.nx[0] + tx - 1) / tx, nty = (p.nx[1] + ty - 1) / ty;
+    for (int by = 0; by < nty; by++)
+      for (int bx = 0; bx < ntx; bx++) items[sh].push_back({m, bx, by, 0});
+    const int nc = (p.nx[0] * p.nx[1] + 255) / 256, n2 = (p.ntot[0] * 4 + 255) / 256;
+    for (int k = 0; k < nc; k++) cells.push_back({m, k});
+    for (int k = 0; k < n2; k++) x2.push_back({m, k});
+  }
+  BCK(cudaMemcpy(b->d_models, b->h_models.data(), sizeof(ps::BatchModel) * b->n,
+                 cudaMemcpyHostToDevice));
+  for (int s = 0; s < ps::kNumShapes; s++) {
+    cudaFree(b->d_items[s]);
+    b->d_items[s] = nullptr;
+    b->nitems[s] = (int)items[s].size();
+    if (items[s].empty()) continue;
+    BCK(cudaMalloc(&b->d_items[s], items[s].size() * sizeof(ps::TileItem)));
+    BCK(cudaMemcpy(b->d_items[s], items[s].data(), items[s].size() * sizeof(ps::TileItem),
+                   cudaMemcpyHostToDevice));
+  }
+  cudaFree(b->d_cells);
+  cudaFree(b->d_x2);
+  BCK(cudaMalloc(&b->d_cells, cells.size() * sizeof(ps::BlockItem)));
+  BCK(cudaMalloc(&b->d_x2, x2.size() * sizeof(ps::BlockItem)));
+  BCK(cudaMemcpy(b->d_cells, cells.data(), cells.size() * sizeof(ps::BlockItem),
+                 cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(b->d_x2, x2.data(), x2.size() * sizeof(ps::BlockItem), cudaMemcpyHostToDevice));
+  b->ncells_blocks = (int)cells.size();
+  b->nx2_blocks = (int)x2.size();
+  for (int k = 0; k < 3; k++) {
+    if (b->g[k]) cudaGraphExecDestroy(b->g[k]);
+    b->g[k] = nullptr;
+  }
+  return 0;
+}
+
+static int batch_stage(ps_batch *b, int stage)
+{
+  for (int s = 0; s < ps::kNumShapes; s++) {
+    if (!b->nitems[s]) continue;
+    const void *k = ps::batch_kernel(s, b->lim, b->solver, stage);
+    void *args[2] = {&b->d_models, &b->d_items[s]};
+    BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(256), args, ps::batch_smem(s), b->stream));
+    b->launches++;
+  }
+  return 0;
+}
+
+static int batch_bnd(ps_batch *b, int stage)
+{
+  ps::k_batch_bnd_x1<6><<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, stage);
+  ps::k_batch_bnd_x2<6><<<b->nx2_blocks, 256, 0, b->stream>>>(b->d_models, b->d_x2, stage);
+  b->launches += 2;
+  return 0;
+}
+
+static int batch_cool(ps_batch *b)
+{
+  if (!b->cooling) return 0;
+  ps::k_batch_blondin<<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, b->d_xi,
+                                                               b->d_tr);
+  b->launches++;
+  return 0;
+}
+
+static int batch_step(ps_batch *b, int odd)
+{
+  int r = 0;
+  if (odd) r = batch_cool(b);
+  for (int st = 1; !r && st <= 2; st++) {
+    r = batch_bnd(b, st);
+    if (!r) r = batch_stage(b, st);
+  }
+  if (!r && !odd) r = batch_cool(b);
+  if (!r) {
+    ps::k_batch_finish<<<b->n, 256, 0, b->stream>>>(b->d_models);
+    b->launches++;
+  }
+  return r;
+}
+
+static void batch_free(ps_batch *b)
+{
+  if (!b) return;
+  for (int k = 0; k < 3; k++)
+    if (b->g[k]) cudaGraphExecDestroy(b->g[k]);
+  cudaFree(b->d_models);
+  for (int s = 0; s < ps::kNumShapes; s++) cudaFree(b->d_items[s]);
+  cudaFree(b->d_cells);
+  cudaFree(b->d_x2);
+  cudaFree(b->d_xi);
+  cudaFree(b->d_tr);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+}
+
+extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
+{
+  if (!ctxs || n <= 0 || !out) return batch_fail("ps_batch_create: bad arguments");
+  *out = nullptr;
+  for (int m = 0; m < n; m++) {
+    ps_ctx *c = ctxs[m];
+    if (!c || !c->wind) return batch_fail("ps_batch_create: every model needs ps_set_wind");
+    if (c->p.limiter != ctxs[0]->p.limiter || c->p.solver != ctxs[0]->p.solver ||
+        c->p.cooling != ctxs[0]->p.cooling || c->host_step != ctxs[0]->host_step)
+      return batch_fail("ps_batch_create: models must share limiter, solver, cooling and step");
+  }
+  ps_batch *b = new ps_batch();
+  b->n = n;
+  b->ctx.assign(ctxs, ctxs + n);
+  b->h_models.resize(n);
+  b->shape.assign(n, 0);
+  b->lim = ctxs[0]->p.limiter;
+  b->solver = ctxs[0]->p.solver;
+  b->cooling = ctxs[0]->p.cooling;
+  b->host_step = ctxs[0]->host_step;
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_models, sizeof(ps::BatchModel) * n)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_xi, sizeof(double *) * n)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_tr, sizeof(double *) * n)) != cudaSuccess) {
+    batch_free(b);
+    return batch_cuda(e, "ps_batch_create");
+  }
+  b->stream = b->own_stream;
+  std::vector<const double *> xi(n), tr(n);
+  for (int m = 0; m < n; m++) {
+    xi[m] = ctxs[m]->wind->xi;
+    tr[m] = ctxs[m]->wind->tr;
+    cudaStreamSynchronize(ctxs[m]->stream);
+  }
+  cudaMemcpy(b->d_xi, xi.data(), sizeof(double *) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_tr, tr.data(), sizeof(double *) * n, cudaMemcpyHostToDevice);
+  for (int s = 0; s < ps::kNumShapes; s++) {
+    for (int st = 1; st <= 2; st++) {
+      e = cudaFuncSetAttribute(ps::batch_kernel(s, b->lim, b->solver, st),
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)ps::batch_smem(s));
+      if (e != cudaSuccess) {
+        batch_free(b);
+        return batch_cuda(e, "ps_batch_create: smem attribute");
+      }
+    }
+  }
+  int r = batch_upload(b);
+  if (r) {
+    batch_free(b);
+    return r;
+  }
+  *out = b;
+  return 0;
+}
+
+extern "C" int ps_batch_destroy(ps_batch *b)
+{
+  if (!b) return PS_EINVAL;
+  cudaStreamSynchronize(b->stream);
+  batch_free(b);
+  return 0;
+}
+
+extern "C" int ps_batch_set_shape(ps_batch *b, int model, int shape)
+{
+  if (!b || model < -1 || model >= b->n || shape < 0 || shape >= ps::kNumShapes)
+    return batch_fail("ps_batch_set_shape: bad arguments");
+  if (model < 0)
+    std::fill(b->shape.begin(), b->shape.end(), shape);
+  else
+    b->shape[model] = shape;
+  BCK(cudaStreamSynchronize(b->stream));
+  return batch_upload(b);
+}
+
+extern "C" int ps_batch_get_shape(const ps_batch *b, int model, int *tx, int *ty)
+{
+  if (!b || model < 0 || model >= b->n) return batch_fail("ps_batch_get_shape: bad arguments");
+  if (tx) *tx = ps::kShapeX[b->shape[model]];
+  if (ty) *ty = ps::kShapeY[b->shape[model]];
+  return b->shape[model];
+}
+
+// For every distinct grid size of the batch, time the stage-1 kernel of
+// those models with each candidate tile shape (CUDA events, `reps`
+// launches after one warm-up) and keep the fastest.  The state is not
+// changed: the scalars each model's stage 1 touches are saved and put back.
+extern "C" int ps_batch_autotune(ps_batch *b, int reps)
+{
+  if (!b) return PS_EINVAL;
+  if (reps <= 0) reps = 5;
+  BCK(cudaStreamSynchronize(b->stream));
+  std::vector<ps::Scalars> saved(b->n);
+  for (int m = 0; m < b->n; m++)
+    BCK(cudaMemcpy(&saved[m], b->ctx[m]->sc, sizeof(ps::Scalars), cudaMemcpyDeviceToHost));
+  std::map<std::pair<int, int>, std::vector<int>> groups;
+  for (int m = 0; m < b->n; m++) groups[{b->ctx[m]->p.nx[0], b->ctx[m]->p.nx[1]}].push_back(m);
+  const std::vector<int> orig = b->shape;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (auto &g : groups) {
+    float best = 1e30f;
+    int best_s = 0;
+    for (int s = 0; s < ps::kNumShapes; s++) {
+      // only this group's models are timed: the others get no items
+      std::vector<ps::TileItem> items;
+      for (int m : g.second) {
+        ps_ctx *c = b->ctx[m];
+        const int tx = ps::kShapeX[s], ty = ps::kShapeY[s];
+        const int ntx = (c->p.nx[0] + tx - 1) / tx, nty = (c->p.nx[1] + ty - 1) / ty;
+        for (int by = 0; by < nty; by++)
+          for (int bx = 0; bx < ntx; bx++) items.push_back({m, bx, by, 0});
+        b->shape[m] = s;
+      }
+      int r = batch_upload(b);
+      if (r) return r;
+      ps::TileItem *d_items = nullptr;
+      BCK(cudaMalloc(&d_items, items.size() * sizeof(ps::TileItem)));
+      BCK(cudaMemcpy(d_items, items.data(), items.size() * sizeof(ps::TileItem),
+                     cudaMemcpyHostToDevice));
+      const void *k = ps::batch_kernel(s, b->lim, b->solver, 1);
+      void *args[2] = {&b->d_models, &d_items};
+      BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(256), args, ps::batch_smem(s),
+                           b->stream));
+      BCK(cudaEventRecord(e0, b->stream));
+      for (int it = 0; it < reps; it++)
+        BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(256), args, ps::batch_smem(s),
+                             b->stream));
+      BCK(cudaEventRecord(e1, b->stream));
+      BCK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      cudaFree(d_items);
+      if (ms < best) {
+        best = ms;
+        best_s = s;
+      }
+    }
+    for (int m : g.second) b->shape[m] = best_s;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  (void)orig;
+  for (int m = 0; m < b->n; m++)
+    BCK(cudaMemcpy(b->ctx[m]->sc, &saved[m], sizeof(ps::Scalars), cudaMemcpyHostToDevice));
+  return batch_upload(b);
+}
+
+static int batch_graph(ps_batch *b, int kind, cudaGraphExec_t *out)
+{
+  cudaGraph_t g;
+  const long before = b->launches;
+  BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  int r = 0;
+  if (kind == 0 || kind == 2) r = batch_step(b, 0);
+  if (!r && (kind == 1 || kind == 2)) r = batch_step(b, 1);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  b->launches = before;
+  if (r) return r;
+  if (e != cudaSuccess) return batch_cuda(e, "ps_batch: capture");
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return batch_cuda(e, "ps_batch: instantiate");
+  return 0;
+}
+
+extern "C" int ps_batch_run(ps_batch *b, int nsteps)
+{
+  if (!b || nsteps < 0) return PS_EINVAL;
+  int nshape = 0;
+  for (int s = 0; s < ps::kNumShapes; s++) nshape += b->nitems[s] > 0;
+  const long per_step = 4 + 2 * nshape + (b->cooling ? 1 : 0) + 1;
+  for (int k = 0; k < 3; k++)
+    if (!b->g[k]) {
+      int r = batch_graph(b, k, &b->g[k]);
+      if (r) return r;
+    }
+  b->host_step = b->ctx[0]->host_step;   // follows ps_restore_state of the contexts
+  int left = nsteps;
+  while (left > 0) {
+    const int odd = (int)(b->host_step & 1);
+    if (!odd && left >= 2) {
+      BCK(cudaGraphLaunch(b->g[2], b->stream));
+      b->launches += 2 * per_step;
+      b->host_step += 2;
+      left -= 2;
+    } else {
+      BCK(cudaGraphLaunch(b->g[odd], b->stream));
+      b->launches += per_step;
+      b->host_step += 1;
+      left -= 1;
+    }
+  }
+  for (ps_ctx *c : b->ctx) c->host_step = b->host_step;
+  BCK(cudaGetLastError());
+  return 0;
+}
+
+extern "C" int ps_batch_sync(ps_batch *b)
+{
+  if (!b) return PS_EINVAL;
+  BCK(cudaStreamSynchronize(b->stream));
+  unsigned all = 0;
+  for (ps_ctx *c : b->ctx) {
+    unsigned f = 0;
+    BCK(cudaMemcpy(&f, &c->sc->flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    all |= f;
+  }
+  return (int)all;
+}
+
+extern "C" int ps_batch_set_stream(ps_batch *b, void *stream)
+{
+  if (!b) return PS_EINVAL;
+  BCK(cudaStreamSynchronize(b->stream));
+  b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+  return 0;
+}
+
+extern "C" long ps_batch_launch_count(const ps_batch *b) { return b ? b->launches : -1; }
+
+// One step issued launch by launch with CUDA events between the phases:
+// ms[0] = the stage-1 launches, ms[1] = the stage-2 launches, ms[2] = the
+// rest (boundaries, split source, dt kernel).  Advances the models.
+extern "C" int ps_batch_time_step_kernels(ps_batch *b, float *ms)
+{
+  if (!b || !ms) return PS_EINVAL;
+  cudaEvent_t ev[8];
+  for (int k = 0; k < 8; k++) BCK(cudaEventCreate(&ev[k]));
+  b->host_step = b->ctx[0]->host_step;
+  const int odd = (int)(b->host_step & 1);
+  int r = 0;
+  BCK(cudaEventRecord(ev[0], b->stream));
+  if (odd) r = batch_cool(b);
+  if (!r) r = batch_bnd(b, 1);
+  BCK(cudaEventRecord(ev[1], b->stream));
+  if (!r) r = batch_stage(b, 1);
+  BCK(cudaEventRecord(ev[2], b->stream));
+  if (!r) r = batch_bnd(b, 2);
+  BCK(cudaEventRecord(ev[3], b->stream));
+  if (!r) r = batch_stage(b, 2);
+  BCK(cudaEventRecord(ev[4], b->stream));
+  if (!r && !odd) r = batch_cool(b);
+  if (!r) {
+    ps::k_batch_finish<<<b->n, 256, 0, b->stream>>>(b->d_models);
+    b->launches++;
+  }
+  BCK(cudaEventRecord(ev[5], b->stream));
+  BCK(cudaEventSynchronize(ev[5]));
+  float t[5];
+  for (int k = 0; k < 5; k++) cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]);
+  for (int k = 0; k < 8; k++) cudaEventDestroy(ev[k]);
+  if (r) return r;
+  BCK(cudaGetLastError());
+  b->host_step++;
+  for (ps_ctx *c : b->ctx) c->host_step = b->host_step;
+  ms[0] = t[1];
+  ms[1] = t[3];
+  ms[2] = t[0] + t[2] + t[4];
+  return 0;
+}

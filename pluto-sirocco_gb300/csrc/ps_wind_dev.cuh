@@ -238,7 +238,7 @@ __device__ __forceinline__ double bl_func(const BlCtx &b, int which, double x)
   return which == 0 ? bl_zfunc(b, x) : bl_heatcool(b, x);
 }
 
-__device__ double bl_zbrent(const BlCtx &bc, int which, double x1, double x2, double tol)
+static __device__ __noinline__ double bl_zbrent(const BlCtx &bc, int which, double x1, double x2, double tol)
 {
   const double EPS = 3.0e-8;
   double a = x1, b = x2, c = x2, d = 0.0, e = 0.0;

@@ -26,7 +26,10 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_advance_step", "ps_run", "ps_sync", "ps_device_state", "ps_launch_count",
            "ps_get_dt_history", "ps_set_stream", "ps_probe_fp64_flops", "ps_save_state",
            "ps_restore_state", "ps_time_step_kernels", "ps_advance_step_noalloc",
-           "ps_init_wind", "ps_wind_synthetic_flux", "ps_set_wind", "ps_split_source"]
+           "ps_init_wind", "ps_wind_synthetic_flux", "ps_set_wind", "ps_split_source",
+           "ps_batch_create", "ps_batch_destroy", "ps_batch_run", "ps_batch_sync",
+           "ps_batch_set_stream", "ps_batch_launch_count", "ps_batch_set_shape",
+           "ps_batch_get_shape", "ps_batch_autotune", "ps_batch_time_step_kernels"]
 
 
 class Config(ctypes.Structure):
@@ -106,6 +109,17 @@ def lib():
                                              DP, DP, DP, DP]
         L.ps_set_wind.argtypes = [P, ctypes.POINTER(Wind), DP, DP, DP]
         L.ps_split_source.argtypes = [P, D, D]
+        L.ps_batch_create.argtypes = [ctypes.POINTER(P), I, ctypes.POINTER(P)]
+        L.ps_batch_destroy.argtypes = [P]
+        L.ps_batch_run.argtypes = [P, I]
+        L.ps_batch_sync.argtypes = [P]
+        L.ps_batch_set_stream.argtypes = [P, P]
+        L.ps_batch_launch_count.argtypes = [P]
+        L.ps_batch_launch_count.restype = ctypes.c_long
+        L.ps_batch_set_shape.argtypes = [P, I, I]
+        L.ps_batch_get_shape.argtypes = [P, I, ctypes.POINTER(I), ctypes.POINTER(I)]
+        L.ps_batch_autotune.argtypes = [P, I]
+        L.ps_batch_time_step_kernels.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
         _lib = L
     return _lib
 
@@ -306,3 +320,87 @@ class Solver:
         pitch = ctypes.c_int()
         ptr = lib().ps_device_state(self.ctx, ctypes.byref(pitch))
         return ptr, pitch.value
+
+
+class Batch:
+    """Independent wind models advanced together (ps_batch)."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (ctypes.c_void_p * len(self.solvers))(*[s.ctx.value for s in self.solvers])
+        self.h = ctypes.c_void_p()
+        check(lib().ps_batch_create(arr, len(self.solvers), ctypes.byref(self.h)),
+              "ps_batch_create")
+
+    def close(self):
+        if self.h:
+            lib().ps_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, nsteps):
+        check(lib().ps_batch_run(self.h, nsteps), "ps_batch_run")
+        return self.sync()
+
+    def sync(self):
+        return check(lib().ps_batch_sync(self.h), "ps_batch_sync")
+
+    def set_stream(self, handle):
+        check(lib().ps_batch_set_stream(self.h, ctypes.c_void_p(handle)), "ps_batch_set_stream")
+
+    def launches(self):
+        return lib().ps_batch_launch_count(self.h)
+
+    def set_shape(self, shape, model=-1):
+        check(lib().ps_batch_set_shape(self.h, model, shape), "ps_batch_set_shape")
+
+    def shape(self, model):
+        tx, ty = ctypes.c_int(), ctypes.c_int()
+        lib().ps_batch_get_shape(self.h, model, ctypes.byref(tx), ctypes.byref(ty))
+        return tx.value, ty.value
+
+    def autotune(self, reps=5):
+        check(lib().ps_batch_autotune(self.h, reps), "ps_batch_autotune")
+
+    def time_step_kernels(self):
+        ms = (ctypes.c_float * 3)()
+        check(lib().ps_batch_time_step_kernels(self.h, ms), "ps_batch_time_step_kernels")
+        return np.array(ms[:], dtype=np.float64)
+
+
+# Grid sizes and parameter ranges of the batched-wind configuration.
+BATCH_GRIDS = [(128, 64), (256, 128), (384, 192), (512, 256)]
+
+
+def batch_models(n=64, seed=4):
+    """Per-model (grid, L_x, krad, alpha) drawn with numpy's seeded generator:
+    L_x log-uniform in 1e36..1e38 erg/s, k uniform in 0.1..0.4, alpha
+    uniform in 0.5..0.7 (M = k t^-alpha), grid uniform over BATCH_GRIDS."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        g = BATCH_GRIDS[int(rng.integers(0, len(BATCH_GRIDS)))]
+        lx = 10 ** rng.uniform(36.0, 38.0)
+        k = rng.uniform(0.1, 0.4)
+        a = rng.uniform(0.5, 0.7)
+        out.append(dict(grid=g, l_star=lx, krad=k, alpharad=-a))
+    return out
+
+
+def wind_model_solver(spec, cooling=1, line_force=1):
+    """One wind context for a batch spec (see batch_models)."""
+    nr, nt = spec["grid"]
+    cfg = make_wind_config(nr, nt, cooling=cooling)
+    w = make_wind(line_force=line_force, l_star=spec["l_star"], krad=spec["krad"],
+                  alpharad=spec["alpharad"])
+    g = WindGrid(cfg)
+    s = Solver(cfg, g)
+    s.set_state(wind_state(cfg, w, g))
+    s.set_time(0.0, 1e-4, 0)
+    s.set_wind(w, wind_flux(cfg, w, g) if line_force else None)
+    return s

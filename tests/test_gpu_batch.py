@@ -1,0 +1,76 @@
+"""Batched wind models (ps_batch): several independent line-driven wind
+models of uneven grid sizes and parameters advanced together must give
+exactly what each model gives when advanced on its own with ps_run, for
+every tile shape and after the autotuner has chosen shapes."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [
+    dict(grid=(64, 32), l_star=1e37, krad=0.2, alpharad=-0.6),
+    dict(grid=(96, 48), l_star=3e36, krad=0.35, alpharad=-0.52),
+    dict(grid=(128, 64), l_star=6e37, krad=0.12, alpharad=-0.68),
+]
+
+
+def _pairs(cooling):
+    # without cooling: the hydro-only wind (no line force either), as the
+    # reference's hydro-only configuration
+    import psgb
+    solo = [psgb.wind_model_solver(s, cooling=cooling, line_force=cooling) for s in SPECS]
+    inb = [psgb.wind_model_solver(s, cooling=cooling, line_force=cooling) for s in SPECS]
+    return solo, inb
+
+
+def _check_equal(solo, inb):
+    for m, (a, b) in enumerate(zip(solo, inb)):
+        va, vb = a.get_state(), b.get_state()
+        d = np.abs(va - vb)
+        assert np.array_equal(va, vb), f"model {m}: {np.count_nonzero(d)} values differ, max {d.max():.3e}"
+        assert a.time()[:2] == b.time()[:2], f"model {m}: t/dt differ"
+
+
+@pytest.mark.parametrize("cooling", [0, 1])
+def test_batch_matches_individual_runs(built, cooling):
+    import psgb
+    solo, inb = _pairs(cooling)
+    batch = psgb.Batch(inb)
+    for chunk in (7, 6):   # odd then even chunk: every step graph is used
+        flags = 0
+        for s in solo:
+            flags |= s.run(chunk)
+        assert batch.run(chunk) == flags
+        _check_equal(solo, inb)
+    batch.close()
+
+
+def test_batch_tile_shapes_and_autotune(built):
+    import psgb
+    solo, inb = _pairs(1)
+    batch = psgb.Batch(inb)
+    batch.set_shape(1, model=0)
+    batch.set_shape(2, model=2)
+    assert batch.shape(0) == (16, 16) and batch.shape(1) == (32, 8) and batch.shape(2) == (64, 4)
+    for s in solo:
+        s.run(5)
+    batch.run(5)
+    _check_equal(solo, inb)
+    t_before = [b.time()[:2] for b in inb]
+    batch.autotune(reps=3)
+    assert [b.time()[:2] for b in inb] == t_before   # the autotuner leaves the state alone
+    for s in solo:
+        s.run(6)
+    batch.run(6)
+    _check_equal(solo, inb)
+    for m in range(len(SPECS)):
+        assert batch.shape(m) in [(32, 8), (16, 16), (64, 4)]
+    batch.close()
+
+
+def test_batch_rejects_mixed_models(built):
+    import psgb
+    a = psgb.wind_model_solver(SPECS[0], cooling=1)
+    b = psgb.wind_model_solver(SPECS[1], cooling=0)
+    with pytest.raises(RuntimeError):
+        psgb.Batch([a, b])
