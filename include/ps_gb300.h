@@ -246,6 +246,67 @@ int  ps_batch_autotune(ps_batch *b, int reps);
  * stage-1 launches, ms[1] the stage-2 launches, ms[2] everything else. */
 int  ps_batch_time_step_kernels(ps_batch *b, float ms[3]);
 
+/* ---------------------------------------------------------------- */
+/* learned cooling step (surrogate of BLONDIN)                       */
+/* ---------------------------------------------------------------- */
+
+/* No reference counterpart.  A 4 -> 64 -> 64 -> 1 SiLU network maps
+ * (log10 n_H [cm^-3], log10 T [K], log10 xi, log10 dt [s]) to
+ * log10 T_new of one BLONDIN solve (Src/Cooling/BLONDIN/cooling.c:50-165,
+ * prefactors 1, T_x and mu fixed); it runs on the tensor cores (BF16
+ * weights, FP32 accumulation).  Per cell, FP64 Newton steps on BLONDIN's
+ * implicit energy equation judge and polish the result: a cell whose
+ * residual at the old temperature is already within 1e-3 of its thermal
+ * energy takes one Newton step from there; a stiff cell iterates from the
+ * network's prediction (at most 5 net-rate evaluations in all).  A cell is
+ * left to the reference method (bracket + Brent) when its inputs leave the
+ * box, when the residual does not reach 1e-3, or when the net rate changes
+ * sign (the reference's equilibrium branch).
+ * Parameter vector (FP32, 4545 values): W1[64][4], b1[64], W2[64][64],
+ * b2[64], w3[64], b3. */
+typedef struct ps_surrogate ps_surrogate;
+typedef struct {
+  double lo[4], hi[4];   /* log10 bounds of n_H, T, xi, dt (the training box) */
+  double t_x, mu;        /* X-ray temperature [K] and mean molecular weight */
+} ps_sg_box;
+enum { PS_SG_ACCEPT = 0, PS_SG_OUT_OF_BOX = 1, PS_SG_REJECT = 2, PS_SG_BELOW_MIN = 3 };
+
+int ps_sg_create(const ps_sg_box *box, ps_surrogate **out);
+int ps_sg_destroy(ps_surrogate *s);
+int ps_sg_set_params(ps_surrogate *s, const float *params);
+int ps_sg_get_params(const ps_surrogate *s, float *params);
+/* T_new of the reference method on the GPU for n tuples (row-major
+ * n x 4: n_H, T, xi, dt [s]): the training labels.  t_cool (may be NULL)
+ * gets the cooling time E / |net rate| at T in seconds. */
+int ps_sg_label(ps_surrogate *s, const double *tuples, long n, double *t_new, double *t_cool);
+/* Training set (tuples inside the box are used) and Adam training on the
+ * GPU: `steps` minibatches of `batch` rows (multiple of 128), learning
+ * rate cosine-decayed from lr to lr_end; loss_hist[steps] (may be NULL)
+ * gets the mean squared error of (log10 T_new - log10 T) / 4 per step. */
+int ps_sg_set_data(ps_surrogate *s, const double *tuples, const double *t_new, long n);
+int ps_sg_train(ps_surrogate *s, int steps, int batch, float lr, float lr_end,
+                unsigned long long seed, float *loss_hist);
+/* Loss and gradient (4545 values, the parameter layout) of the mean
+ * squared error over n tuples, without an update. */
+int ps_sg_grad(ps_surrogate *s, const double *tuples, const double *t_new, int n,
+               float *grad, float *loss);
+/* The surrogate cooling step on n tuples: t_out (after the 1e4 K floor),
+ * status (PS_SG_*), t_mlp (network prediction, may be NULL).  use_net = 0
+ * starts the Newton steps from T instead of the prediction. */
+int ps_sg_predict(ps_surrogate *s, const double *tuples, long n, int use_net,
+                  double *t_out, int *status, double *t_mlp);
+/* Counters since the last reset: cells accepted, out of box, rejected by
+ * the judge, below 1e4 K; net-rate evaluations made by the judge; stiff
+ * cells (not already within the residual at the old temperature). */
+int ps_sg_stats(ps_surrogate *s, long long out[6], int reset);
+/* Use the surrogate in the wind context's split-source step (NULL: the
+ * reference method).  use_net as in ps_sg_predict. */
+int ps_set_surrogate(ps_ctx *ctx, ps_surrogate *s, int use_net);
+int ps_batch_set_surrogate(ps_batch *b, ps_surrogate *s, int use_net);
+/* (n_H, T, xi, dt [s]) of every cell the next split-source step of the
+ * wind context would solve (at most cap rows); *n = rows written. */
+int ps_sg_collect(ps_ctx *ctx, double *tuples, long cap, long *n);
+
 /* Device-side checkpoint / restore of Data.Vc and the main-loop scalars:
  * the backup that FAILSAFE keeps before a step (Src/failsafe.c:5-160),
  * held on the GPU so that a step can be retried or a run replayed. */

@@ -68,6 +68,8 @@ def lib():
         L.or_init_wind.argtypes = [P]
         L.or_set_flux.argtypes = [P, I, DP, DP, DP]
         L.or_cooling.argtypes = [P, D, D]
+        L.or_blondin_point.restype = D
+        L.or_blondin_point.argtypes = [D, D, D, D, D, D]
         L.or_sirocco_xi.restype = DP
         L.or_sirocco_xi.argtypes = [P]
         _lib = L
@@ -209,3 +211,10 @@ def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, *
                                    l_uv=prm["l_star"] * prm["f_uv"]))
     o.init_wind()
     return o
+
+
+def blondin_points(tuples, tx=5.6e7, mu=0.6):
+    """BLONDIN T_new for rows (n_H, T, xi, dt_seconds) (or_blondin_point)."""
+    L = lib()
+    return np.array([L.or_blondin_point(float(r[0]), float(r[1]), float(r[2]), tx, float(r[3]), mu)
+                     for r in np.asarray(tuples, dtype=np.float64)])

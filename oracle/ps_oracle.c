@@ -1316,6 +1316,46 @@ void or_cooling(or_sim *s, double dt, double t)
   }
 }
 
+/* One BLONDIN solve for a (n_H, T, xi, T_x, dt) tuple, prefactors 1
+ * (cooling.c:95-162 with the per-cell quantities given): the thermal
+ * energy is E = T n kB / (2/3) with n = n_H 1.43 / mu, and the result is
+ * T_f after the 1e4 K floor; T below 1e4 K is returned unchanged.  This is
+ * how the surrogate's training pairs and its fallback are defined. */
+double or_blondin_point(double nH, double T, double xi, double tx, double dt_s, double mu)
+{
+  bl_ctx b;
+  double t_l, t_u, test, T_f;
+  memset(&b, 0, sizeof(b));
+  b.comp_c_pre = b.comp_h_pre = b.line_c_pre = b.brem_c_pre = b.xray_h_pre = 1.0;
+  if (T < 1.e4) return T;
+  b.dt_share = dt_s;
+  b.nH = nH;
+  b.n = nH * 1.43 / mu;
+  b.E = T * b.n * C_KB / (2.0 / 3.0);
+  b.xi = xi;
+  b.tx = tx;
+  b.sqxi = sqrt(b.xi);
+  b.sqsqxi = pow(b.xi, 0.25);
+  b.hc_init = bl_heatcool(&b, T);
+  t_l = T * 0.9;
+  t_u = T * 1.1;
+  test = bl_zfunc(&b, t_l) * bl_zfunc(&b, t_u);
+  while (test > 0 && test == test) {
+    t_l *= 0.9;
+    t_u *= 1.1;
+    test = bl_zfunc(&b, t_l) * bl_zfunc(&b, t_u);
+  }
+  if (test != test) {
+    T_f = T;
+  } else {
+    double hc_final;
+    T_f = bl_zbrent(&b, 0, t_l, t_u, 1.0);
+    hc_final = bl_heatcool(&b, T_f);
+    if (hc_final * b.hc_init < 0.0) T_f = bl_zbrent(&b, 1, fmin(T_f, T), fmax(T_f, T), 1.0);
+  }
+  return MAXD(T_f, 1.e4);
+}
+
 /* RK2 AdvanceStep (rk_step.c:29-384) */
 static int advance_step(or_sim *s)
 {

@@ -99,6 +99,7 @@ int     or_history(const or_sim *s, double *dt_used, double *inv_dt, int max);
 /* One BLONDIN cooling pass over the active cells with the given dt and
  * simulation time (BlondinCooling, Src/Cooling/BLONDIN/cooling.c:50-165). */
 void    or_cooling(or_sim *s, double dt, double t);
+double  or_blondin_point(double nH, double T, double xi, double tx, double dt_s, double mu);
 
 /* Frozen ionisation parameter and radiation temperature per cell
  * ([k][j][i], total box). */

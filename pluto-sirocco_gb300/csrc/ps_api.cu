@@ -121,9 +121,30 @@ int ps_wind_cool_launch(ps_ctx *c);
 int ps_wind_bnd_launch(ps_ctx *c, int stage);
 int ps_wind_stage_launch(ps_ctx *c, int stage);
 
+void ps_sg_free_ctx(ps_ctx *c);
+
+// Drops the captured step graphs (they are rebuilt at the next ps_run).
+void ps_ctx_invalidate_graphs(ps_ctx *c)
+{
+  for (int k = 0; k < 3; k++)
+    if (c->gw[k]) {
+      cudaGraphExecDestroy(c->gw[k]);
+      c->gw[k] = nullptr;
+    }
+  if (c->g1) {
+    cudaGraphExecDestroy(c->g1);
+    c->g1 = nullptr;
+  }
+  if (c->gN) {
+    cudaGraphExecDestroy(c->gN);
+    c->gN = nullptr;
+  }
+}
+
 static void free_ctx(ps_ctx *c)
 {
   if (!c) return;
+  ps_sg_free_ctx(c);
   if (c->wind) ps_wind_free(c->wind);
   for (int k = 0; k < 3; k++)
     if (c->gw[k]) cudaGraphExecDestroy(c->gw[k]);

@@ -11,6 +11,7 @@
 // (model, cell block).  Results are identical to advancing each model on
 // its own (the per-cell arithmetic does not depend on the tile shape).
 #include "ps_finish.cuh"
+#include "ps_surrogate_cool.cuh"
 #include "ps_wind_dev.cuh"
 
 #include <cudaTypedefs.h>
@@ -94,6 +95,46 @@ __global__ void k_batch_blondin(const BatchModel *__restrict__ models,
                  sc->t, q);
 }
 
+// The split-source step with the surrogate: one CTA per 128-cell block of
+// one model; the cells the judge rejects are queued as (model, cell).
+__device__ __forceinline__ SgCoolArgs batch_cool_args(const BatchModel &M, const double *xi,
+                                                      const double *tr)
+{
+  const WindStageArgs &A = M.st[0];
+  SgCoolArgs c;
+  c.V = const_cast<double *>(A.s.Vn);
+  c.xi = xi;
+  c.tr = tr;
+  c.x1 = A.g.x1;
+  c.p = A.s.p;
+  c.w = A.w;
+  c.sc = A.s.sc;
+  return c;
+}
+
+__global__ void __launch_bounds__(128)
+    k_batch_sg_cool(const BatchModel *__restrict__ models, const BlockItem *__restrict__ blocks,
+                    const double *const *xi, const double *const *tr, SgNet net, SgBox bx,
+                    int use_net, int2 *queue, int *qcount, unsigned long long *stats)
+{
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const BlockItem bi = blocks[blockIdx.x];
+  const SgCoolArgs A = batch_cool_args(models[bi.m], xi[bi.m], tr[bi.m]);
+  sg_cool_block(net, bx, A, bi.m, bi.b, use_net, smem, queue, qcount, stats);
+}
+
+__global__ void k_batch_sg_fallback(const BatchModel *__restrict__ models, const double *const *xi,
+                                    const double *const *tr, const int2 *__restrict__ queue,
+                                    const int *__restrict__ qcount)
+{
+  const int cnt = *qcount;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+    const int2 e = queue[k];
+    const SgCoolArgs A = batch_cool_args(models[e.x], xi[e.x], tr[e.x]);
+    blondin_cell(A.V, A.xi, A.tr, A.p, A.w, A.x1, A.sc, A.sc->dt, A.sc->t, e.y);
+  }
+}
+
 __global__ void k_batch_finish(const BatchModel *__restrict__ models)
 {
   finish_block(models[blockIdx.x].fin);
@@ -163,6 +204,13 @@ struct ps_batch {
   ps::BlockItem *d_cells = nullptr, *d_x2 = nullptr;
   int ncells_blocks = 0, nx2_blocks = 0;
   const double **d_xi = nullptr, **d_tr = nullptr;
+  ps::BlockItem *d_cells128 = nullptr;  // 128-cell blocks (surrogate kernel)
+  int ncells128 = 0;
+  long total_cells = 0;
+  ps_surrogate *sg = nullptr;
+  int sg_use_net = 1;
+  int2 *sg_queue = nullptr;
+  int *sg_qcount = nullptr;
   int lim = 0, solver = 0, cooling = 0;
   cudaStream_t stream = nullptr;      // stream the work is issued on
   cudaStream_t own_stream = nullptr;  // stream created by the batch
@@ -221,7 +269,8 @@ static int encode_box(const ps::Params &p, double *base, int tx, int ty, CUtenso
 static int batch_upload(ps_batch *b)
 {
   std::vector<ps::TileItem> items[ps::kNumShapes];
-  std::vector<ps::BlockItem> cells, x2;
+  std::vector<ps::BlockItem> cells, x2, cells128;
+  b->total_cells = 0;
   for (int m = 0; m < b->n; m++) {
     ps_ctx *c = b->ctx[m];
     ps::BatchModel &M = b->h_models[m];
@@ -257,6 +306,9 @@ static int batch_upload(ps_batch *b)
       for (int bx = 0; bx < ntx; bx++) items[sh].push_back({m, bx, by, 0});
     const int nc = (p.nx[0] * p.nx[1] + 255) / 256, n2 = (p.ntot[0] * 4 + 255) / 256;
     for (int k = 0; k < nc; k++) cells.push_back({m, k});
+    const int nc128 = (p.nx[0] * p.nx[1] + 127) / 128;
+    for (int k = 0; k < nc128; k++) cells128.push_back({m, k});
+    b->total_cells += (long)p.nx[0] * p.nx[1];
     for (int k = 0; k < n2; k++) x2.push_back({m, k});
   }
   BCK(cudaMemcpy(b->d_models, b->h_models.data(), sizeof(ps::BatchModel) * b->n,
@@ -277,6 +329,11 @@ static int batch_upload(ps_batch *b)
   BCK(cudaMemcpy(b->d_cells, cells.data(), cells.size() * sizeof(ps::BlockItem),
                  cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(b->d_x2, x2.data(), x2.size() * sizeof(ps::BlockItem), cudaMemcpyHostToDevice));
+  cudaFree(b->d_cells128);
+  BCK(cudaMalloc(&b->d_cells128, cells128.size() * sizeof(ps::BlockItem)));
+  BCK(cudaMemcpy(b->d_cells128, cells128.data(), cells128.size() * sizeof(ps::BlockItem),
+                 cudaMemcpyHostToDevice));
+  b->ncells128 = (int)cells128.size();
   b->ncells_blocks = (int)cells.size();
   b->nx2_blocks = (int)x2.size();
   for (int k = 0; k < 3; k++) {
@@ -306,9 +363,23 @@ static int batch_bnd(ps_batch *b, int stage)
   return 0;
 }
 
+ps::SgNet ps_sg_net(const ps_surrogate *s);
+ps::SgBox ps_sg_boxv(const ps_surrogate *s);
+unsigned long long *ps_sg_stats_dev(ps_surrogate *s);
+
 static int batch_cool(ps_batch *b)
 {
   if (!b->cooling) return 0;
+  if (b->sg) {
+    BCK(cudaMemsetAsync(b->sg_qcount, 0, sizeof(int), b->stream));
+    ps::k_batch_sg_cool<<<b->ncells128, 128, ps::kInfBytes, b->stream>>>(
+        b->d_models, b->d_cells128, b->d_xi, b->d_tr, ps_sg_net(b->sg), ps_sg_boxv(b->sg),
+        b->sg_use_net, b->sg_queue, b->sg_qcount, ps_sg_stats_dev(b->sg));
+    ps::k_batch_sg_fallback<<<1216, 128, 0, b->stream>>>(b->d_models, b->d_xi, b->d_tr, b->sg_queue,
+                                                         b->sg_qcount);
+    b->launches += 2;
+    return 0;
+  }
   ps::k_batch_blondin<<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, b->d_xi,
                                                                b->d_tr);
   b->launches++;
@@ -342,6 +413,9 @@ static void batch_free(ps_batch *b)
   cudaFree(b->d_x2);
   cudaFree(b->d_xi);
   cudaFree(b->d_tr);
+  cudaFree(b->d_cells128);
+  cudaFree(b->sg_queue);
+  cudaFree(b->sg_qcount);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
 }
@@ -520,7 +594,7 @@ extern "C" int ps_batch_run(ps_batch *b, int nsteps)
   if (!b || nsteps < 0) return PS_EINVAL;
   int nshape = 0;
   for (int s = 0; s < ps::kNumShapes; s++) nshape += b->nitems[s] > 0;
-  const long per_step = 4 + 2 * nshape + (b->cooling ? 1 : 0) + 1;
+  const long per_step = 4 + 2 * nshape + (b->cooling ? (b->sg ? 2 : 1) : 0) + 1;
   for (int k = 0; k < 3; k++)
     if (!b->g[k]) {
       int r = batch_graph(b, k, &b->g[k]);
@@ -569,6 +643,23 @@ extern "C" int ps_batch_set_stream(ps_batch *b, void *stream)
 }
 
 extern "C" long ps_batch_launch_count(const ps_batch *b) { return b ? b->launches : -1; }
+
+extern "C" int ps_batch_set_surrogate(ps_batch *b, ps_surrogate *s, int use_net)
+{
+  if (!b) return batch_fail("ps_batch_set_surrogate: null batch");
+  BCK(cudaStreamSynchronize(b->stream));
+  if (s && !b->sg_queue) {
+    BCK(cudaMalloc(&b->sg_queue, sizeof(int2) * (size_t)b->total_cells));
+    BCK(cudaMalloc(&b->sg_qcount, sizeof(int)));
+  }
+  b->sg = s;
+  b->sg_use_net = use_net;
+  for (int k = 0; k < 3; k++) {
+    if (b->g[k]) cudaGraphExecDestroy(b->g[k]);
+    b->g[k] = nullptr;
+  }
+  return 0;
+}
 
 // One step issued launch by launch with CUDA events between the phases:
 // ms[0] = the stage-1 launches, ms[1] = the stage-2 launches, ms[2] = the

@@ -1,0 +1,204 @@
+// ps_blondin.cuh -- BLONDIN heating/cooling on the device
+// (Src/Cooling/BLONDIN/cooling.c:50-319, prefactors 1): the per-cell
+// implicit trapezoidal energy equation in T solved by bracket expansion and
+// Brent's method, shared by the wind kernels, the batched kernels and the
+// surrogate (which uses it as its fallback and to label training pairs).
+// Also the analytic T-derivative of the net rate, used by the Newton steps
+// that polish and judge the surrogate's prediction.
+#pragma once
+
+#include "ps_hydro.cuh"
+
+namespace ps {
+
+// CONST_* of Src/pluto.h:299-321 (cgs)
+constexpr double kAmu = 1.66053886e-24, kC = 2.99792458e10, kG = 6.6726e-8, kKB = 1.3806505e-16,
+                 kMP = 1.67262171e-24, kPI = 3.14159265358979, kSigmaT = 6.6524e-25;
+constexpr int kMaxCoolIter = 10000;  // the bracket search of the reference ends far earlier
+
+struct BlCtx {
+  double xi, sqxi, sqsqxi, nH, n, tx, E, hc_init, dt_share;
+};
+
+// ne_rat (cooling.c:210-222)
+__device__ __forceinline__ double bl_ne_rat(double T)
+{
+  if (T < 1.5e4) return 1e-2 + pow(10.0, (-51.59417133 + 12.27740153 * log10(T)));
+  if (T >= 1.5e4 && T < 3.3e4) return pow(10.0, (-3.80749689 + 0.86092628 * log10(T)));
+  return 1.21;
+}
+
+// heatcool (cooling.c:173-202), all prefactors 1
+__device__ __forceinline__ double bl_heatcool(const BlCtx &b, double T)
+{
+  const double sqT = sqrt(T);
+  const double ne = b.nH * bl_ne_rat(T);
+  const double comp_heat = 1.0 * (8.9e-36 * b.xi * b.tx);
+  const double comp_cool = 1.0 * (8.9e-36 * b.xi * (4.0 * T));
+  const double xray_heat = 1.0 * (1.5e-21 * (b.sqsqxi / sqT));
+  const double line_cool =
+      1.0 * ((1e-16 * exp(-1.3e5 / T) / b.sqxi / T) + fmin(fmin(1e-24, 5e-27 * sqT), 1.5e-17 / T));
+  const double brem_cool = 1.0 * (3.3e-27 * sqT);
+  return b.nH *
+         (ne * comp_heat + b.nH * xray_heat - ne * comp_cool - ne * line_cool - ne * brem_cool);
+}
+
+// heatcool and d(heatcool)/dT, differentiated term by term:
+//   ne = nH r(T), r = 1e-2 + 10^(a + b log10 T) -> r' = b 10^(a + b log10 T) / T (same for the
+//   middle branch without the 1e-2), 0 above 3.3e4 K;
+//   comp_cool' = 8.9e-36 xi 4; xray' = -xray / (2T);
+//   line term 1e-16 e^(-1.3e5/T) / (sqrt(xi) T): ' = term (1.3e5/T^2 - 1/T);
+//   the min() term: 0, 2.5e-27/sqrt(T) or -1.5e-17/T^2 by the active branch;
+//   brem' = brem / (2T).
+__device__ __forceinline__ double bl_heatcool_d(const BlCtx &b, double T, double &dhc)
+{
+  const double sqT = sqrt(T);
+  double r, dr;
+  if (T < 1.5e4) {
+    const double q = pow(10.0, (-51.59417133 + 12.27740153 * log10(T)));
+    r = 1e-2 + q;
+    dr = 12.27740153 * q / T;
+  } else if (T < 3.3e4) {
+    const double q = pow(10.0, (-3.80749689 + 0.86092628 * log10(T)));
+    r = q;
+    dr = 0.86092628 * q / T;
+  } else {
+    r = 1.21;
+    dr = 0.0;
+  }
+  const double ne = b.nH * r, dne = b.nH * dr;
+  const double comp_heat = 8.9e-36 * b.xi * b.tx;
+  const double comp_cool = 8.9e-36 * b.xi * (4.0 * T), dcomp_cool = 8.9e-36 * b.xi * 4.0;
+  const double xray_heat = 1.5e-21 * (b.sqsqxi / sqT), dxray_heat = -0.5 * xray_heat / T;
+  const double l1 = 1e-16 * exp(-1.3e5 / T) / b.sqxi / T;
+  const double dl1 = l1 * (1.3e5 / (T * T) - 1.0 / T);
+  const double m1 = 5e-27 * sqT, m2 = 1.5e-17 / T;
+  double l2, dl2;
+  if (1e-24 <= m1 && 1e-24 <= m2) {
+    l2 = 1e-24;
+    dl2 = 0.0;
+  } else if (m1 <= m2) {
+    l2 = m1;
+    dl2 = 0.5 * m1 / T;
+  } else {
+    l2 = m2;
+    dl2 = -m2 / T;
+  }
+  const double line_cool = l1 + l2, dline_cool = dl1 + dl2;
+  const double brem_cool = 3.3e-27 * sqT, dbrem_cool = 0.5 * brem_cool / T;
+  const double net = comp_heat - comp_cool - line_cool - brem_cool;
+  const double dnet = -dcomp_cool - dline_cool - dbrem_cool;
+  dhc = b.nH * (dne * net + ne * dnet + b.nH * dxray_heat);
+  return b.nH * (ne * net + b.nH * xray_heat);
+}
+
+// zfunc (cooling.c:233-237)
+__device__ __forceinline__ double bl_zfunc(const BlCtx &b, double temp)
+{
+  return (temp * b.n * kKB / (2.0 / 3.0)) - b.E - b.dt_share * (b.hc_init + bl_heatcool(b, temp)) / 2.0;
+}
+
+__device__ __forceinline__ double bl_func(const BlCtx &b, int which, double x)
+{
+  return which == 0 ? bl_zfunc(b, x) : bl_heatcool(b, x);
+}
+
+// zbrent (cooling.c:250-319): ITMAX 100, EPS 3e-8
+static __device__ __noinline__ double bl_zbrent(const BlCtx &bc, int which, double x1, double x2,
+                                                double tol)
+{
+  const double EPS = 3.0e-8;
+  double a = x1, b = x2, c = x2, d = 0.0, e = 0.0;
+  double fa = bl_func(bc, which, a), fb = bl_func(bc, which, b), fc = fb;
+  if (fb * fa > 0.0) return b;
+  for (int iter = 1; iter <= 100; iter++) {
+    if (fb * fc > 0.0) {
+      c = a;
+      fc = fa;
+      e = d = b - a;
+    }
+    if (fabs(fc) < fabs(fb)) {
+      a = b;
+      b = c;
+      c = a;
+      fa = fb;
+      fb = fc;
+      fc = fa;
+    }
+    const double tol1 = 2.0 * EPS * fabs(b) + 0.5 * tol;
+    const double xm = 0.5 * (c - b);
+    if (fabs(xm) <= tol1 || fb == 0.0) return b;
+    if (fabs(e) >= tol1 && fabs(fa) > fabs(fb)) {
+      double p, q, r;
+      const double s = fb / fa;
+      if (a == c) {
+        p = 2.0 * xm * s;
+        q = 1.0 - s;
+      } else {
+        q = fa / fc;
+        r = fb / fc;
+        p = s * (2.0 * xm * q * (q - r) - (b - a) * (r - 1.0));
+        q = (q - 1.0) * (r - 1.0) * (s - 1.0);
+      }
+      if (p > 0.0) q = -q;
+      p = fabs(p);
+      const double min1 = 3.0 * xm * q - fabs(tol1 * q);
+      const double min2 = fabs(e * q);
+      if (2.0 * p < (min1 < min2 ? min1 : min2)) {
+        e = d;
+        d = p / q;
+      } else {
+        d = xm;
+        e = d;
+      }
+    } else {
+      d = xm;
+      e = d;
+    }
+    a = b;
+    fa = fb;
+    if (fabs(d) > tol1)
+      b += d;
+    else
+      b += (xm > 0.0 ? fabs(tol1) : -fabs(tol1));
+    fb = bl_func(bc, which, b);
+  }
+  return b;
+}
+
+// The per-cell set-up after E, nH, n, xi, tx and dt_share are known
+// (cooling.c:108-113): the xi roots and the initial net rate.
+__device__ __forceinline__ void bl_prepare(BlCtx &b, double T)
+{
+  b.sqxi = sqrt(b.xi);
+  b.sqsqxi = pow(b.xi, 0.25);
+  b.hc_init = bl_heatcool(b, T);
+}
+
+// Bracket expansion and Brent (cooling.c:115-157) from the prepared
+// context at temperature T; returns T_f before the 1e4 K floor.  `overflow`
+// is set when the bracket search hit kMaxCoolIter.
+__device__ __forceinline__ double bl_solve(const BlCtx &b, double T, bool &overflow)
+{
+  double t_l = T * 0.9, t_u = T * 1.1;
+  double test = bl_zfunc(b, t_l) * bl_zfunc(b, t_u);
+  int it = 0;
+  while (test > 0 && test == test && it < kMaxCoolIter) {
+    t_l *= 0.9;
+    t_u *= 1.1;
+    test = bl_zfunc(b, t_l) * bl_zfunc(b, t_u);
+    it++;
+  }
+  overflow = it >= kMaxCoolIter;
+  double T_f;
+  if (test != test) {
+    T_f = T;
+  } else {
+    T_f = bl_zbrent(b, 0, t_l, t_u, 1.0);
+    const double hc_final = bl_heatcool(b, T_f);
+    if (hc_final * b.hc_init < 0.0) T_f = bl_zbrent(b, 1, fmin(T_f, T), fmax(T_f, T), 1.0);
+  }
+  return T_f;
+}
+
+}  // namespace ps

@@ -1,0 +1,258 @@
+// ps_surrogate.cuh -- the learned cooling step: a 4 -> 64 -> 64 -> 1 SiLU
+// MLP mapping (log n_H, log T, log xi, log dt) to log T_new of one BLONDIN
+// solve, run on the tensor cores (BF16 operands, FP32 accumulation in tensor
+// memory), followed by FP64 Newton steps on BLONDIN's implicit energy
+// equation that both polish the prediction and judge it (sg_judge).  A
+// cell whose inputs leave the training box, or whose residual does not
+// reach 1e-3 of its thermal energy, is solved by the reference method
+// (bracket + Brent) instead.
+//
+// Network (all per row b of a 128-row tile, one thread per row):
+//   x   = features, 4 values in [-1, 1] (bf16), padded with zeros to K = 16
+//   z1  = W1 x + b1          (tensor cores, FP32)   h1 = silu(z1)   -> bf16
+//   z2  = W2 h1 + b2         (tensor cores, FP32)   h2 = silu(z2)   (FP32)
+//   y   = w3 . h2 + b3       (CUDA cores, FP32; w3 rounded to bf16)
+//   log10 T_new = log10 T + 4 y
+// Parameter vector (FP32 master copy, kSgParams values):
+//   W1[64][4], b1[64], W2[64][64], b2[64], w3[64], b3.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "ps_blondin.cuh"
+#include "ps_tc.cuh"
+
+namespace ps {
+
+constexpr int kSgH = 64, kSgIn = 4, kSgK1 = 16, kSgRows = 128;
+constexpr int kSgW1 = 0, kSgB1 = 256, kSgW2 = 320, kSgB2 = 4416, kSgW3 = 4480, kSgB3 = 4544;
+constexpr int kSgParams = 4545;
+constexpr int kSgSmall = 3 * kSgH + 1;  // b1, b2, w3 (bf16-rounded), b3 as FP32
+
+// Training box and scales: u = (log10 v - lo) * scale - 1.
+struct SgBox {
+  double lo[4], hi[4], scale[4];
+  double t_x, mu;
+};
+
+// Device copies of the network the kernels read.
+struct SgNet {
+  const __nv_bfloat16 *w1b;   // [64][16] W1 in bf16, inputs 4..15 zero
+  const __nv_bfloat16 *w2b;   // [64][64] W2 (row j = output unit)
+  const __nv_bfloat16 *w2tb;  // [64][64] W2 transposed
+  const float *small;         // b1[64], b2[64], w3r[64], b3
+};
+
+// Acceptance rule of the Newton judge: |z| / thermal energy, and the
+// most net-rate evaluations per cell (the one at the old T included).
+constexpr double kSgResidual = 1e-3;
+constexpr int kSgMaxNewton = 5;
+// A stiff cell starts from the prediction when that moves T by more than
+// this fraction; below it the first Newton step from T is as good a start.
+constexpr double kSgJump = 0.1;
+
+enum { SG_ACCEPT = 0, SG_OUT_OF_BOX = 1, SG_REJECT = 2, SG_BELOW_MIN = 3 };
+
+// ------------------------------------------------------------------
+// shared-memory layout of the forward pass
+// ------------------------------------------------------------------
+
+constexpr int kSgOffX = 0;                                   // 128 x 16 bf16
+constexpr int kSgOffW1 = kSgOffX + kSgRows * kSgK1 * 2;      // 64 x 16 bf16
+constexpr int kSgOffH1 = kSgOffW1 + kSgH * kSgK1 * 2;        // 128 x 64 bf16
+constexpr int kSgOffW2 = kSgOffH1 + kSgRows * kSgH * 2;      // 64 x 64 bf16
+constexpr int kSgOffSmall = kSgOffW2 + kSgH * kSgH * 2;      // 193 floats
+constexpr int kSgOffBar = kSgOffSmall + 1024;                // mbarrier
+constexpr int kSgOffSlot = kSgOffBar + 8;                    // tensor-memory address
+constexpr int kSgFwdBytes = kSgOffSlot + 8;
+
+__device__ __forceinline__ float sg_silu(float z) { return z / (1.0f + __expf(-z)); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// Copies the network into shared memory (all threads of the CTA).
+__device__ __forceinline__ void sg_load_net(const SgNet &net, unsigned char *smem)
+{
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // W1: 64 rows x 2 chunks of 8 bf16
+  for (int c = tid; c < kSgH * 2; c += nt) {
+    const int j = c >> 1, kb = c & 1;
+    *reinterpret_cast<uint4 *>(smem + kSgOffW1 + kmaj_off(j, kb * 8, kSgK1)) =
+        *reinterpret_cast<const uint4 *>(net.w1b + j * kSgK1 + kb * 8);
+  }
+  // W2: 64 rows x 8 chunks
+  for (int c = tid; c < kSgH * 8; c += nt) {
+    const int j = c >> 3, kb = c & 7;
+    *reinterpret_cast<uint4 *>(smem + kSgOffW2 + kmaj_off(j, kb * 8, kSgH)) =
+        *reinterpret_cast<const uint4 *>(net.w2b + j * kSgH + kb * 8);
+  }
+  float *sm = reinterpret_cast<float *>(smem + kSgOffSmall);
+  for (int c = tid; c < kSgSmall; c += nt) sm[c] = net.small[c];
+}
+
+// Writes one row of bf16 values (16 at a time) into a K-major operand.
+__device__ __forceinline__ void sg_store_row16(unsigned char *base, int r, int k0, int K,
+                                               const float (&v)[16])
+{
+  uint4 a, b;
+  a.x = pack_bf16(v[0], v[1]);
+  a.y = pack_bf16(v[2], v[3]);
+  a.z = pack_bf16(v[4], v[5]);
+  a.w = pack_bf16(v[6], v[7]);
+  b.x = pack_bf16(v[8], v[9]);
+  b.y = pack_bf16(v[10], v[11]);
+  b.z = pack_bf16(v[12], v[13]);
+  b.w = pack_bf16(v[14], v[15]);
+  *reinterpret_cast<uint4 *>(base + kmaj_off(r, k0, K)) = a;
+  *reinterpret_cast<uint4 *>(base + kmaj_off(r, k0 + 8, K)) = b;
+}
+
+// Bounded wait for the MMA group committed to `bar`; CTA-uniform result.
+__device__ __forceinline__ bool sg_wait(uint64_t *bar, uint32_t &phase)
+{
+  const bool ok = mbar_wait_bounded(bar, phase, 1u << 22);
+  phase ^= 1u;
+  tc_fence_after();
+  return __syncthreads_and(ok) != 0;
+}
+
+// Forward pass of a 128-row tile; thread tid owns row tid (tensor-memory
+// lane tid).  Tensor memory: z1 in columns [c1, c1 + 64), z2 in
+// [c2, c2 + 64) (c1 == c2 is allowed: z1 is consumed before the second
+// MMA is issued).  The network and the tensor-memory address must already
+// be in shared memory.  Returns false (CTA-uniform) if an MMA did not
+// complete in time.
+__device__ __forceinline__ bool sg_forward(unsigned char *smem, uint32_t tmem, uint32_t &phase,
+                                           const float (&x)[4], int c1, int c2, float &y)
+{
+  const int r = threadIdx.x, warp = r >> 5;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kSgOffBar);
+  const float *sm = reinterpret_cast<const float *>(smem + kSgOffSmall);
+  const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+  {
+    uint4 a, z = make_uint4(0u, 0u, 0u, 0u);
+    a.x = pack_bf16(x[0], x[1]);
+    a.y = pack_bf16(x[2], x[3]);
+    a.z = 0u;
+    a.w = 0u;
+    *reinterpret_cast<uint4 *>(smem + kSgOffX + kmaj_off(r, 0, kSgK1)) = a;
+    *reinterpret_cast<uint4 *>(smem + kSgOffX + kmaj_off(r, 8, kSgK1)) = z;
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  if (r == 0) {
+    tc_fence_after();
+    umma_bf16(tmem + c1, umma_slice_desc(smem + kSgOffX, kSgK1, 0),
+              umma_slice_desc(smem + kSgOffW1, kSgK1, 0), umma_idesc_bf16(128, kSgH), false);
+    umma_commit(bar);
+  }
+  if (!sg_wait(bar, phase)) return false;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float v[16];
+    tmem_ld16(lane_addr + c1 + 16 * c, v);
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = sg_silu(v[i] + sm[16 * c + i]);
+    sg_store_row16(smem + kSgOffH1, r, 16 * c, kSgH, v);
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  if (r == 0) {
+    tc_fence_after();
+#pragma unroll
+    for (int s = 0; s < 4; s++)
+      umma_bf16(tmem + c2, umma_slice_desc(smem + kSgOffH1, kSgH, s),
+                umma_slice_desc(smem + kSgOffW2, kSgH, s), umma_idesc_bf16(128, kSgH), s > 0);
+    umma_commit(bar);
+  }
+  if (!sg_wait(bar, phase)) return false;
+  float acc = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float v[16];
+    tmem_ld16(lane_addr + c2 + 16 * c, v);
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const float h = sg_silu(v[i] + sm[kSgH + 16 * c + i]);
+      acc += sm[2 * kSgH + 16 * c + i] * h;
+    }
+  }
+  y = acc + sm[3 * kSgH];
+  return true;
+}
+
+// Features of a tuple; false when it lies outside the training box.
+__device__ __forceinline__ bool sg_features(const SgBox &bx, double nH, double T, double xi,
+                                            double dt, float (&x)[4])
+{
+  const double l[4] = {log10(nH), log10(T), log10(xi), log10(dt)};
+  bool in = true;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    in = in && (l[i] >= bx.lo[i]) && (l[i] <= bx.hi[i]);
+    x[i] = (float)((l[i] - bx.lo[i]) * bx.scale[i] - 1.0);
+  }
+  return in;
+}
+
+// z(T) of BLONDIN's energy equation and dz/dT.
+__device__ __forceinline__ double sg_z(const BlCtx &b, double T, double &dz, double &hc)
+{
+  double dhc;
+  hc = bl_heatcool_d(b, T, dhc);
+  dz = b.n * kKB / (2.0 / 3.0) - b.dt_share * dhc / 2.0;
+  return (T * b.n * kKB / (2.0 / 3.0)) - b.E - b.dt_share * (b.hc_init + hc) / 2.0;
+}
+
+// The judge.  With E, n, xi, tx and dt_share set: the net rate and its
+// derivative at the old temperature T give z(T) = -dt hc(T) for free.  If
+// |z(T)| is already within kSgResidual of the thermal energy, one Newton
+// step from T is the answer (non-stiff cell: one rate evaluation in all).
+// Otherwise (stiff cell) damped Newton iterations (each step kept within a
+// factor 2) run until the residual is within kSgResidual, at most
+// kSgMaxNewton evaluations, starting from the network's prediction T0 when
+// it moves T by more than kSgJump (from T when from_net is false or the
+// predicted change is small); a final Newton step polishes the converged
+// point.  Rejected:
+// no convergence, z' <= 0, the net rate at the root of opposite sign to
+// the initial one (the reference then solves for the equilibrium
+// temperature instead), or a root on the wrong side of T.  Sets hc_init.
+__device__ __forceinline__ int sg_judge(BlCtx &b, double T, double T0, bool from_net, double &T_f,
+                                        int &evals, bool &stiff)
+{
+  const double cth = b.n * kKB / (2.0 / 3.0);
+  double dhc;
+  b.hc_init = bl_heatcool_d(b, T, dhc);
+  evals = 1;
+  double Tk = T, hc = b.hc_init;
+  double z = T * cth - b.E - b.dt_share * b.hc_init;
+  double dz = cth - b.dt_share * dhc / 2.0;
+  bool conv = fabs(z) <= kSgResidual * T * cth;
+  stiff = !conv;
+  if (!conv && from_net && T0 > 0.0 && isfinite(T0) && fabs(T0 - T) > kSgJump * T) {
+    Tk = T0;
+    z = sg_z(b, Tk, dz, hc);
+    evals++;
+    conv = fabs(z) <= kSgResidual * Tk * cth;
+  }
+  for (int it = 0; !conv; it++) {
+    if (evals >= kSgMaxNewton || !(dz > 0.0)) return SG_REJECT;
+    Tk = fmin(fmax(Tk - z / dz, 0.5 * Tk), 2.0 * Tk);
+    z = sg_z(b, Tk, dz, hc);
+    evals++;
+    conv = fabs(z) <= kSgResidual * Tk * cth;
+  }
+  if (!(dz > 0.0) || hc * b.hc_init < 0.0) return SG_REJECT;
+  const double Tn = Tk - z / dz;
+  if (!(Tn > 0.0) || !isfinite(Tn) || (Tn - T) * b.hc_init < 0.0) return SG_REJECT;
+  T_f = Tn;
+  return SG_ACCEPT;
+}
+
+}  // namespace ps

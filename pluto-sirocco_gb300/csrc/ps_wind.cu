@@ -453,11 +453,14 @@ int ps_wind_hydro_launches(ps_ctx *c)
 }
 
 // SplitSource with BLONDIN (Src/split_source.c:52-53) for the device dt/time.
+int ps_sg_cool_launch(ps_ctx *c);
+
 int ps_wind_cool_launch(ps_ctx *c)
 {
   WindDev *w = c->wind;
   const ps::Params &p = c->p;
   if (!p.cooling) return 0;
+  if (c->sg) return ps_sg_cool_launch(c);
   const int nb = (p.nx[0] * p.nx[1] + 127) / 128;
   ps::k_blondin<<<nb, 128, 0, c->stream>>>(c->V, w->xi, w->tr, p, w->a.w, w->a.g.x1, c->sc);
   c->launches++;

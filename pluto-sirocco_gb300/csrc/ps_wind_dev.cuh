@@ -14,6 +14,7 @@
 //   BlondinCooling            Src/Cooling/BLONDIN/cooling.c:50-319
 #pragma once
 
+#include "ps_blondin.cuh"
 #include "ps_ctx.cuh"
 #include "ps_physics.cuh"
 #include "ps_stage.cuh"
@@ -22,9 +23,6 @@
 
 namespace ps {
 
-constexpr double kAmu = 1.66053886e-24, kC = 2.99792458e10, kG = 6.6726e-8, kKB = 1.3806505e-16,
-                 kMP = 1.67262171e-24, kPI = 3.14159265358979, kSigmaT = 6.6524e-25;
-constexpr int kMaxCoolIter = 10000;  // the bracket search of the reference ends far earlier
 
 struct WindDev {
   WindStageArgs a;       // geometry, line list, parameters (stage part filled per launch)
@@ -201,102 +199,43 @@ __device__ __forceinline__ void init_xi_cell(const double *V, double *xi, double
 
 // ---------------------------------------------------------------
 // BLONDIN heating/cooling, one thread per active cell
+// (Src/Cooling/BLONDIN/cooling.c:50-165)
 // ---------------------------------------------------------------
 
-struct BlCtx {
-  double xi, sqxi, sqsqxi, nH, n, tx, E, hc_init, dt_share;
-};
-
-__device__ __forceinline__ double bl_ne_rat(double T)
+// The cell's BLONDIN context from the state; false when the cell is below
+// the minimum cooling temperature and is left alone.
+__device__ __forceinline__ bool blondin_ctx(const double *V, const double *xi_s, const double *tr_s,
+                                            const Params &p, const WindParams &w,
+                                            const double *x1, double dt, double t, int q,
+                                            BlCtx &b, double &T, long long &c)
 {
-  if (T < 1.5e4) return 1e-2 + pow(10.0, (-51.59417133 + 12.27740153 * log10(T)));
-  if (T >= 1.5e4 && T < 3.3e4) return pow(10.0, (-3.80749689 + 0.86092628 * log10(T)));
-  return 1.21;
-}
-
-__device__ __forceinline__ double bl_heatcool(const BlCtx &b, double T)
-{
-  const double sqT = sqrt(T);
-  const double ne = b.nH * bl_ne_rat(T);
-  const double comp_heat = 1.0 * (8.9e-36 * b.xi * b.tx);
-  const double comp_cool = 1.0 * (8.9e-36 * b.xi * (4.0 * T));
-  const double xray_heat = 1.0 * (1.5e-21 * (b.sqsqxi / sqT));
-  const double line_cool =
-      1.0 * ((1e-16 * exp(-1.3e5 / T) / b.sqxi / T) + fmin(fmin(1e-24, 5e-27 * sqT), 1.5e-17 / T));
-  const double brem_cool = 1.0 * (3.3e-27 * sqT);
-  return b.nH *
-         (ne * comp_heat + b.nH * xray_heat - ne * comp_cool - ne * line_cool - ne * brem_cool);
-}
-
-__device__ __forceinline__ double bl_zfunc(const BlCtx &b, double temp)
-{
-  return (temp * b.n * kKB / (2.0 / 3.0)) - b.E - b.dt_share * (b.hc_init + bl_heatcool(b, temp)) / 2.0;
-}
-
-__device__ __forceinline__ double bl_func(const BlCtx &b, int which, double x)
-{
-  return which == 0 ? bl_zfunc(b, x) : bl_heatcool(b, x);
-}
-
-static __device__ __noinline__ double bl_zbrent(const BlCtx &bc, int which, double x1, double x2, double tol)
-{
-  const double EPS = 3.0e-8;
-  double a = x1, b = x2, c = x2, d = 0.0, e = 0.0;
-  double fa = bl_func(bc, which, a), fb = bl_func(bc, which, b), fc = fb;
-  if (fb * fa > 0.0) return b;
-  for (int iter = 1; iter <= 100; iter++) {
-    if (fb * fc > 0.0) {
-      c = a;
-      fc = fa;
-      e = d = b - a;
-    }
-    if (fabs(fc) < fabs(fb)) {
-      a = b;
-      b = c;
-      c = a;
-      fa = fb;
-      fb = fc;
-      fc = fa;
-    }
-    const double tol1 = 2.0 * EPS * fabs(b) + 0.5 * tol;
-    const double xm = 0.5 * (c - b);
-    if (fabs(xm) <= tol1 || fb == 0.0) return b;
-    if (fabs(e) >= tol1 && fabs(fa) > fabs(fb)) {
-      double p, q, r;
-      const double s = fb / fa;
-      if (a == c) {
-        p = 2.0 * xm * s;
-        q = 1.0 - s;
-      } else {
-        q = fa / fc;
-        r = fb / fc;
-        p = s * (2.0 * xm * q * (q - r) - (b - a) * (r - 1.0));
-        q = (q - 1.0) * (r - 1.0) * (s - 1.0);
-      }
-      if (p > 0.0) q = -q;
-      p = fabs(p);
-      const double min1 = 3.0 * xm * q - fabs(tol1 * q);
-      const double min2 = fabs(e * q);
-      if (2.0 * p < (min1 < min2 ? min1 : min2)) {
-        e = d;
-        d = p / q;
-      } else {
-        d = xm;
-        e = d;
-      }
-    } else {
-      d = xm;
-      e = d;
-    }
-    a = b;
-    fa = fb;
-    if (fabs(d) > tol1)
-      b += d;
-    else
-      b += (xm > 0.0 ? fabs(tol1) : -fabs(tol1));
-    fb = bl_func(bc, which, b);
+  const int gi = q % p.nx[0] + p.beg[0], gj = q / p.nx[0] + p.beg[1];
+  c = vcell(p, gj, gi);
+  b.dt_share = dt * w.unit_time;
+  const double r = x1[gi] * w.unit_length;
+  const double rho = V[RHO * p.vstride + c] * w.unit_density;
+  const double pr = V[PRS * p.vstride + c];
+  b.E = (pr * w.unit_pressure) / (p.gamma - 1);
+  b.nH = rho / (1.43 * kMP);
+  if (t <= 3.0) {
+    b.xi = w.lx / b.nH / r / r;
+    b.tx = w.t_x;
+  } else {
+    b.xi = xi_s[c];
+    b.tx = tr_s[c];
   }
-  return b;
+  b.n = rho / (w.mu * kMP);
+  T = b.E * (2.0 / 3.0) / (b.n * kKB);
+  return T >= 1.e4;
+}
+
+// The new pressure of a cell from its final temperature (cooling.c:158-162).
+__device__ __forceinline__ void blondin_store(double *V, const Params &p, const WindParams &w,
+                                              const BlCtx &b, long long c, double T_f)
+{
+  T_f = dmax(T_f, 1.e4);
+  const double E_f = T_f / (2.0 / 3.0) * (b.n * kKB);
+  V[PRS * p.vstride + c] = E_f * (p.gamma - 1) / w.unit_pressure;
 }
 
 __device__ __forceinline__ void blondin_cell(double *V, const double *xi_s, const double *tr_s,
@@ -304,51 +243,15 @@ __device__ __forceinline__ void blondin_cell(double *V, const double *xi_s, cons
                                              const double *x1, Scalars *sc, double dt, double t,
                                              int q)
 {
-  do {
-    const int gi = q % p.nx[0] + p.beg[0], gj = q / p.nx[0] + p.beg[1];
-    const long long c = vcell(p, gj, gi);
-    BlCtx b;
-    b.dt_share = dt * w.unit_time;
-    const double r = x1[gi] * w.unit_length;
-    const double rho = V[RHO * p.vstride + c] * w.unit_density;
-    const double pr = V[PRS * p.vstride + c];
-    b.E = (pr * w.unit_pressure) / (p.gamma - 1);
-    b.nH = rho / (1.43 * kMP);
-    if (t <= 3.0) {
-      b.xi = w.lx / b.nH / r / r;
-      b.tx = w.t_x;
-    } else {
-      b.xi = xi_s[c];
-      b.tx = tr_s[c];
-    }
-    b.n = rho / (w.mu * kMP);
-    const double T = b.E * (2.0 / 3.0) / (b.n * kKB);
-    if (T < 1.e4) continue;
-    b.sqxi = sqrt(b.xi);
-    b.sqsqxi = pow(b.xi, 0.25);
-    b.hc_init = bl_heatcool(b, T);
-    double t_l = T * 0.9, t_u = T * 1.1;
-    double test = bl_zfunc(b, t_l) * bl_zfunc(b, t_u);
-    int it = 0;
-    while (test > 0 && test == test && it < kMaxCoolIter) {
-      t_l *= 0.9;
-      t_u *= 1.1;
-      test = bl_zfunc(b, t_l) * bl_zfunc(b, t_u);
-      it++;
-    }
-    if (it >= kMaxCoolIter) atomicOr(&sc->flags, F_NAN);
-    double T_f;
-    if (test != test) {
-      T_f = T;
-    } else {
-      T_f = bl_zbrent(b, 0, t_l, t_u, 1.0);
-      const double hc_final = bl_heatcool(b, T_f);
-      if (hc_final * b.hc_init < 0.0) T_f = bl_zbrent(b, 1, fmin(T_f, T), fmax(T_f, T), 1.0);
-    }
-    T_f = dmax(T_f, 1.e4);
-    const double E_f = T_f / (2.0 / 3.0) * (b.n * kKB);
-    V[PRS * p.vstride + c] = E_f * (p.gamma - 1) / w.unit_pressure;
-  } while (0);
+  BlCtx b;
+  double T;
+  long long c;
+  if (!blondin_ctx(V, xi_s, tr_s, p, w, x1, dt, t, q, b, T, c)) return;
+  bl_prepare(b, T);
+  bool overflow;
+  const double T_f = bl_solve(b, T, overflow);
+  if (overflow) atomicOr(&sc->flags, F_NAN);
+  blondin_store(V, p, w, b, c, T_f);
 }
 
 // ---------------------------------------------------------------

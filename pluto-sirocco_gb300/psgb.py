@@ -29,7 +29,10 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_init_wind", "ps_wind_synthetic_flux", "ps_set_wind", "ps_split_source",
            "ps_batch_create", "ps_batch_destroy", "ps_batch_run", "ps_batch_sync",
            "ps_batch_set_stream", "ps_batch_launch_count", "ps_batch_set_shape",
-           "ps_batch_get_shape", "ps_batch_autotune", "ps_batch_time_step_kernels"]
+           "ps_batch_get_shape", "ps_batch_autotune", "ps_batch_time_step_kernels",
+           "ps_sg_create", "ps_sg_destroy", "ps_sg_set_params", "ps_sg_get_params",
+           "ps_sg_label", "ps_sg_set_data", "ps_sg_train", "ps_sg_grad", "ps_sg_predict",
+           "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect"]
 
 
 class Config(ctypes.Structure):
@@ -66,6 +69,11 @@ def make_wind(line_force=1, body_force=1, floors=1, nangles=36, **over):
 
 
 _lib = None
+
+
+class SgBox(ctypes.Structure):
+    _fields_ = [("lo", ctypes.c_double * 4), ("hi", ctypes.c_double * 4),
+                ("t_x", ctypes.c_double), ("mu", ctypes.c_double)]
 
 
 def lib():
@@ -120,6 +128,23 @@ def lib():
         L.ps_batch_get_shape.argtypes = [P, I, ctypes.POINTER(I), ctypes.POINTER(I)]
         L.ps_batch_autotune.argtypes = [P, I]
         L.ps_batch_time_step_kernels.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
+        FP = ctypes.POINTER(ctypes.c_float)
+        DP = ctypes.POINTER(ctypes.c_double)
+        IP = ctypes.POINTER(ctypes.c_int)
+        Lg = ctypes.c_long
+        L.ps_sg_create.argtypes = [ctypes.POINTER(SgBox), ctypes.POINTER(P)]
+        L.ps_sg_destroy.argtypes = [P]
+        L.ps_sg_set_params.argtypes = [P, FP]
+        L.ps_sg_get_params.argtypes = [P, FP]
+        L.ps_sg_label.argtypes = [P, DP, Lg, DP, DP]
+        L.ps_sg_set_data.argtypes = [P, DP, DP, Lg]
+        L.ps_sg_train.argtypes = [P, I, I, ctypes.c_float, ctypes.c_float, ctypes.c_ulonglong, FP]
+        L.ps_sg_grad.argtypes = [P, DP, DP, I, FP, FP]
+        L.ps_sg_predict.argtypes = [P, DP, Lg, I, DP, IP, DP]
+        L.ps_sg_stats.argtypes = [P, ctypes.POINTER(ctypes.c_longlong), I]
+        L.ps_set_surrogate.argtypes = [P, P, I]
+        L.ps_batch_set_surrogate.argtypes = [P, P, I]
+        L.ps_sg_collect.argtypes = [P, DP, Lg, ctypes.POINTER(Lg)]
         _lib = L
     return _lib
 
@@ -404,3 +429,174 @@ def wind_model_solver(spec, cooling=1, line_force=1):
     s.set_time(0.0, 1e-4, 0)
     s.set_wind(w, wind_flux(cfg, w, g) if line_force else None)
     return s
+
+
+# ----------------------------------------------------------------------
+# learned cooling step
+# ----------------------------------------------------------------------
+
+N_SG_PARAMS = 4545
+SG_ACCEPT, SG_OUT_OF_BOX, SG_REJECT, SG_BELOW_MIN = 0, 1, 2, 3
+# log-uniform draws of the training set: n_H [cm^-3], T [K], xi, dt [s]
+SG_DRAW_BOX = ((-2.0, 12.0), (4.0, 8.0), (-1.0, 5.0), (-5.0, 0.0))
+
+
+def _np_dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Surrogate:
+    """The learned BLONDIN step (ps_surrogate)."""
+
+    def __init__(self, lo, hi, t_x=5.6e7, mu=0.6):
+        b = SgBox()
+        b.lo[:] = [float(v) for v in lo]
+        b.hi[:] = [float(v) for v in hi]
+        b.t_x, b.mu = t_x, mu
+        self.box = b
+        self.h = ctypes.c_void_p()
+        check(lib().ps_sg_create(ctypes.byref(b), ctypes.byref(self.h)), "ps_sg_create")
+
+    def close(self):
+        if self.h:
+            lib().ps_sg_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        p = np.zeros(N_SG_PARAMS, dtype=np.float32)
+        check(lib().ps_sg_get_params(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+              "ps_sg_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib().ps_sg_set_params(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+              "ps_sg_set_params")
+
+    def label(self, tuples, t_cool=False):
+        t = np.ascontiguousarray(tuples, dtype=np.float64)
+        out = np.zeros(len(t))
+        tc = np.zeros(len(t)) if t_cool else None
+        check(lib().ps_sg_label(self.h, _np_dp(t), len(t), _np_dp(out),
+                                _np_dp(tc) if t_cool else None), "ps_sg_label")
+        return (out, tc) if t_cool else out
+
+    def set_data(self, tuples, t_new):
+        t = np.ascontiguousarray(tuples, dtype=np.float64)
+        y = np.ascontiguousarray(t_new, dtype=np.float64)
+        check(lib().ps_sg_set_data(self.h, _np_dp(t), _np_dp(y), len(t)), "ps_sg_set_data")
+
+    def train(self, steps, batch=8192, lr=3e-3, lr_end=3e-5, seed=3):
+        hist = np.zeros(steps, dtype=np.float32)
+        flags = check(lib().ps_sg_train(self.h, steps, batch, lr, lr_end, seed,
+                                        hist.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+                      "ps_sg_train")
+        return hist, flags
+
+    def grad(self, tuples, t_new):
+        t = np.ascontiguousarray(tuples, dtype=np.float64)
+        y = np.ascontiguousarray(t_new, dtype=np.float64)
+        g = np.zeros(N_SG_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        flags = check(lib().ps_sg_grad(self.h, _np_dp(t), _np_dp(y), len(t),
+                                       g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                       ctypes.byref(loss)), "ps_sg_grad")
+        return g, loss.value, flags
+
+    def predict(self, tuples, use_net=1):
+        t = np.ascontiguousarray(tuples, dtype=np.float64)
+        out = np.zeros(len(t))
+        st = np.zeros(len(t), dtype=np.int32)
+        t0 = np.zeros(len(t))
+        check(lib().ps_sg_predict(self.h, _np_dp(t), len(t), use_net, _np_dp(out),
+                                  st.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _np_dp(t0)),
+              "ps_sg_predict")
+        return out, st, t0
+
+    def stats(self, reset=True):
+        """accepted, out of box, rejected, below 1e4 K, judge evaluations, stiff cells"""
+        out = (ctypes.c_longlong * 6)()
+        check(lib().ps_sg_stats(self.h, out, int(reset)), "ps_sg_stats")
+        return list(out)
+
+
+def sg_draws(n, seed=3, box=SG_DRAW_BOX):
+    """Log-uniform (n_H, T, xi, dt) draws over `box` (numpy, seeded)."""
+    rng = np.random.default_rng(seed)
+    return np.stack([10.0 ** rng.uniform(lo, hi, n) for lo, hi in box], axis=1)
+
+
+def sg_collect(solver, cap=1 << 22):
+    """(n_H, T, xi, dt) of the cells the next split-source step would solve."""
+    out = np.zeros((cap, 4))
+    n = ctypes.c_long()
+    check(lib().ps_sg_collect(solver.ctx, _np_dp(out), cap, ctypes.byref(n)), "ps_sg_collect")
+    return out[:n.value].copy()
+
+
+def sg_box_of(tuples, pad=0.05):
+    """log10 bounding box of a tuple set, padded by `pad` decades."""
+    lt = np.log10(tuples)
+    return lt.min(axis=0) - pad, lt.max(axis=0) + pad
+
+
+def wind_training_tuples(specs, steps=(0, 40, 120, 240), per_model=4000, seed=3, cooling=1):
+    """Tuples from wind runs: each spec run on the GPU, sampled at the given
+    step numbers (`per_model` cells drawn at random from each snapshot)."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for sp in specs:
+        s = wind_model_solver(sp, cooling=cooling)
+        done = 0
+        for st in steps:
+            if st > done:
+                s.run(st - done)
+                done = st
+            t = sg_collect(s)
+            if len(t):
+                k = rng.choice(len(t), size=min(per_model, len(t)), replace=False)
+                rows.append(t[k])
+        s.close()
+    return np.concatenate(rows) if rows else np.zeros((0, 4))
+
+
+def sg_stiff_draws(sg, n, seed=3, box=SG_DRAW_BOX, ratio=(-1.0, 2.0)):
+    """Log-uniform (n_H, T, xi) draws whose dt is a log-uniform multiple
+    10^ratio of the cell's own cooling time (clipped to the dt range of
+    `box`): the stiff cells, where the prediction is what the Newton steps
+    start from."""
+    rng = np.random.default_rng(seed + 1000)
+    t = sg_draws(n, seed=seed, box=box)
+    _, tc = sg.label(t, t_cool=True)
+    dt = tc * 10.0 ** rng.uniform(ratio[0], ratio[1], n)
+    t[:, 3] = np.clip(dt, 10.0 ** box[3][0], 10.0 ** box[3][1])
+    return t
+
+
+def train_surrogate(wind_tuples, n_draws=500000, steps=20000, batch=8192, seed=3, t_x=5.6e7,
+                    mu=0.6, stiff_frac=0.5):
+    """The learned cooling step: log-uniform draws (a fraction `stiff_frac`
+    of them with dt drawn relative to the cooling time) plus wind tuples,
+    labelled by the reference method on the GPU and trained with Adam on the
+    GPU.  The box is the bounding box of the training tuples with
+    T >= 1e4 K.  Returns (surrogate, loss history, tuples, labels)."""
+    n_stiff = int(n_draws * stiff_frac)
+    probe = Surrogate(*zip(*SG_DRAW_BOX), t_x=t_x, mu=mu)
+    parts = [sg_draws(n_draws - n_stiff, seed=seed), sg_stiff_draws(probe, n_stiff, seed=seed)]
+    probe.close()
+    if len(wind_tuples):
+        parts.append(wind_tuples)
+    tup = np.concatenate(parts)
+    tup = tup[tup[:, 1] >= 1e4]
+    lo, hi = sg_box_of(tup)
+    sg = Surrogate(lo, hi, t_x=t_x, mu=mu)
+    lab = sg.label(tup)
+    sg.set_data(tup, lab)
+    hist, _ = sg.train(steps, batch=batch, seed=seed)
+    return sg, hist, tup, lab

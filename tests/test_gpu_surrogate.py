@@ -1,0 +1,208 @@
+"""The learned cooling step on the GPU.
+
+* the tensor-core forward pass and the training backward pass against the
+  numpy network (oracle/mlp_oracle.py), which follows the same bfloat16
+  rounding points;
+* the training labels (reference method on the GPU) against the oracle's
+  BLONDIN point solve;
+* training on the GPU lowers the loss, and the trained surrogate keeps every
+  cell within 1% of the reference method's temperature;
+* what the network gains over the same Newton judge started from the old
+  temperature (no network);
+* the surrogate inside the wind's split-source step and in the batched form.
+"""
+import numpy as np
+import pytest
+
+import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+BOX_LO = (-2.0, 4.0, -1.0, -5.0)
+BOX_HI = (12.0, 8.0, 5.0, 0.0)
+
+
+def _params(seed):
+    rng = np.random.default_rng(seed)
+    return np.concatenate([rng.uniform(-0.5, 0.5, 256), rng.uniform(-0.5, 0.5, 64),
+                           rng.uniform(-0.125, 0.125, 4096), rng.uniform(-0.125, 0.125, 64),
+                           rng.uniform(-0.125, 0.125, 64), [0.01]]).astype(np.float32)
+
+
+def _draws(n, seed):
+    import psgb
+    t = psgb.sg_draws(n, seed=seed)
+    t[:, 1] = np.clip(t[:, 1], 1.0001e4, None)
+    return t
+
+
+def test_forward_matches_oracle(built):
+    import psgb
+    sg = psgb.Surrogate(BOX_LO, BOX_HI)
+    p = _params(5)
+    sg.set_params(p)
+    tup = _draws(3000, 11)
+    _, st, t0 = sg.predict(tup)
+    assert np.all(st != psgb.SG_OUT_OF_BOX)
+    y_gpu = np.log10(t0 / tup[:, 1]) / 4.0
+    u = M.features(tup, BOX_LO, BOX_HI)
+    y_ref, _ = M.forward(p.astype(np.float64), u)
+    d = np.abs(y_gpu - y_ref)
+    print("forward |dy|: median %.2e  p99 %.2e  max %.2e" % (np.median(d), np.percentile(d, 99), d.max()))
+    assert np.percentile(d, 99) < 1e-4
+    assert d.max() < 1e-2
+
+
+def test_backward_matches_oracle(built):
+    import psgb
+    from oracle import blondin_points
+    sg = psgb.Surrogate(BOX_LO, BOX_HI)
+    p = _params(6)
+    sg.set_params(p)
+    tup = _draws(1000, 12)
+    lab = blondin_points(tup)
+    g, loss, flags = sg.grad(tup, lab)
+    assert flags == 0
+    u = M.features(tup, BOX_LO, BOX_HI)
+    t = M.targets(tup, lab)
+    loss_ref, g_ref = M.loss_grad(p.astype(np.float64), u, t)
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    for name, a, b in (("W1", 0, 256), ("b1", 256, 320), ("W2", 320, 4416), ("b2", 4416, 4480),
+                       ("w3", 4480, 4544), ("b3", 4544, 4545)):
+        err = np.linalg.norm(g[a:b] - g_ref[a:b]) / np.linalg.norm(g_ref[a:b])
+        print(name, "relative gradient error %.2e" % err)
+        assert err < 1e-2, name
+
+
+def test_labels_match_oracle(built):
+    import psgb
+    from oracle import blondin_points
+    sg = psgb.Surrogate(BOX_LO, BOX_HI)
+    tup = _draws(4000, 13)
+    lab = sg.label(tup)
+    ref = blondin_points(tup)
+    rel = np.abs(lab - ref) / ref
+    print("label rel diff: max %.2e" % rel.max())
+    assert rel.max() < 1e-4
+
+
+@pytest.fixture(scope="module")
+def trained(built):
+    import psgb
+    specs = [dict(grid=(128, 64), l_star=1e37, krad=0.2, alpharad=-0.6),
+             dict(grid=(128, 64), l_star=1e38, krad=0.3, alpharad=-0.55)]
+    wt = psgb.wind_training_tuples(specs, steps=(0, 40, 120), per_model=8000)
+    sg, hist, tup, lab = psgb.train_surrogate(wt, n_draws=200000, steps=40000)
+    return sg, hist, specs
+
+
+def _held_out(sg, n, seed):
+    import psgb
+    a = _draws(n // 2, seed)
+    b = psgb.sg_stiff_draws(sg, n - n // 2, seed=seed)
+    b[:, 1] = np.clip(b[:, 1], 1.0001e4, None)
+    return np.concatenate([a, b])
+
+
+def test_training_and_temperature_error(trained):
+    import psgb
+    sg, hist, _ = trained
+    print("loss: first %.3e  last %.3e" % (hist[:20].mean(), hist[-20:].mean()))
+    assert hist[-20:].mean() < 0.2 * hist[:20].mean()
+    tup = _held_out(sg, 50000, 99)
+    inb = np.all((np.log10(tup) >= np.array(sg.box.lo[:])) & (np.log10(tup) <= np.array(sg.box.hi[:])), axis=1)
+    tup = tup[inb]
+    lab = sg.label(tup)
+    out, st, t0 = sg.predict(tup, use_net=1)
+    rel = np.abs(out - lab) / lab
+    acc = np.mean(st == psgb.SG_ACCEPT)
+    mlp = np.abs(t0 - lab) / lab
+    print("held-out: accepted %.4f, max rel T error %.2e; network alone: median %.2e p90 %.2e"
+          % (acc, rel.max(), np.median(mlp), np.percentile(mlp, 90)))
+    assert rel.max() <= 1e-2
+    assert acc > 0.9
+
+
+def test_network_gain_over_plain_newton(trained):
+    """What the network adds to the Newton judge: started from the old
+    temperature (no network), cells whose temperature changes by more than a
+    factor 3 in the step rarely converge within the judge's budget; started
+    from the network's prediction, many more do, with fewer rate
+    evaluations.  (On mildly stiff cells the two starts are equivalent, and
+    on non-stiff cells the network is not used at all.)"""
+    import psgb
+    sg, _, _ = trained
+    tup = psgb.sg_stiff_draws(sg, 200000, seed=97)
+    inb = np.all((np.log10(tup) >= np.array(sg.box.lo[:])) & (np.log10(tup) <= np.array(sg.box.hi[:])), axis=1)
+    tup = tup[inb & (tup[:, 1] >= 1e4)]
+    lab = sg.label(tup)
+    big = np.abs(np.log10(lab / tup[:, 1])) > 0.5
+    tup, lab = tup[big], lab[big]
+    assert len(tup) > 200
+    res = {}
+    for use_net in (1, 0):
+        sg.stats(reset=True)
+        out, st, _ = sg.predict(tup, use_net=use_net)
+        acc, oob, rej, below, evals, stiff = sg.stats(reset=True)
+        res[use_net] = (acc / len(tup), evals / max(acc + rej, 1), np.max(np.abs(out - lab) / lab))
+        print("use_net=%d: %d cells changing by > 3x: judge passes %.3f, %.2f rate evaluations "
+              "per cell, max rel T error %.2e" % (use_net, len(tup), *res[use_net]))
+    assert res[1][0] > res[0][0] + 0.05
+    assert res[1][1] < res[0][1]
+    assert res[1][2] <= 1e-2 and res[0][2] <= 1e-2
+
+
+def test_wind_step_with_surrogate(trained):
+    import psgb
+    sg, _, specs = trained
+    plain = psgb.wind_model_solver(specs[0])
+    fast = psgb.wind_model_solver(specs[0])
+    psgb.lib().ps_set_surrogate(fast.ctx, sg.h, 1)
+    sg.stats(reset=True)
+    kMP, kKB = 1.67262171e-24, 1.3806505e-16
+    for chunk in (1, 1, 8, 20):
+        plain.run(chunk)
+        fast.run(chunk)
+        a, b = plain.get_state(), fast.get_state()
+        Ta = a[4] / a[0]
+        Tb = b[4] / b[0]
+        act = (slice(None), slice(2, -2), slice(2, -2))
+        rel = np.abs(Tb[act] - Ta[act]) / Ta[act]
+        print("step", plain.time()[2], "max rel T diff %.2e" % rel.max())
+    st = sg.stats()
+    print("stats accepted/out/rejected/below", st)
+    assert st[0] > 0
+    # one split-source step from the same state: every cell within 1%
+    plain2 = psgb.wind_model_solver(specs[0])
+    fast2 = psgb.wind_model_solver(specs[0])
+    psgb.lib().ps_set_surrogate(fast2.ctx, sg.h, 1)
+    plain2.run(40)
+    fast2.set_state(plain2.get_state())
+    t, dt, step, inv = plain2.time()
+    fast2.set_time(t, dt, step)
+    plain2.split_source(dt, t)
+    fast2.split_source(dt, t)
+    a, b = plain2.get_state(), fast2.get_state()
+    act = (slice(None), slice(2, -2), slice(2, -2))
+    rel = np.abs(b[4][act] - a[4][act]) / a[4][act]
+    print("one split-source step: max rel T diff %.2e" % rel.max())
+    assert rel.max() <= 1e-2
+    assert np.array_equal(a[0][act], b[0][act])
+
+
+def test_batch_with_surrogate_matches_individual(trained):
+    import psgb
+    sg, _, specs = trained
+    sp = specs + [dict(grid=(64, 32), l_star=3e36, krad=0.15, alpharad=-0.65)]
+    solo = [psgb.wind_model_solver(s) for s in sp]
+    inb = [psgb.wind_model_solver(s) for s in sp]
+    for s in solo:
+        psgb.lib().ps_set_surrogate(s.ctx, sg.h, 1)
+    batch = psgb.Batch(inb)
+    psgb.lib().ps_batch_set_surrogate(batch.h, sg.h, 1)
+    for s in solo:
+        s.run(9)
+    batch.run(9)
+    for a, b in zip(solo, inb):
+        assert np.array_equal(a.get_state(), b.get_state())
+    batch.close()
