@@ -1,32 +1,37 @@
 """Benchmark of the GB300 hydro path: cell-updates per second, FP64.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
-                    [--workload wind|blast|batch]
+                    [--workload batch|wind|blast]
 
 Workloads (synthetic inputs of the reference's configurations):
+  batch  Default.  64 independent line-driven disk-wind models (grids drawn
+         from 128x64, 256x128, 384x192, 512x256; L_x log-uniform 1e36..1e38
+         erg/s, k U(0.1, 0.4), alpha U(0.5, 0.7); seed 4), 100 steps, in
+         three forms: plain (each model's ps_run in turn, BLONDIN by bracket
+         + Brent), batched (ps_batch_run) and batched with the learned
+         cooling step (trained on the GPU before timing).  `value` is the
+         last; the other two and the temperature error of the learned step
+         are in `config`.
   wind   2-D spherical (r, theta) line-driven disk wind, 512 x 256 cells
          (r log-spaced 1e10..1e12 cm, theta uniform 0..pi/2), 7 M_sun point
          mass, 1e-20 g/cm^3 halo with a 1e-9 g/cm^3 disk-plane layer at
          4e4 K, L_x = 1e37 erg/s, BLONDIN heating/cooling (Strang split),
          force multiplier M = 0.2 t^-0.6 (M_max 4400) with a synthetic 36-bin
-         UV flux, PLM van Leer, HLL, RK2, CFL 0.4; 1000 steps.  Default.
+         UV flux, PLM van Leer, HLL, RK2, CFL 0.4; 1000 steps, plain form.
   blast  2-D Cartesian ideal-gas blast wave, 256 x 256, PLM MC, HLLC, RK2,
          CFL 0.4, outflow, seeded 1% density noise; 100 steps.
-  batch  64 independent wind models (grids 128x64 .. 512x256, L_x, k and
-         alpha drawn with seed 4) advanced together by ps_batch_run, timed
-         beside the plain form (each model's ps_run in turn); 100 steps.
-One benchmark step is one time step of the whole grid (split source +
+One benchmark step is one time step of every grid (split source +
 AdvanceStep + NextTimeStep); the default K is the configured run length,
 restarted from the initial condition after the warm-up.
 
-value     device-resident throughput: ps_run() replaying the captured CUDA
-          graph, timed with CUDA events on the library's stream, L2 flushed
-          (a 256 MiB write) before each timed step.
-e2e       the same metric through the drop-in entry points with host
-          arrays: per step a pinned host->device copy of Data.Vc,
-          ps_split_source()/ps_advance_step() in the reference's Strang
-          order, a device->host copy, and NextTimeStep on the host; timed
-          by the host clock.
+value     device-resident throughput: CUDA-graph replays timed with CUDA
+          events on the stream the work is issued on, L2 flushed (a 256 MiB
+          write) before each timed step.
+e2e       the same metric through the C ABI with host arrays: per step a
+          pinned host->device copy of every Data.Vc, the step, and a
+          device->host copy (wind/blast: ps_split_source()/ps_advance_step()
+          in the reference's Strang order with NextTimeStep on the host);
+          timed by the host clock.
 roofline  of the fused stage kernel: 40*NVAR algorithmic bytes per
           cell-update split over its two launches, against the measured HBM
           copy bandwidth; the FP64 roofline (measured FMA peak) beside it,
@@ -373,10 +378,43 @@ def _batch_e2e(solvers, batch, V0s, steps):
     return time.perf_counter() - t0, int(sum(v.nbytes for v in V0s))
 
 
+def _sg_training(wl, psgb):
+    """Trains the learned cooling step for the batch: tuples from 16 of the
+    models (GPU runs, snapshots at steps 0, 40 and 120) plus log-uniform
+    draws, 1e6 samples in all, labelled by the reference method on the GPU,
+    40000 Adam steps of 8192 rows on the GPU."""
+    t0 = time.perf_counter()
+    wt = psgb.wind_training_tuples(wl.specs[::4], steps=(0, 40, 120), per_model=6000, seed=3)
+    sg, hist, tup, _ = psgb.train_surrogate(wt, n_draws=1000000 - len(wt), steps=40000,
+                                            batch=8192, seed=3)
+    return sg, {"samples": int(len(tup)), "wind_samples": int(len(wt)),
+                "train_steps": 40000, "batch": 8192, "final_loss": float(hist[-100:].mean()),
+                "seconds": time.perf_counter() - t0}
+
+
+def _sg_check(sg, solvers, psgb):
+    """Temperature error of the learned step on every cell of every model's
+    current state: the surrogate path against the reference method, both
+    on the same (n_H, T, xi, dt) of each cell."""
+    import numpy as np
+    tup = np.concatenate([psgb.sg_collect(s) for s in solvers])
+    ref = sg.label(tup)
+    sg.stats(reset=True)
+    out, st, _ = sg.predict(tup, use_net=1)
+    acc, oob, rej, below, evals, stiff = sg.stats(reset=True)
+    rel = np.abs(out - ref) / ref
+    return {"cells": int(len(tup)), "max_rel_T_error": float(rel.max()),
+            "accepted": acc / max(len(tup), 1), "out_of_box": oob / max(len(tup), 1),
+            "rejected_to_reference": rej / max(len(tup), 1), "stiff": stiff / max(len(tup), 1),
+            "rate_evaluations_per_cell": evals / max(acc + rej, 1)}
+
+
 def batch_bench(wl, steps, warmup, rank, world):
-    """64 wind models: the plain GPU form (each model's ps_run in turn, one
-    graph replay per model and step) against the batched form (ps_batch_run:
-    one launch per phase for all models, one graph replay per step)."""
+    """64 wind models in three forms: the plain GPU form (each model's
+    ps_run in turn, BLONDIN by bracket + Brent), the batched form
+    (ps_batch_run: one launch per phase for all models, one graph replay per
+    step) and the batched form with the learned cooling step (the headline
+    value)."""
     import numpy as np
     import torch
     import psgb
@@ -426,6 +464,8 @@ def batch_bench(wl, steps, warmup, rank, world):
             dist.barrier()
         return ms, clk.summary()
 
+    rate = lambda ms: wl.cells * steps * world / (ms * 1e-3)
+
     # plain GPU form
     plain, _ = make()
 
@@ -442,28 +482,36 @@ def batch_bench(wl, steps, warmup, rank, world):
     for s in plain:
         s.close()
 
-    # batched form
+    # batched form, reference cooling
     solvers, V0s = make()
     batch = psgb.Batch(solvers)
     batch.set_stream(stream.cuda_stream)
     t_tune = time.perf_counter()
     batch.autotune(reps=5)
     t_tune = time.perf_counter() - t_tune
-    for s in solvers:
-        s.restore()
-    launches0 = batch.launches()
-    ms, clocks = timed(lambda: batch.run(1), lambda: [s.restore() for s in solvers])
-    launches = batch.launches() - launches0
-    flags = batch.sync()
+    restore_all = lambda: [s.restore() for s in solvers]
+    restore_all()
+    ms_batched, _ = timed(lambda: batch.run(1), restore_all)
     same = all(np.array_equal(a, s.get_state()) for a, s in zip(plain_end, solvers[:4]))
-    value = wl.cells * steps * world / (ms * 1e-3)
-    value_plain = wl.cells * steps * world / (ms_plain * 1e-3)
     shapes = {}
     for m, sp in enumerate(wl.specs):
         shapes["%dx%d" % tuple(sp["grid"])] = "%dx%d" % batch.shape(m)
 
-    for s in solvers:
-        s.restore()
+    # batched form with the learned cooling step (headline)
+    sg, train = _sg_training(wl, psgb)
+    psgb.lib().ps_batch_set_surrogate(batch.h, sg.h, 1)
+    restore_all()
+    sg.stats(reset=True)
+    launches0 = batch.launches()
+    ms, clocks = timed(lambda: batch.run(1), restore_all)
+    launches = batch.launches() - launches0
+    flags = batch.sync()
+    run_stats = dict(zip(["accepted", "out_of_box", "rejected", "below_1e4K", "rate_evaluations",
+                          "stiff"], sg.stats(reset=True)))
+    check = _sg_check(sg, solvers, psgb)
+    value = rate(ms)
+
+    restore_all()
     per_kernel = np.zeros(3)
     reps = 10
     for _ in range(reps):
@@ -480,18 +528,25 @@ def batch_bench(wl, steps, warmup, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (the reference configuration's initial condition, generated)",
         "config": {"workload": wl.desc, "cells": wl.cells, "models": len(wl.specs),
-                   "method": "batched GPU form (ps_batch_run, one CUDA graph per step)",
-                   "plain_value": value_plain, "plain_ms_per_step": ms_plain / steps,
-                   "speedup_vs_plain": value / value_plain,
-                   "identical_to_plain": same,
+                   "method": "batched GPU form with the learned cooling step (ps_batch_run + "
+                             "ps_batch_set_surrogate, one CUDA graph per step)",
+                   "plain_value": rate(ms_plain), "plain_ms_per_step": ms_plain / steps,
+                   "batched_value": rate(ms_batched), "batched_ms_per_step": ms_batched / steps,
+                   "speedup_vs_plain": ms_plain / ms,
+                   "speedup_batched_only_vs_plain": ms_plain / ms_batched,
+                   "batched_identical_to_plain": same,
+                   "cooling_T_error": check, "surrogate_run_counters": run_stats,
+                   "surrogate_training": train,
+                   "hydro": "bit-exact against the oracle (tests/test_gpu_wind.py, "
+                            "tests/test_gpu_batch.py); the learned step only changes pressure",
                    "tile_shapes": shapes, "autotune_s": t_tune,
                    "l2": "256 MiB buffer written before every timed step (L2 flushed)",
                    "parallelism": "replicas only" if world > 1 else "single GPU"},
         "e2e": {"value": wl.cells * e2e_steps / e2e_wall, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
                 "steps": e2e_steps,
-                "path": "per step: H2D of every model's Data.Vc, ps_batch_run(1), D2H of every "
-                        "model's Data.Vc (pinned host memory)"},
+                "path": "per step: H2D of every model's Data.Vc, ps_batch_run(1) with the "
+                        "learned cooling step, D2H of every model's Data.Vc (pinned host memory)"},
         "gpu_launches": int(launches),
         "device_flags": int(flags),
         "clocks": clocks,
@@ -561,7 +616,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="wind", choices=["wind", "blast", "batch"])
+    ap.add_argument("--workload", default="batch", choices=["wind", "blast", "batch"])
     a = ap.parse_args()
     wl = Workload(a.workload)
     steps = a.steps if a.steps is not None else wl.steps
