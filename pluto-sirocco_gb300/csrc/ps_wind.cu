@@ -128,7 +128,6 @@ void ps_wind_free(ps::WindDev *w)
   if (!w) return;
   cudaFree(w->geo);
   cudaFree(w->off);
-  cudaFree(w->ang);
   cudaFree(w->ent);
   cudaFree(w->dvds);
   cudaFree(w->xi);
@@ -156,10 +155,10 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   // geometry (Src/set_geometry.c:62-240) and PLM weights (plm_coeffs.c:30-74)
   enum {
     G_X1, G_DX1, G_INVDX1, G_RINV, G_ABSX1, G_ABSX1P, G_A1F, G_DVR, G_RDR, G_RTINV, G_G0, G_X11A,
-    G_X22A, G_LOCR, G_XGC1, N1ARR
+    G_X22A, G_LOCR, G_XGC1, G_FX, N1ARR
   };
   enum { H_X2, H_DX2, H_INVDX2, H_DMU, H_SXP, H_SPABS, H_SN, H_CT, H_SIN2, H_COS2, H_X11B, H_X22B,
-         H_XGC2, N2ARR };
+         H_XGC2, H_FY, N2ARR };
   std::vector<double> a1((size_t)N1ARR * n0, 0.0), a2((size_t)N2ARR * n1, 0.0);
   std::vector<double> plm((size_t)12 * (n0 > n1 ? n0 : n1), 0.0);
   const int nmax = n0 > n1 ? n0 : n1;
@@ -186,6 +185,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
     if (i >= 1 && i + 1 < n0) {
       A1(G_X11A, i) = (x1[i - 1] + x1[i]) / 2.0 * UL;
       A1(G_X22A, i) = (x1[i + 1] + x1[i]) / 2.0 * UL;
+      A1(G_FX, i) = (A1(G_LOCR, i) - A1(G_X11A, i)) / (A1(G_X22A, i) - A1(G_X11A, i));
     }
   }
   for (int j = 0; j < n1; j++) {
@@ -206,6 +206,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
     if (j >= 1 && j + 1 < n1) {
       A2(H_X11B, j) = (x2[j - 1] + x2[j]) / 2.0;
       A2(H_X22B, j) = (x2[j + 1] + x2[j]) / 2.0;
+      A2(H_FY, j) = (x2[j] - A2(H_X11B, j)) / (A2(H_X22B, j) - A2(H_X11B, j));
     }
   }
   for (int d = 0; d < 2; d++) {
@@ -229,7 +230,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   const int na = wp->line_force ? wp->nangles : 0;
   const size_t ncell = (size_t)n0 * n1;
   std::vector<int> off((size_t)p.nx[0] * p.nx[1] + 1, 0), ang;
-  std::vector<double> eFr, eFt, eRo, eTo, eSt, eCt, eDs;
+  std::vector<double> eFr, eFt, eF1, eF2, eC1a, eC1b, eC2a, eC2b, eIds;
   for (int jj = 0; jj < p.nx[1]; jj++) {
     for (int ii = 0; ii < p.nx[0]; ii++) {
       const int i = ii + p.beg[0], j = jj + p.beg[1];
@@ -254,14 +255,23 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
           ro = std::sqrt((x + ddx1) * (x + ddx1) + (z + ddx2) * (z + ddx2));
           to = std::atan((x + ddx1) / (z + ddx2));
         }
+        // VGradCalc's static part (line_connect.c:628-738): the bilinear
+        // weights of the offset point and the projections of (v_r, v_theta)
+        // at the centre and at the offset point on the bin direction
+        const double th = (a + 0.5) * (2.0 * ps::kPI) / 36.0;
+        const double sa = std::sin(th), ca = std::cos(th);
+        const double st = std::sin(to), ctt = std::cos(to);
+        const double s2 = A2(H_SIN2, j), c2 = A2(H_COS2, j);
         ang.push_back(a);
         eFr.push_back(fr);
         eFt.push_back(ft);
-        eRo.push_back(ro);
-        eTo.push_back(to);
-        eSt.push_back(std::sin(to));
-        eCt.push_back(std::cos(to));
-        eDs.push_back(ds);
+        eF1.push_back((ro - A1(G_X11A, i)) / (A1(G_X22A, i) - A1(G_X11A, i)));
+        eF2.push_back((to - A2(H_X11B, j)) / (A2(H_X22B, j) - A2(H_X11B, j)));
+        eC1a.push_back(UV * (sa * s2 + ca * c2));
+        eC1b.push_back(UV * (sa * c2 - ca * s2));
+        eC2a.push_back(UV * (sa * st + ca * ctt));
+        eC2b.push_back(UV * (sa * ctt - ca * st));
+        eIds.push_back(ds == -999 ? 0.0 : 1.0 / ds);
       }
     }
   }
@@ -288,13 +298,11 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   WTRY(cudaMalloc(&w->off, off.size() * sizeof(int)));
   WTRY(cudaMemcpy(w->off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
   const long ne = nent > 0 ? nent : 1;
-  WTRY(cudaMalloc(&w->ang, ne * sizeof(int)));
-  WTRY(cudaMalloc(&w->ent, 7 * ne * sizeof(double)));
+  WTRY(cudaMalloc(&w->ent, 9 * ne * sizeof(double)));
   WTRY(cudaMalloc(&w->dvds, ne * sizeof(double)));
   if (nent > 0) {
-    WTRY(cudaMemcpy(w->ang, ang.data(), nent * sizeof(int), cudaMemcpyHostToDevice));
-    const std::vector<double> *cols[7] = {&eFr, &eFt, &eRo, &eTo, &eSt, &eCt, &eDs};
-    for (int k = 0; k < 7; k++)
+    const std::vector<double> *cols[9] = {&eFr, &eFt, &eF1, &eF2, &eC1a, &eC1b, &eC2a, &eC2b, &eIds};
+    for (int k = 0; k < 9; k++)
       WTRY(cudaMemcpy(w->ent + k * ne, cols[k]->data(), nent * sizeof(double),
                       cudaMemcpyHostToDevice));
   }
@@ -317,9 +325,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   G.rdr = g1 + (size_t)G_RDR * n0;
   G.rtinv = g1 + (size_t)G_RTINV * n0;
   G.g0 = g1 + (size_t)G_G0 * n0;
-  G.x11a = g1 + (size_t)G_X11A * n0;
-  G.x22a = g1 + (size_t)G_X22A * n0;
-  G.locr = g1 + (size_t)G_LOCR * n0;
+  G.fx = g1 + (size_t)G_FX * n0;
   G.x2 = g2 + (size_t)H_X2 * n1;
   G.dx2 = g2 + (size_t)H_DX2 * n1;
   G.inv_dx2 = g2 + (size_t)H_INVDX2 * n1;
@@ -330,8 +336,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   G.ct = g2 + (size_t)H_CT * n1;
   G.sin2 = g2 + (size_t)H_SIN2 * n1;
   G.cos2 = g2 + (size_t)H_COS2 * n1;
-  G.x11b = g2 + (size_t)H_X11B * n1;
-  G.x22b = g2 + (size_t)H_X22B * n1;
+  G.fy = g2 + (size_t)H_FY * n1;
   for (int d = 0; d < 2; d++) {
     const double *P = gp + (size_t)d * 6 * nmax;
     G.cp[d] = P + 0 * nmax;
@@ -343,15 +348,16 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   }
   ps::LineList &L = w->a.L;
   L.off = w->off;
-  L.ang = w->ang;
   L.Fr = w->ent + 0 * ne;
   L.Ft = w->ent + 1 * ne;
-  L.roff = w->ent + 2 * ne;
-  L.toff = w->ent + 3 * ne;
-  L.sinto = w->ent + 4 * ne;
-  L.costo = w->ent + 5 * ne;
-  L.ds = w->ent + 6 * ne;
-  L.dvds = w->dvds;
+  L.fr1 = w->ent + 2 * ne;
+  L.fr2 = w->ent + 3 * ne;
+  L.c1a = w->ent + 4 * ne;
+  L.c1b = w->ent + 5 * ne;
+  L.c2a = w->ent + 6 * ne;
+  L.c2b = w->ent + 7 * ne;
+  L.inv_ds = w->ent + 8 * ne;
+  L.lq = w->dvds;
 
   ps::WindParams &W = w->a.w;
   std::memset(&W, 0, sizeof(W));
@@ -375,10 +381,12 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   W.t_x = wp->t_x;
   W.unit_pressure = UD * UV * UV;
   W.unit_time = UL / UV;
-  for (int a = 0; a < 64; a++) {
-    const double th = (a + 0.5) * (2.0 * ps::kPI) / 36.0;
-    W.sin_a[a] = std::sin(th);
-    W.cos_a[a] = std::cos(th);
+  {
+    // t = sigma_e rho_cgs v_th / (dv/ds), v_th = sqrt(2 kB T / m_p),
+    // T = p / rho KELVIN mu  =>  t = C sqrt(rho p) / (dv/ds) in code units
+    const double C = W.sigma_e * UD * std::sqrt(W.kelvin * W.mu * 2.0 * ps::kKB / ps::kMP);
+    W.lf_a0 = std::log(W.krad) + W.alpharad * std::log(C);
+    W.lf_cf = W.sigma_e / ps::kC / W.unit_acc;
   }
 
   w->k1 = ps::stage_kernel_sph(p.nvar, p.limiter, p.solver, 1);

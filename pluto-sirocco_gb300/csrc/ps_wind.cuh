@@ -21,7 +21,7 @@ struct SphGeom {
   const double *rdr;     // |x1|*dx1
   const double *rtinv;   // 1/rt                    (dx/dl in x2, r_1 of the x2 sources)
   const double *g0;      // -1*GM/(x1*x1)            (BodyForceVector)
-  const double *x11a, *x22a, *locr;  // VGradCalc interpolation corners / centre (cm)
+  const double *fx;      // VGradCalc: bilinear weight of the cell centre in x1
   // x2 direction (ntot[1] entries)
   const double *x2, *dx2, *inv_dx2;
   const double *dmu;     // |cos(x2m) - cos(x2p)|
@@ -30,7 +30,7 @@ struct SphGeom {
   const double *sn;      // |sin(x2)|
   const double *ct;      // 1/tan(x2)
   const double *sin2, *cos2;
-  const double *x11b, *x22b;
+  const double *fy;      // VGradCalc: bilinear weight of the cell centre in x2
   // PLM weights per direction
   const double *cp[2], *cm[2], *wp[2], *wm[2], *dp[2], *dm[2];
 };
@@ -39,10 +39,14 @@ struct SphGeom {
 // bin order (the order the reference sums them in), as a CSR list.
 struct LineList {
   const int *off;        // [nx0*nx1 + 1], active cell (i, j) -> (j*nx0 + i)
-  const int *ang;        // bin index
-  const double *Fr, *Ft;
-  const double *roff, *toff, *sinto, *costo, *ds;
-  double *dvds;          // per-entry dv/ds of the current stage
+  const double *Fr, *Ft; // the bin's flux
+  const double *fr1, *fr2;  // bilinear weights of the bin's offset point (static)
+  // projections of the interpolated (v_r, v_theta) on the bin direction,
+  // times UNIT_VELOCITY: at the cell centre (c1a, c1b) and at the offset
+  // point (c2a, c2b)
+  const double *c1a, *c1b, *c2a, *c2b;
+  const double *inv_ds;  // 1 / ds; 0 for a bin without direction (dv/ds = -999)
+  double *lq;            // per entry and stage: -alpharad * log(dv/ds), -inf if dv/ds <= 0
 };
 
 struct WindParams {
@@ -53,7 +57,10 @@ struct WindParams {
   double krad, alpharad, sigma_e, unit_acc;
   double lx, t_x;        // L_star*f_x, T_x
   double unit_pressure, unit_time;
-  double sin_a[64], cos_a[64];  // sin/cos of the bin directions
+  // force multiplier M = krad t^alpharad with t = C sqrt(rho p) / (dv/ds)
+  // (code-unit rho and p): lf_a0 = log(krad) + alpharad log(C); the
+  // acceleration per bin is (1 + M) F lf_cf
+  double lf_a0, lf_cf;
 };
 
 struct WindStageArgs {

@@ -27,9 +27,9 @@ namespace ps {
 struct WindDev {
   WindStageArgs a;       // geometry, line list, parameters (stage part filled per launch)
   double *geo = nullptr; // all 1-D geometry arrays in one allocation
-  int *off = nullptr, *ang = nullptr;
-  double *ent = nullptr; // Fr, Ft, roff, toff, sinto, costo, ds (SoA, nent each)
-  double *dvds = nullptr;
+  int *off = nullptr;
+  double *ent = nullptr; // Fr, Ft, fr1, fr2, c1a, c1b, c2a, c2b, inv_ds (SoA, nent each)
+  double *dvds = nullptr; // per-entry stage values (LineList::lq)
   double *xi = nullptr, *tr = nullptr;
   long nent = 0;
   const void *k1 = nullptr, *k2 = nullptr;
@@ -258,42 +258,39 @@ __device__ __forceinline__ void blondin_cell(double *V, const double *xi_s, cons
 // spherical stage kernel
 // ---------------------------------------------------------------
 
-__device__ __forceinline__ void bilinear(double x110, double x111, double x220, double x221,
-                                         const double (&v11)[2], const double (&v12)[2],
-                                         const double (&v21)[2], const double (&v22)[2],
-                                         double t0, double t1, double (&ans)[2])
+// bilinear() of line_connect.c:746-777 with the weights of the target
+// point given: ans = (1-fy)((1-fx) v11 + fx v21) + fy((1-fx) v12 + fx v22)
+__device__ __forceinline__ void bilinear_w(double fx, double fy, const double (&v11)[2],
+                                           const double (&v12)[2], const double (&v21)[2],
+                                           const double (&v22)[2], double (&ans)[2])
 {
-  const double fracx1 = (t0 - x110) / (x220 - x110);
-  const double fracx2 = (t1 - x111) / (x221 - x111);
-  double temp1 = (1.0 - fracx1) * v11[0] + fracx1 * v21[0];
-  double temp2 = (1.0 - fracx1) * v12[0] + fracx1 * v22[0];
-  ans[0] = (1.0 - fracx2) * temp1 + fracx2 * temp2;
-  temp1 = (1.0 - fracx1) * v11[1] + fracx1 * v21[1];
-  temp2 = (1.0 - fracx1) * v12[1] + fracx1 * v22[1];
-  ans[1] = (1.0 - fracx2) * temp1 + fracx2 * temp2;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const double t1 = (1.0 - fx) * v11[k] + fx * v21[k];
+    const double t2 = (1.0 - fx) * v12[k] + fx * v22[k];
+    ans[k] = (1.0 - fy) * t1 + fy * t2;
+  }
 }
 
-// LineForce component `comp` (0: r, 1: theta) for the state vg of one cell.
+// LineForce component `comp` (0: r, 1: theta) for the state vg of one cell
+// (line_connect.c:815-903): sum over the cell's bins of
+// (1 + M) sigma_e F / c, M = min(krad t^alpharad, 4400), t = sigma_e rho
+// v_th / (dv/ds), M = 0 where dv/ds <= 0.  Evaluated as
+// M = exp(lf_a0 + alpharad/2 log(rho p) + lq) with lq = -alpharad log(dv/ds)
+// from VGradCalc (one log per call, one exp per bin).
 template <int NV>
 __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineList &L,
                                              const WindParams &w, int e0, int e1, int comp)
 {
-  const double rho = vg[RHO] * w.unit_density;
-  const double T = vg[PRS] / vg[RHO] * w.kelvin * w.mu;
-  const double v_th = sqrt((2.0 * kKB * T) / kMP);
+  const double base = w.lf_a0 + 0.5 * w.alpharad * log(vg[RHO] * vg[PRS]);
   double g = 0.0;
   for (int e = e0; e < e1; e++) {
-    const double dvds = L.dvds[e];
-    double M = 0.0;
-    if (dvds > 0.0) {
-      const double t_UV = w.sigma_e * rho * v_th / dvds;
-      M = w.krad * pow(t_UV, w.alpharad);
-      if (M > 4400.) M = 4400.;
-    }
+    double M = exp(base + L.lq[e]);
+    if (M > 4400.) M = 4400.;
     const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
-    g += ((1.0 + M) * w.sigma_e * F / kC) / w.unit_acc;
+    g += (1.0 + M) * F;
   }
-  return g;
+  return g * w.lf_cf;
 }
 
 template <int D, int NV, int LIM, int SOLVER, class TL>
@@ -522,30 +519,21 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       v22[1] = (V2[jp] + V2[jp + 1] + V2[sc0 + 1] + V2[sc0]) / 4.0;
       v21[0] = (V1[sc0 + 1] + V1[jm + 1] + V1[jm] + V1[sc0]) / 4.0;
       v21[1] = (V2[sc0 + 1] + V2[jm + 1] + V2[jm] + V2[sc0]) / 4.0;
-      const double x110 = g.x11a[gi], x111 = g.x11b[gj], x220 = g.x22a[gi], x221 = g.x22b[gj];
-      bilinear(x110, x111, x220, x221, v11, v12, v21, v22, g.locr[gi], g.x2[gj], ans1);
-      const double UV = A.w.unit_velocity;
-      const double vx1 = (ans1[0] * UV * g.sin2[gj] + ans1[1] * UV * g.cos2[gj]);
-      const double vz1 = (ans1[0] * UV * g.cos2[gj] - ans1[1] * UV * g.sin2[gj]);
+      bilinear_w(g.fx[gi], g.fy[gj], v11, v12, v21, v22, ans1);
+      const double alpha = A.w.alpharad;
       for (int e = e0; e < e1; e++) {
-        const double ds = A.L.ds[e];
-        double dvds;
-        if (ds == -999) {
-          dvds = -999;
-        } else {
+        const double ids = A.L.inv_ds[e];
+        double lq = -INFINITY;
+        if (ids != 0.0) {
           double ans2[2];
-          bilinear(x110, x111, x220, x221, v11, v12, v21, v22, A.L.roff[e], A.L.toff[e], ans2);
-          const double st = A.L.sinto[e], ctt = A.L.costo[e];
-          const double vx2 = (ans2[0] * UV * st + ans2[1] * UV * ctt);
-          const double vz2 = (ans2[0] * UV * ctt - ans2[1] * UV * st);
-          const int an = A.L.ang[e];
-          const double sa = A.w.sin_a[an], ca = A.w.cos_a[an];
-          const double v1 = sa * vx1 + ca * vz1;
-          const double v2 = sa * vx2 + ca * vz2;
-          dvds = fabs((v2 - v1) / ds);
+          bilinear_w(A.L.fr1[e], A.L.fr2[e], v11, v12, v21, v22, ans2);
+          const double v1 = ans1[0] * A.L.c1a[e] + ans1[1] * A.L.c1b[e];
+          const double v2 = ans2[0] * A.L.c2a[e] + ans2[1] * A.L.c2b[e];
+          const double dvds = fabs(v2 - v1) * ids;
+          if (is_nan_bits(dvds)) flags |= F_NAN;
+          if (dvds > 0.0) lq = -alpha * log(dvds);
         }
-        if (is_nan_bits(dvds)) flags |= F_NAN;
-        A.L.dvds[e] = dvds;
+        A.L.lq[e] = lq;
       }
     }
   }
