@@ -35,9 +35,6 @@ struct BatchModel {
 struct TileItem {
   int m, bx, by, pad;
 };
-struct BlockItem {
-  int m, b;
-};
 
 __device__ __forceinline__ void tensormap_acquire(const CUtensorMap *tm)
 {
@@ -114,13 +111,12 @@ __device__ __forceinline__ SgCoolArgs batch_cool_args(const BatchModel &M, const
 
 __global__ void __launch_bounds__(128)
     k_batch_sg_cool(const BatchModel *__restrict__ models, const BlockItem *__restrict__ blocks,
-                    const double *const *xi, const double *const *tr, SgNet net, SgBox bx,
-                    int use_net, int2 *queue, int *qcount, unsigned long long *stats)
+                    int nitems, const double *const *xi, const double *const *tr, SgNet net,
+                    SgBox bx, int use_net, int2 *queue, int *qcount, unsigned long long *stats)
 {
   extern __shared__ __align__(1024) unsigned char smem[];
-  const BlockItem bi = blocks[blockIdx.x];
-  const SgCoolArgs A = batch_cool_args(models[bi.m], xi[bi.m], tr[bi.m]);
-  sg_cool_block(net, bx, A, bi.m, bi.b, use_net, smem, queue, qcount, stats);
+  auto args_of = [&](int m) { return batch_cool_args(models[m], xi[m], tr[m]); };
+  sg_cool_items(net, bx, args_of, blocks, nitems, use_net, smem, queue, qcount, stats);
 }
 
 __global__ void k_batch_sg_fallback(const BatchModel *__restrict__ models, const double *const *xi,
@@ -209,11 +205,14 @@ struct ps_batch {
   long total_cells = 0;
   ps_surrogate *sg = nullptr;
   int sg_use_net = 1;
+  int num_sms = 148;
   int2 *sg_queue = nullptr;
   int *sg_qcount = nullptr;
   int lim = 0, solver = 0, cooling = 0;
   cudaStream_t stream = nullptr;      // stream the work is issued on
   cudaStream_t own_stream = nullptr;  // stream created by the batch
+  cudaStream_t side[ps::kNumShapes] = {nullptr, nullptr, nullptr};  // tile-shape groups
+  cudaEvent_t fork = nullptr, join[ps::kNumShapes] = {nullptr, nullptr, nullptr};
   cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};
   long long host_step = 0;
   long launches = 0;
@@ -343,15 +342,27 @@ static int batch_upload(ps_batch *b)
   return 0;
 }
 
+// The stage kernels of the tile-shape groups run side by side (a fork onto
+// the group streams and a join back), so that one group's tail overlaps the
+// others' work; the groups touch disjoint models.
 static int batch_stage(ps_batch *b, int stage)
 {
+  int first = -1;
+  for (int s = 0; s < ps::kNumShapes; s++)
+    if (b->nitems[s] && first < 0) first = s;
+  BCK(cudaEventRecord(b->fork, b->stream));
   for (int s = 0; s < ps::kNumShapes; s++) {
     if (!b->nitems[s]) continue;
+    cudaStream_t st = s == first ? b->stream : b->side[s];
+    if (s != first) BCK(cudaStreamWaitEvent(st, b->fork, 0));
     const void *k = ps::batch_kernel(s, b->lim, b->solver, stage);
     void *args[2] = {&b->d_models, &b->d_items[s]};
-    BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(256), args, ps::batch_smem(s), b->stream));
+    BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(256), args, ps::batch_smem(s), st));
     b->launches++;
+    if (s != first) BCK(cudaEventRecord(b->join[s], st));
   }
+  for (int s = 0; s < ps::kNumShapes; s++)
+    if (b->nitems[s] && s != first) BCK(cudaStreamWaitEvent(b->stream, b->join[s], 0));
   return 0;
 }
 
@@ -372,9 +383,10 @@ static int batch_cool(ps_batch *b)
   if (!b->cooling) return 0;
   if (b->sg) {
     BCK(cudaMemsetAsync(b->sg_qcount, 0, sizeof(int), b->stream));
-    ps::k_batch_sg_cool<<<b->ncells128, 128, ps::kInfBytes, b->stream>>>(
-        b->d_models, b->d_cells128, b->d_xi, b->d_tr, ps_sg_net(b->sg), ps_sg_boxv(b->sg),
-        b->sg_use_net, b->sg_queue, b->sg_qcount, ps_sg_stats_dev(b->sg));
+    const int grid = std::min(b->ncells128, b->num_sms * ps::kInfCtasPerSm);
+    ps::k_batch_sg_cool<<<grid, 128, ps::kInfBytes, b->stream>>>(
+        b->d_models, b->d_cells128, b->ncells128, b->d_xi, b->d_tr, ps_sg_net(b->sg),
+        ps_sg_boxv(b->sg), b->sg_use_net, b->sg_queue, b->sg_qcount, ps_sg_stats_dev(b->sg));
     ps::k_batch_sg_fallback<<<1216, 128, 0, b->stream>>>(b->d_models, b->d_xi, b->d_tr, b->sg_queue,
                                                          b->sg_qcount);
     b->launches += 2;
@@ -416,6 +428,11 @@ static void batch_free(ps_batch *b)
   cudaFree(b->d_cells128);
   cudaFree(b->sg_queue);
   cudaFree(b->sg_qcount);
+  for (int k = 0; k < ps::kNumShapes; k++) {
+    if (b->side[k]) cudaStreamDestroy(b->side[k]);
+    if (b->join[k]) cudaEventDestroy(b->join[k]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
 }
@@ -444,11 +461,24 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
   if ((e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaMalloc(&b->d_models, sizeof(ps::BatchModel) * n)) != cudaSuccess ||
       (e = cudaMalloc(&b->d_xi, sizeof(double *) * n)) != cudaSuccess ||
-      (e = cudaMalloc(&b->d_tr, sizeof(double *) * n)) != cudaSuccess) {
+      (e = cudaMalloc(&b->d_tr, sizeof(double *) * n)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess) {
     batch_free(b);
     return batch_cuda(e, "ps_batch_create");
   }
   b->stream = b->own_stream;
+  for (int k = 0; k < ps::kNumShapes; k++) {
+    if ((e = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming)) != cudaSuccess) {
+      batch_free(b);
+      return batch_cuda(e, "ps_batch_create: streams");
+    }
+  }
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   std::vector<const double *> xi(n), tr(n);
   for (int m = 0; m < n; m++) {
     xi[m] = ctxs[m]->wind->xi;

@@ -3,8 +3,6 @@
 // implicit trapezoidal energy equation in T solved by bracket expansion and
 // Brent's method, shared by the wind kernels, the batched kernels and the
 // surrogate (which uses it as its fallback and to label training pairs).
-// Also the analytic T-derivative of the net rate, used by the Newton steps
-// that polish and judge the surrogate's prediction.
 #pragma once
 
 #include "ps_hydro.cuh"
@@ -41,55 +39,6 @@ __device__ __forceinline__ double bl_heatcool(const BlCtx &b, double T)
   const double brem_cool = 1.0 * (3.3e-27 * sqT);
   return b.nH *
          (ne * comp_heat + b.nH * xray_heat - ne * comp_cool - ne * line_cool - ne * brem_cool);
-}
-
-// heatcool and d(heatcool)/dT, differentiated term by term:
-//   ne = nH r(T), r = 1e-2 + 10^(a + b log10 T) -> r' = b 10^(a + b log10 T) / T (same for the
-//   middle branch without the 1e-2), 0 above 3.3e4 K;
-//   comp_cool' = 8.9e-36 xi 4; xray' = -xray / (2T);
-//   line term 1e-16 e^(-1.3e5/T) / (sqrt(xi) T): ' = term (1.3e5/T^2 - 1/T);
-//   the min() term: 0, 2.5e-27/sqrt(T) or -1.5e-17/T^2 by the active branch;
-//   brem' = brem / (2T).
-__device__ __forceinline__ double bl_heatcool_d(const BlCtx &b, double T, double &dhc)
-{
-  const double sqT = sqrt(T);
-  double r, dr;
-  if (T < 1.5e4) {
-    const double q = pow(10.0, (-51.59417133 + 12.27740153 * log10(T)));
-    r = 1e-2 + q;
-    dr = 12.27740153 * q / T;
-  } else if (T < 3.3e4) {
-    const double q = pow(10.0, (-3.80749689 + 0.86092628 * log10(T)));
-    r = q;
-    dr = 0.86092628 * q / T;
-  } else {
-    r = 1.21;
-    dr = 0.0;
-  }
-  const double ne = b.nH * r, dne = b.nH * dr;
-  const double comp_heat = 8.9e-36 * b.xi * b.tx;
-  const double comp_cool = 8.9e-36 * b.xi * (4.0 * T), dcomp_cool = 8.9e-36 * b.xi * 4.0;
-  const double xray_heat = 1.5e-21 * (b.sqsqxi / sqT), dxray_heat = -0.5 * xray_heat / T;
-  const double l1 = 1e-16 * exp(-1.3e5 / T) / b.sqxi / T;
-  const double dl1 = l1 * (1.3e5 / (T * T) - 1.0 / T);
-  const double m1 = 5e-27 * sqT, m2 = 1.5e-17 / T;
-  double l2, dl2;
-  if (1e-24 <= m1 && 1e-24 <= m2) {
-    l2 = 1e-24;
-    dl2 = 0.0;
-  } else if (m1 <= m2) {
-    l2 = m1;
-    dl2 = 0.5 * m1 / T;
-  } else {
-    l2 = m2;
-    dl2 = -m2 / T;
-  }
-  const double line_cool = l1 + l2, dline_cool = dl1 + dl2;
-  const double brem_cool = 3.3e-27 * sqT, dbrem_cool = 0.5 * brem_cool / T;
-  const double net = comp_heat - comp_cool - line_cool - brem_cool;
-  const double dnet = -dcomp_cool - dline_cool - dbrem_cool;
-  dhc = b.nH * (dne * net + ne * dnet + b.nH * dxray_heat);
-  return b.nH * (ne * net + b.nH * xray_heat);
 }
 
 // zfunc (cooling.c:233-237)

@@ -41,4 +41,5 @@ struct ps_ctx {
   int sg_use_net;           // 0: Newton from the old temperature (no network)
   void *sg_queue;           // cells left to the reference method (int2 each)
   int *sg_qcount;
+  void *sg_items;           // (0, block) work items of the surrogate kernel
 };

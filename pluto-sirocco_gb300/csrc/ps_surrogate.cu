@@ -364,14 +364,19 @@ __global__ void __launch_bounds__(128) k_sg_predict(SgNet net, SgBox bx, const d
   const uint32_t tmem = sg_inf_setup(net, smem);
   const long r = blockIdx.x * (long)kSgRows + threadIdx.x;
   const bool active = r < n;
-  BlCtx b;
+  SgCtx b;
   double T = 0.0;
   float x[4] = {0.f, 0.f, 0.f, 0.f};
   bool inbox = false;
   int st = SG_BELOW_MIN;
   if (active) {
     T = tup[n + r];
-    sg_tuple_ctx(bx, tup[r], T, tup[2 * n + r], tup[3 * n + r], b);
+    b.nH = tup[r];
+    b.n = b.nH * 1.43 / bx.mu;
+    b.E = T * b.n * kKB * 1.5;
+    b.xi = tup[2 * n + r];
+    b.tx = bx.t_x;
+    b.dt = tup[3 * n + r];
     if (T >= 1.e4) {
       st = SG_OUT_OF_BOX;
       inbox = sg_features(bx, tup[r], T, tup[2 * n + r], tup[3 * n + r], x);
@@ -420,12 +425,15 @@ __global__ void k_sg_fallback_tuples(SgBox bx, const double *__restrict__ tup, l
 // the wind's split-source step with the surrogate
 // ------------------------------------------------------------------
 
-__global__ void __launch_bounds__(128) k_sg_cool(SgNet net, SgBox bx, SgCoolArgs A, int use_net,
-                                                 int2 *queue, int *qcount,
+__global__ void __launch_bounds__(128) k_sg_cool(SgNet net, SgBox bx, SgCoolArgs A,
+                                                 const BlockItem *__restrict__ items, int nitems,
+                                                 int use_net, int2 *queue, int *qcount,
                                                  unsigned long long *stats)
 {
   extern __shared__ __align__(1024) unsigned char smem[];
-  sg_cool_block(net, bx, A, 0, blockIdx.x, use_net, smem, queue, qcount, stats);
+  if (A.sc->done) return;
+  auto args_of = [&](int) { return A; };
+  sg_cool_items(net, bx, args_of, items, nitems, use_net, smem, queue, qcount, stats);
 }
 
 __global__ void k_sg_cool_fallback(SgCoolArgs A, const int2 *__restrict__ queue,
@@ -904,8 +912,13 @@ extern "C" int ps_set_surrogate(ps_ctx *c, ps_surrogate *s, int use_net)
   if (s) SCK(cudaStreamSynchronize(s->stream));
   if (s && !c->sg_queue) {
     const size_t ncell = (size_t)c->p.nx[0] * c->p.nx[1];
+    const int nblk = (int)((ncell + ps::kSgRows - 1) / ps::kSgRows);
+    std::vector<ps::BlockItem> items(nblk);
+    for (int k = 0; k < nblk; k++) items[k] = ps::BlockItem{0, k};
     SCK(cudaMalloc(&c->sg_queue, sizeof(int2) * ncell));
     SCK(cudaMalloc(&c->sg_qcount, sizeof(int)));
+    SCK(cudaMalloc(&c->sg_items, sizeof(ps::BlockItem) * nblk));
+    SCK(cudaMemcpy(c->sg_items, items.data(), sizeof(ps::BlockItem) * nblk, cudaMemcpyHostToDevice));
   }
   c->sg = s;
   c->sg_use_net = use_net;
@@ -920,9 +933,13 @@ int ps_sg_cool_launch(ps_ctx *c)
   const ps::SgCoolArgs A = sg_cool_args(c);
   const int ncell = c->p.nx[0] * c->p.nx[1];
   SCK(cudaMemsetAsync(c->sg_qcount, 0, sizeof(int), c->stream));
-  ps::k_sg_cool<<<(ncell + ps::kSgRows - 1) / ps::kSgRows, 128, ps::kInfBytes, c->stream>>>(
-      s->net(), s->box, A, c->sg_use_net, reinterpret_cast<int2 *>(c->sg_queue), c->sg_qcount,
-      s->stats);
+  const int nblk = (ncell + ps::kSgRows - 1) / ps::kSgRows;
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  ps::k_sg_cool<<<std::min(nblk, nsm * ps::kInfCtasPerSm), 128, ps::kInfBytes, c->stream>>>(
+      s->net(), s->box, A, reinterpret_cast<const ps::BlockItem *>(c->sg_items), nblk,
+      c->sg_use_net, reinterpret_cast<int2 *>(c->sg_queue), c->sg_qcount, s->stats);
   ps::k_sg_cool_fallback<<<608, 128, 0, c->stream>>>(A, reinterpret_cast<int2 *>(c->sg_queue),
                                                      c->sg_qcount);
   c->launches += 2;
@@ -934,8 +951,10 @@ void ps_sg_free_ctx(ps_ctx *c)
 {
   cudaFree(c->sg_queue);
   cudaFree(c->sg_qcount);
+  cudaFree(c->sg_items);
   c->sg_queue = nullptr;
   c->sg_qcount = nullptr;
+  c->sg_items = nullptr;
 }
 
 extern "C" int ps_sg_collect(ps_ctx *c, double *tuples, long cap, long *n)

@@ -187,52 +187,110 @@ __device__ __forceinline__ bool sg_forward(unsigned char *smem, uint32_t tmem, u
   return true;
 }
 
-// Features of a tuple; false when it lies outside the training box.
+// Features of a tuple (FP32 logarithms: the network sees them as bf16);
+// false when the tuple lies outside the training box.
 __device__ __forceinline__ bool sg_features(const SgBox &bx, double nH, double T, double xi,
                                             double dt, float (&x)[4])
 {
-  const double l[4] = {log10(nH), log10(T), log10(xi), log10(dt)};
+  const float l[4] = {log10f((float)nH), log10f((float)T), log10f((float)xi), log10f((float)dt)};
   bool in = true;
 #pragma unroll
   for (int i = 0; i < 4; i++) {
-    in = in && (l[i] >= bx.lo[i]) && (l[i] <= bx.hi[i]);
-    x[i] = (float)((l[i] - bx.lo[i]) * bx.scale[i] - 1.0);
+    in = in && (l[i] >= (float)bx.lo[i]) && (l[i] <= (float)bx.hi[i]);
+    x[i] = (l[i] - (float)bx.lo[i]) * (float)bx.scale[i] - 1.0f;
   }
   return in;
 }
 
-// z(T) of BLONDIN's energy equation and dz/dT.
-__device__ __forceinline__ double sg_z(const BlCtx &b, double T, double &dz, double &hc)
+// One cell's BLONDIN quantities for the learned step: n_H, n, thermal
+// energy E, xi with sqrt(xi)^-1 and xi^1/4, T_x, dt [s] and the net rate at
+// the old temperature.
+struct SgCtx {
+  double nH, n, E, xi, isqxi, sqsqxi, tx, dt, hc_init;
+};
+
+// heatcool (Src/Cooling/BLONDIN/cooling.c:173-222, prefactors 1) and its
+// T-derivative, term by term:
+//   ne = nH r(T), r = 1e-2 + 10^(a + b log10 T) -> r' = b 10^(a + b log10 T) / T
+//   (the middle branch without the 1e-2), 0 above 3.3e4 K;
+//   comp_cool' = 8.9e-36 xi 4; xray' = -xray / (2T);
+//   line term 1e-16 e^(-1.3e5/T) / (sqrt(xi) T): ' = term (1.3e5/T - 1) / T;
+//   the min() term: 0, 2.5e-27/sqrt(T) or -1.5e-17/T^2 by the active branch;
+//   brem' = brem / (2T).
+__device__ __forceinline__ double sg_heatcool_d(const SgCtx &b, double T, double &dhc)
 {
-  double dhc;
-  hc = bl_heatcool_d(b, T, dhc);
-  dz = b.n * kKB / (2.0 / 3.0) - b.dt_share * dhc / 2.0;
-  return (T * b.n * kKB / (2.0 / 3.0)) - b.E - b.dt_share * (b.hc_init + hc) / 2.0;
+  const double iT = 1.0 / T, sqT = sqrt(T);
+  double r, dr;
+  if (T < 1.5e4) {
+    const double q = exp(2.302585092994046 * (-51.59417133) + 12.27740153 * log(T));
+    r = 1e-2 + q;
+    dr = 12.27740153 * q * iT;
+  } else if (T < 3.3e4) {
+    const double q = exp(2.302585092994046 * (-3.80749689) + 0.86092628 * log(T));
+    r = q;
+    dr = 0.86092628 * q * iT;
+  } else {
+    r = 1.21;
+    dr = 0.0;
+  }
+  const double ne = b.nH * r, dne = b.nH * dr;
+  const double comp_heat = 8.9e-36 * b.xi * b.tx;
+  const double comp_cool = 8.9e-36 * b.xi * (4.0 * T), dcomp_cool = 8.9e-36 * b.xi * 4.0;
+  const double xray_heat = 1.5e-21 * b.sqsqxi * sqT * iT, dxray_heat = -0.5 * xray_heat * iT;
+  const double l1 = 1e-16 * exp(-1.3e5 * iT) * b.isqxi * iT;
+  const double dl1 = l1 * (1.3e5 * iT - 1.0) * iT;
+  const double m1 = 5e-27 * sqT, m2 = 1.5e-17 * iT;
+  double l2, dl2;
+  if (1e-24 <= m1 && 1e-24 <= m2) {
+    l2 = 1e-24;
+    dl2 = 0.0;
+  } else if (m1 <= m2) {
+    l2 = m1;
+    dl2 = 0.5 * m1 * iT;
+  } else {
+    l2 = m2;
+    dl2 = -m2 * iT;
+  }
+  const double brem_cool = 3.3e-27 * sqT, dbrem_cool = 0.5 * brem_cool * iT;
+  const double net = comp_heat - comp_cool - (l1 + l2) - brem_cool;
+  const double dnet = -dcomp_cool - (dl1 + dl2) - dbrem_cool;
+  dhc = b.nH * (dne * net + ne * dnet + b.nH * dxray_heat);
+  return b.nH * (ne * net + b.nH * xray_heat);
 }
 
-// The judge.  With E, n, xi, tx and dt_share set: the net rate and its
-// derivative at the old temperature T give z(T) = -dt hc(T) for free.  If
-// |z(T)| is already within kSgResidual of the thermal energy, one Newton
-// step from T is the answer (non-stiff cell: one rate evaluation in all).
-// Otherwise (stiff cell) damped Newton iterations (each step kept within a
-// factor 2) run until the residual is within kSgResidual, at most
-// kSgMaxNewton evaluations, starting from the network's prediction T0 when
-// it moves T by more than kSgJump (from T when from_net is false or the
-// predicted change is small); a final Newton step polishes the converged
-// point.  Rejected:
-// no convergence, z' <= 0, the net rate at the root of opposite sign to
-// the initial one (the reference then solves for the equilibrium
-// temperature instead), or a root on the wrong side of T.  Sets hc_init.
-__device__ __forceinline__ int sg_judge(BlCtx &b, double T, double T0, bool from_net, double &T_f,
+// z(T) = T n kB / (2/3) - E - dt (hc(T_old) + hc(T)) / 2 (cooling.c:233-237)
+// and dz/dT.
+__device__ __forceinline__ double sg_z(const SgCtx &b, double T, double &dz, double &hc)
+{
+  double dhc;
+  hc = sg_heatcool_d(b, T, dhc);
+  const double cth = b.n * kKB * 1.5;
+  dz = cth - b.dt * dhc * 0.5;
+  return T * cth - b.E - b.dt * (b.hc_init + hc) * 0.5;
+}
+
+// The judge.  The net rate and its derivative at the old temperature T give
+// z(T) = -dt hc(T).  If |z(T)| is already within kSgResidual of the
+// thermal energy, one Newton step from T is the answer (non-stiff cell: one
+// rate evaluation in all).  Otherwise (stiff cell) damped Newton iterations
+// (each step kept within a factor 2) run until the residual is within
+// kSgResidual, at most kSgMaxNewton evaluations, starting from the
+// network's prediction T0 when it moves T by more than kSgJump (from T when
+// from_net is false or the predicted change is small); a final Newton step
+// polishes the converged point.  Rejected: no convergence, z' <= 0, the net
+// rate at the root of opposite sign to the initial one (the reference then
+// solves for the equilibrium temperature instead), or a root on the wrong
+// side of T.  Sets hc_init.
+__device__ __forceinline__ int sg_judge(SgCtx &b, double T, double T0, bool from_net, double &T_f,
                                         int &evals, bool &stiff)
 {
-  const double cth = b.n * kKB / (2.0 / 3.0);
+  const double cth = b.n * kKB * 1.5;
   double dhc;
-  b.hc_init = bl_heatcool_d(b, T, dhc);
+  b.hc_init = sg_heatcool_d(b, T, dhc);
   evals = 1;
   double Tk = T, hc = b.hc_init;
-  double z = T * cth - b.E - b.dt_share * b.hc_init;
-  double dz = cth - b.dt_share * dhc / 2.0;
+  double z = T * cth - b.E - b.dt * b.hc_init;
+  double dz = cth - b.dt * dhc * 0.5;
   bool conv = fabs(z) <= kSgResidual * T * cth;
   stiff = !conv;
   if (!conv && from_net && T0 > 0.0 && isfinite(T0) && fabs(T0 - T) > kSgJump * T) {

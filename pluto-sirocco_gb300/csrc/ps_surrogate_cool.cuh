@@ -14,6 +14,12 @@ namespace ps {
 // 31 KB; asking for 48 KB keeps at most 4 CTAs (64 tensor-memory columns
 // each) on an SM, so tcgen05.alloc never has to wait.
 constexpr int kInfBytes = 48 * 1024;
+constexpr int kInfCtasPerSm = 4;
+
+// (model, block of cells) work item
+struct BlockItem {
+  int m, b;
+};
 
 // Tensor-memory allocation and the network in shared memory for a
 // 128-thread inference CTA; returns the tensor-memory address.
@@ -36,16 +42,18 @@ __device__ __forceinline__ void sg_inf_teardown(uint32_t tmem)
   if ((threadIdx.x >> 5) == 0) tmem_dealloc(tmem, 64);
 }
 
-// Prediction + judge for one prepared cell; status and (if accepted) T_f.
-__device__ __forceinline__ int sg_decide(BlCtx &b, double T, bool inbox, float y, int use_net,
+// Prediction + judge for one cell; status and (if accepted) T_f.  The
+// context needs nH, n, E, xi, tx and dt.
+__device__ __forceinline__ int sg_decide(SgCtx &b, double T, bool inbox, float y, int use_net,
                                          double &T_f, double &T0, int &evals, bool &stiff)
 {
   evals = 0;
   stiff = false;
   if (!inbox) return SG_OUT_OF_BOX;
-  b.sqxi = sqrt(b.xi);
-  b.sqsqxi = pow(b.xi, 0.25);
-  T0 = T * exp10(4.0 * (double)y);
+  const double sq = sqrt(b.xi);
+  b.isqxi = 1.0 / sq;
+  b.sqsqxi = sqrt(sq);
+  T0 = T * (double)exp10f(4.0f * y);
   return sg_judge(b, T, T0, use_net != 0, T_f, evals, stiff);
 }
 
@@ -79,47 +87,107 @@ struct SgCoolArgs {
   Scalars *sc;
 };
 
-// One 128-cell block of one grid: surrogate + judge; rejected cells are
-// queued (model, cell) for the reference method.
-__device__ __forceinline__ void sg_cool_block(const SgNet &net, const SgBox &bx, const SgCoolArgs &A,
-                                              int model, int blk, int use_net, unsigned char *smem,
-                                              int2 *queue, int *qcount, unsigned long long *stats)
+// Unit conversions of the learned step (the exact path's divisions by
+// constants folded into factors): E = p e_of_p, n_H = rho nh_of_rho,
+// n = rho n_of_rho, T = (p / rho) t_of_pr, p_new = T_new n p_of_tn
+// (p, rho in code units; cooling.c:95-162).
+struct SgUnits {
+  double e_of_p, nh_of_rho, n_of_rho, t_of_pr, p_of_tn;
+};
+
+__device__ __forceinline__ SgUnits sg_units(const SgCoolArgs &A)
 {
-  if (A.sc->done) return;  // uniform over the CTA
+  SgUnits u;
+  const double gm1 = A.p.gamma - 1.0;
+  u.e_of_p = A.w.unit_pressure / gm1;
+  u.nh_of_rho = A.w.unit_density / (1.43 * kMP);
+  u.n_of_rho = A.w.unit_density / (A.w.mu * kMP);
+  u.t_of_pr = u.e_of_p / (1.5 * u.n_of_rho * kKB);
+  u.p_of_tn = 1.5 * kKB * gm1 / A.w.unit_pressure;
+  return u;
+}
+
+// The cell's quantities for the learned step.  Returns 0 (below 1e4 K:
+// left alone, as the reference does), 1 (to solve) or 2 (within 1e-12 of
+// 1e4 K: the exact path decides).
+__device__ __forceinline__ int sg_cell_ctx(const SgCoolArgs &A, const SgUnits &u, double dt,
+                                           double t, int q, SgCtx &b, double &T, long long &c)
+{
+  const Params &p = A.p;
+  const int gi = q % p.nx[0] + p.beg[0], gj = q / p.nx[0] + p.beg[1];
+  c = vcell(p, gj, gi);
+  const double rho = A.V[RHO * p.vstride + c], pr = A.V[PRS * p.vstride + c];
+  T = pr / rho * u.t_of_pr;
+  if (T < 1.e4 * (1.0 - 1e-12)) return 0;
+  b.dt = dt * A.w.unit_time;
+  b.E = pr * u.e_of_p;
+  b.nH = rho * u.nh_of_rho;
+  b.n = rho * u.n_of_rho;
+  if (t <= 3.0) {
+    const double r = A.x1[gi] * A.w.unit_length;
+    b.xi = A.w.lx / (b.nH * r * r);
+    b.tx = A.w.t_x;
+  } else {
+    b.xi = A.xi[c];
+    b.tx = A.tr[c];
+  }
+  return T < 1.e4 * (1.0 + 1e-12) ? 2 : 1;
+}
+
+// One CTA over 128-cell blocks of grids: the network on the tensor cores,
+// the judge per cell; cells the judge rejects are queued (model, cell)
+// for the reference method.  `blocks` gives (model, block) per item;
+// args(m) the model's arguments.  Set-up (tensor memory, network in shared
+// memory) once per CTA.
+template <class ArgsOf>
+__device__ __forceinline__ void sg_cool_items(const SgNet &net, const SgBox &bx, ArgsOf args_of,
+                                              const BlockItem *blocks, int nitems, int use_net,
+                                              unsigned char *smem, int2 *queue, int *qcount,
+                                              unsigned long long *stats)
+{
   const uint32_t tmem = sg_inf_setup(net, smem);
-  const int ncell = A.p.nx[0] * A.p.nx[1];
-  const int q = blk * kSgRows + threadIdx.x;
-  const bool active = q < ncell;
-  const double dt = A.sc->dt, t = A.sc->t;
-  BlCtx b;
-  double T = 0.0;
-  long long c = 0;
-  float x[4] = {0.f, 0.f, 0.f, 0.f};
-  bool inbox = false, solve = false;
-  if (active) {
-    solve = blondin_ctx(A.V, A.xi, A.tr, A.p, A.w, A.x1, dt, t, q, b, T, c);
-    if (solve && b.tx == bx.t_x) {
-      inbox = sg_features(bx, b.nH, T, b.xi, b.dt_share, x);
-      if (!inbox) x[0] = x[1] = x[2] = x[3] = 0.f;
-    }
-  }
   uint32_t phase = 0;
-  float y = 0.f;
-  const bool ok = sg_forward(smem, tmem, phase, x, 0, 0, y);
-  if (!ok && threadIdx.x == 0) atomicOr(&A.sc->flags, F_TMA_TIMEOUT);
-  int st = SG_BELOW_MIN, evals = 0;
-  bool stiff = false;
-  if (solve) {
-    double T_f = 0.0, T0;
-    st = ok ? sg_decide(b, T, inbox, y, use_net, T_f, T0, evals, stiff) : SG_REJECT;
-    if (st == SG_ACCEPT) {
-      blondin_store(A.V, A.p, A.w, b, c, T_f);
-    } else {
-      const int k = atomicAdd(qcount, 1);
-      queue[k] = make_int2(model, q);
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const BlockItem bi = blocks[it];
+    const SgCoolArgs A = args_of(bi.m);
+    if (A.sc->done) continue;  // uniform over the CTA
+    const SgUnits u = sg_units(A);
+    const int ncell = A.p.nx[0] * A.p.nx[1];
+    const int q = bi.b * kSgRows + threadIdx.x;
+    const bool active = q < ncell;
+    const double dt = A.sc->dt, t = A.sc->t;
+    SgCtx b;
+    double T = 0.0;
+    long long c = 0;
+    float x[4] = {0.f, 0.f, 0.f, 0.f};
+    bool inbox = false;
+    int kind = 0;
+    if (active) {
+      kind = sg_cell_ctx(A, u, dt, t, q, b, T, c);
+      if (kind == 1 && b.tx == bx.t_x) {
+        inbox = sg_features(bx, b.nH, T, b.xi, b.dt, x);
+        if (!inbox) x[0] = x[1] = x[2] = x[3] = 0.f;
+      }
     }
+    float y = 0.f;
+    const bool ok = sg_forward(smem, tmem, phase, x, 0, 0, y);
+    if (!ok && threadIdx.x == 0) atomicOr(&A.sc->flags, F_TMA_TIMEOUT);
+    int st = SG_BELOW_MIN, evals = 0;
+    bool stiff = false;
+    if (kind) {
+      double T_f = 0.0, T0;
+      st = (ok && kind == 1) ? sg_decide(b, T, inbox, y, use_net, T_f, T0, evals, stiff)
+                             : SG_REJECT;
+      if (st == SG_ACCEPT) {
+        A.V[PRS * A.p.vstride + c] = dmax(T_f, 1.e4) * b.n * u.p_of_tn;
+      } else {
+        const int k = atomicAdd(qcount, 1);
+        queue[k] = make_int2(bi.m, q);
+      }
+    }
+    sg_count(st, active, evals, stiff, stats);
+    if (!ok) break;
   }
-  sg_count(st, active, evals, stiff, stats);
   sg_inf_teardown(tmem);
 }
 
