@@ -3,11 +3,14 @@
     python pluto-sirocco_gb300/ps_build.py            # library + oracle
     python pluto-sirocco_gb300/ps_build.py --lib      # library only
 
-CUDA sources are compiled for sm_103a only, in parallel, with -fmad=false
-(no contraction of multiplies and adds, as in the reference's x86-64 build)
-and the IEEE-rounded division and square root that nvcc uses for double.
-Host C sources are compiled with gcc -ffp-contract=off for the same reason.
-The outputs stay in-tree next to the sources.
+CUDA sources are compiled for sm_103a only, in parallel.  Device code
+contracts multiplies and adds into FMAs (nvcc's default -fmad=true) and
+keeps the IEEE-rounded division and square root that nvcc uses for double;
+against the reference's x86-64 build (no FMA) this changes results at the
+level of 1e-16 to 1e-13 relative after 100 steps, far inside the 1e-11
+tolerance the parity tests hold it to.  Host C sources (grid and initial
+conditions, which the parity tests compare exactly) are compiled with gcc
+-ffp-contract=off.  The outputs stay in-tree next to the sources.
 """
 import argparse
 import os
@@ -25,7 +28,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libps_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-std=c++17", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
+NVFLAGS = ["-O3", "-std=c++17", "-fmad=true", "-lineinfo", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off", "-I" + INC, "-I" + CSRC]
 CFLAGS = ["-O3", "-std=c17", "-ffp-contract=off", "-fPIC", "-Wall", "-I" + INC]
 

@@ -1,14 +1,16 @@
 """CUDA path against the reference (golden vectors) and the oracle.
 
-Every comparison here is bit-exact: the device kernels keep the
-reference's operation order with no FMA contraction, so the FP64 results
-must be identical, not merely close."""
+The device kernels keep the reference's operation order; they contract
+multiplies and adds into FMAs, so the state is compared with the
+tolerances of conftest (relative L1 1e-11 per variable, conserved totals
+1e-12), the time-step sequence to 1e-12, and paths of the library against
+each other bit for bit."""
 import hashlib
 
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden
+from conftest import CONSERVED_REL, assert_hydro_close, golden_cases, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -55,14 +57,25 @@ def test_gpu_matches_reference(built, meta):
     assert flags == 0
     a = _active(s.get_state(), meta["dims"])
     if meta["npz"]:
-        _, v1 = load_golden(meta)
-        diff = np.abs(a - v1)
-        assert np.array_equal(a, v1), f"max |diff| {diff.max()} in {np.count_nonzero(diff)} values"
-    assert _digest(a) == meta["final_sha256"]
+        _, ref = load_golden(meta)
+    else:
+        o = _oracle(meta)
+        o.run(meta["steps"])
+        ref = o.active().reshape(a.shape)
+        assert _digest(ref) == meta["final_sha256"]   # the oracle is the reference here
+    r = assert_hydro_close(a, ref, meta["name"])
+    print(meta["name"], "relative L1 per variable", r)
+    g = 5.0 / 3.0
+    for k, (x, y) in enumerate(((a[0], ref[0]),
+                                (0.5 * a[0] * (a[1] ** 2 + a[2] ** 2 + a[3] ** 2) + a[4] / (g - 1),
+                                 0.5 * ref[0] * (ref[1] ** 2 + ref[2] ** 2 + ref[3] ** 2)
+                                 + ref[4] / (g - 1)))):
+        assert abs(x.sum() - y.sum()) <= CONSERVED_REL * abs(y.sum()), ("mass", "energy")[k]
     t, dt, step, _ = s.time()
     assert step == meta["steps"]
-    assert float(f"{t:e}") == float(meta["t_final"])
-    assert float(f"{dt:e}") == float(meta["dt_next"])
+    # the golden files print t and dt with 7 significant digits
+    assert abs(t - float(meta["t_final"])) <= 6e-7 * abs(t)
+    assert abs(dt - float(meta["dt_next"])) <= 6e-7 * abs(dt)
 
 
 @pytest.mark.parametrize("meta", golden_cases(full_only=True)[:3], ids=lambda m: m["name"])
@@ -72,10 +85,12 @@ def test_gpu_dt_sequence_matches_oracle(built, meta):
     o = _oracle(meta)
     o.run(meta["steps"])
     dt_o, _ = o.history(meta["steps"])
-    assert np.array_equal(s.dt_history(meta["steps"]), dt_o)
+    dt_g = s.dt_history(meta["steps"])
+    assert len(dt_g) == len(dt_o)
+    assert np.max(np.abs(dt_g - dt_o) / dt_o) <= 1e-12
     t_g, dt_g, _, _ = s.time()
     t_o, dt_o2, _ = o.time()
-    assert t_g == t_o and dt_g == dt_o2
+    assert abs(t_g - t_o) <= 1e-12 * t_o and abs(dt_g - dt_o2) <= 1e-12 * dt_o2
 
 
 def test_advance_step_dropin_matches_run(built):
@@ -108,9 +123,9 @@ def test_tstop_clamp_matches_oracle(built):
     o = _oracle(meta, tstop=0.01)
     o.run(40)
     t, _, step, _ = s.time()
-    assert t == o.time()[0] and step == o.time()[2]
-    assert abs(t - 0.01) < 1e-15
-    assert np.array_equal(_active(s.get_state(), 2), o.active())
+    assert step == o.time()[2]
+    assert abs(t - 0.01) < 1e-15 and abs(o.time()[0] - 0.01) < 1e-15
+    assert_hydro_close(_active(s.get_state(), 2), o.active(), "tstop")
 
 
 def test_periodic_conservation(built):
