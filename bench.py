@@ -1,7 +1,7 @@
 """Benchmark of the GB300 hydro path: cell-updates per second, FP64.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
-                    [--workload batch|wind|blast]
+                    [--workload batch|wind|blast|cube]
 
 Workloads (synthetic inputs of the reference's configurations):
   batch  Default.  64 independent line-driven disk-wind models (grids drawn
@@ -20,6 +20,9 @@ Workloads (synthetic inputs of the reference's configurations):
          UV flux, PLM van Leer, HLL, RK2, CFL 0.4; 1000 steps, plain form.
   blast  2-D Cartesian ideal-gas blast wave, 256 x 256, PLM MC, HLLC, RK2,
          CFL 0.4, outflow, seeded 1% density noise; 100 steps.
+  cube   3-D Cartesian periodic 512^3 with BLONDIN at xi = 1e2: log-normal
+         density (sigma 0.5, k^-2 spectrum, seed 5), T log-uniform 1e4..1e7 K;
+         50 steps, plain (bracket + Brent) against the learned cooling step.
 One benchmark step is one time step of every grid (split source +
 AdvanceStep + NextTimeStep); the default K is the configured run length,
 restarted from the initial condition after the warm-up.
@@ -81,6 +84,17 @@ class Workload:
                          "1e36..1e38 erg/s, k U(0.1,0.4), alpha U(0.5,0.7); seed 4), each as "
                          "the wind2d workload, all advanced together")
             self.profile = "stage_kernel_wind_512x256.md"
+        elif name == "cube":
+            self.nx = self.ny = self.nz = 512
+            self.nvar = 5
+            self.steps = 50
+            self.cpu_steps = 4
+            self.cpu_n = 48
+            self.desc = ("cube3d-512: 3-D Cartesian periodic HD on [0,1]^3, PLM-MC, HLLC, RK2, "
+                         "CFL 0.4, gamma 5/3, log-normal density (sigma 0.5, P(k) ~ k^-2, seed 5),"
+                         " T log-uniform 1e4..1e7 K per cell, BLONDIN at xi = 1e2 (Strang split),"
+                         " code density 1 = 1e-10 g/cm^3")
+            self.profile = "stage_kernel_cube3d_512.md"
         else:
             self.nx, self.ny, self.nvar = 256, 256, 5
             self.steps = 100
@@ -90,9 +104,11 @@ class Workload:
             self.profile = "stage_kernel_blast2d_256.md"
         if name == "batch":
             self.cells = sum(sp["grid"][0] * sp["grid"][1] for sp in self.specs)
+        elif name == "cube":
+            self.cells = self.nx * self.ny * self.nz
         else:
             self.cells = self.nx * self.ny
-        self.cooling = name in ("wind", "batch")
+        self.cooling = name in ("wind", "batch", "cube")
 
     def solver(self):
         """Device context with the initial state loaded."""
@@ -143,6 +159,19 @@ def _cpu_worker(args):
         o = wind_oracle(sp["grid"][0], sp["grid"][1], l_star=sp["l_star"], krad=sp["krad"],
                         alpharad=sp["alpharad"])
         cells = sp["grid"][0] * sp["grid"][1]
+    elif name == "cube":
+        import psgb
+        from oracle import Oracle
+        n = wl.cpu_n
+        cp = psgb.COOL_PARAMS
+        cfg = psgb.cube_config(n)
+        o = Oracle(dims=3, nx=(n, n, n), nvar=5, limiter="mc", solver="hllc", bc="periodic",
+                   cfl=0.4, cfl_max_var=1.1, tstop=1e10, first_dt=cfg.first_dt, cooling=1,
+                   params=dict(unit_density=cp["unit_density"], unit_length=cp["unit_length"],
+                               unit_velocity=cp["unit_velocity"], mu=cp["mu"], t_x=cp["t_x"],
+                               xi_const=cp["xi"]))
+        o.V[...] = psgb.cube_state(cfg, psgb.Grid(cfg), seed=5 + idx)
+        cells = n ** 3
     else:
         o = wl.oracle()
         cells = wl.cells
@@ -167,7 +196,8 @@ def cpu_throughput(wl, steps, procs=None):
     cells = sum(r[1] for r in res)
     slowest = max(per)
     what = (f"models 0..{n - 1} of the batch" if wl.name == "batch"
-            else wl.desc.split(':')[0])
+            else f"{wl.cpu_n}^3 cubes of the same configuration (one seed per core)"
+            if wl.name == "cube" else wl.desc.split(':')[0])
     return {"value": cells / slowest, "unit": "cell-updates/s", "cores": n, "kind": "port",
             "wall_s": slowest,
             "sample": f"{n} concurrent independent runs of the first {steps} steps of "
@@ -561,6 +591,136 @@ def batch_bench(wl, steps, warmup, rank, world):
         dist.destroy_process_group()
 
 
+def cube_bench(wl, steps, warmup, rank, world):
+    """The 3-D periodic cooling configuration at 512^3: the plain GPU form
+    (BLONDIN by bracket + Brent) and the form with the learned cooling step
+    (the headline value), both from the same initial state."""
+    import numpy as np
+    import torch
+    import psgb
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    t_setup = time.perf_counter()
+    s = psgb.cube_solver(wl.nx)
+    s.set_stream(stream.cuda_stream)
+    s.save()
+    t_setup = time.perf_counter() - t_setup
+
+    def timed():
+        for _ in range(warmup):
+            flush.zero_()
+            s.run(1)
+        torch.cuda.synchronize()
+        s.restore()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            torch.cuda.synchronize()
+            for a, b in ev:
+                flush.zero_()
+                a.record(stream)
+                s.run(1)
+                b.record(stream)
+            torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        if dist:
+            tt = torch.tensor([ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+            dist.barrier()
+        return ms, clk.summary()
+
+    rate = lambda ms: wl.cells * steps * world / (ms * 1e-3)
+    ms_plain, _ = timed()
+    flags_plain = s.sync()
+    # training tuples: cells of the plain run after 10 steps, plus draws
+    s.restore()
+    s.run(10)
+    rng = np.random.default_rng(3)
+    tup = psgb.sg_collect(s, cap=1 << 22)
+    tup = tup[rng.choice(len(tup), size=min(300000, len(tup)), replace=False)]
+    t_train = time.perf_counter()
+    sg, hist, all_tup, _ = psgb.train_surrogate(tup, n_draws=700000, steps=40000, seed=3)
+    t_train = time.perf_counter() - t_train
+    psgb.lib().ps_set_surrogate(s.ctx, sg.h, 1)
+    sg.stats(reset=True)
+    launches0 = s.launches()
+    ms, clocks = timed()
+    launches = s.launches() - launches0
+    flags = s.sync()
+    counters = dict(zip(["accepted", "out_of_box", "rejected", "below_1e4K", "rate_evaluations",
+                         "stiff"], sg.stats(reset=True)))
+    # the learned step's temperature error on a sample of the final state
+    tup_end = psgb.sg_collect(s, cap=1 << 21)
+    ref = sg.label(tup_end)
+    out, st, _ = sg.predict(tup_end, use_net=1)
+    rel = np.abs(out - ref) / ref
+    value = rate(ms)
+
+    s.restore()
+    per_kernel = np.zeros(3)
+    reps = 4
+    for _ in range(reps):
+        per_kernel += s.time_step_kernels()
+    per_kernel /= reps
+    stage_ms = 0.5 * (per_kernel[0] + per_kernel[1])
+
+    e2e_steps = min(steps, 4)
+    s.restore()
+    V0 = s.get_state()
+    host = torch.from_numpy(V0).pin_memory().numpy()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.set_state(host)
+        s.run(1)
+        s.get_state(out=host)
+    e2e_wall = time.perf_counter() - t0
+    out_json = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (the configuration's seeded initial condition, generated on the host)",
+        "config": {"workload": wl.desc, "cells": wl.cells, "grid": [wl.nx, wl.ny, wl.nz],
+                   "method": "learned cooling step (ps_set_surrogate), CUDA-graph steps",
+                   "plain_value": rate(ms_plain), "plain_ms_per_step": ms_plain / steps,
+                   "speedup_vs_plain": ms_plain / ms, "plain_flags": int(flags_plain),
+                   "cooling_T_error": {"cells_sampled": int(len(tup_end)),
+                                       "max_rel_T_error": float(rel.max()),
+                                       "accepted": float(np.mean(st == 0))},
+                   "surrogate_run_counters": counters,
+                   "surrogate_training": {"samples": int(len(all_tup)), "cube_samples": int(len(tup)),
+                                          "seconds": t_train,
+                                          "final_loss": float(hist[-100:].mean())},
+                   "setup_s": t_setup,
+                   "l2": "inputs (5.5 GB per array) far larger than L2; 256 MiB flush as well",
+                   "parallelism": "replicas only" if world > 1 else "single GPU"},
+        "e2e": {"value": wl.cells * e2e_steps / e2e_wall, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": int(V0.nbytes), "d2h_bytes_per_step": int(V0.nbytes),
+                "steps": e2e_steps,
+                "path": "per step: H2D Data.Vc, ps_run(1) with the learned cooling step, D2H "
+                        "Data.Vc (pinned host memory)"},
+        "gpu_launches": int(launches),
+        "device_flags": int(flags),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        _rooflines(out_json, wl, stage_ms, per_kernel)
+        if world == 1:
+            out_json["cpu_baseline"] = cpu_throughput(wl, wl.cpu_steps)
+        print(json.dumps(out_json), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def _rooflines(out, wl, stage_ms, per_kernel):
     import psgb
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
@@ -601,8 +761,9 @@ def reference_bench(wl, steps, warmup, rank, world):
            "ms_per_step": base["wall_s"] / per_core * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (the reference configuration's initial condition, generated)",
-           "config": {"workload": wl.desc, "cells": wl.cells, "grid": [wl.nx, wl.ny]}
-           if wl.nx else {"workload": wl.desc, "cells": wl.cells, "models": len(wl.specs)},
+           "config": ({"workload": wl.desc, "cells": wl.cells, "models": len(wl.specs)}
+                      if wl.name == "batch" else
+                      {"workload": wl.desc, "cells": wl.cells, "grid": [wl.nx, wl.ny]}),
            "impl": "reference",
            "cpu_baseline": base,
            "e2e": {"value": base["value"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
@@ -616,7 +777,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["wind", "blast", "batch"])
+    ap.add_argument("--workload", default="batch", choices=["wind", "blast", "batch", "cube"])
     a = ap.parse_args()
     wl = Workload(a.workload)
     steps = a.steps if a.steps is not None else wl.steps
@@ -625,6 +786,8 @@ def main():
         reference_bench(wl, steps, a.warmup, rank, world)
     elif a.workload == "batch":
         batch_bench(wl, steps, max(a.warmup, 3), rank, world)
+    elif a.workload == "cube":
+        cube_bench(wl, steps, max(a.warmup, 3), rank, world)
     else:
         gpu_bench(wl, steps, max(a.warmup, 3), rank, world)
 

@@ -215,6 +215,21 @@ int ps_get_dt_history(ps_ctx *ctx, double *out, int max);
  * counterpart: lets a host framework order the path with its own work. */
 int ps_set_stream(ps_ctx *ctx, void *stream);
 
+/* Operator-split BLONDIN heating/cooling on a Cartesian context (created
+ * with cooling = 1) at a constant ionisation parameter: SplitSource with
+ * BlondinCooling (Src/split_source.c:28-79,
+ * Src/Cooling/BLONDIN/cooling.c:50-165, prefactors 1) with xi and T_x
+ * fixed instead of read from sirocco_xi / sirocco_t_r.  ps_run then
+ * alternates the source around the hydro step in PLUTO's Strang order,
+ * and ps_split_source() runs it alone. */
+typedef struct ps_cooling {
+  double unit_density, unit_length, unit_velocity;  /* UNIT_* of definitions.h */
+  double mu;      /* MU: mean molecular weight                           */
+  double t_x;     /* T_x: X-ray (Compton) temperature [K]                */
+  double xi;      /* ionisation parameter L_x / (n_H r^2), constant       */
+} ps_cooling;
+int ps_set_cooling(ps_ctx *ctx, const ps_cooling *c);
+
 /* ---------------------------------------------------------------- */
 /* batches of independent wind models                                */
 /* ---------------------------------------------------------------- */

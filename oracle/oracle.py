@@ -34,7 +34,7 @@ class OrConfig(ctypes.Structure):
                 ("t_iso", ctypes.c_double), ("l_star", ctypes.c_double),
                 ("f_x", ctypes.c_double), ("f_uv", ctypes.c_double), ("t_x", ctypes.c_double),
                 ("krad", ctypes.c_double), ("alpharad", ctypes.c_double),
-                ("dfloor", ctypes.c_double)]
+                ("dfloor", ctypes.c_double), ("xi_const", ctypes.c_double)]
 
 
 _lib = None

@@ -1280,7 +1280,10 @@ void or_cooling(or_sim *s, double dt, double t)
     (void)T;
     b.E = (p * UNIT_P(s)) / (s->c.gamma - 1);
     b.nH = rho / (1.43 * C_MP);
-    if (t <= 3.0) {
+    if (s->c.xi_const > 0.0) {
+      b.xi = s->c.xi_const;
+      b.tx = s->c.t_x;
+    } else if (t <= 3.0) {
       b.xi = lx / b.nH / r / r;
       b.tx = s->c.t_x;
     } else {

@@ -50,6 +50,9 @@ typedef struct {
   double unit_density, unit_length, unit_velocity;
   double mu, rho_0, cent_mass, t_iso, l_star, f_x, f_uv, t_x;
   double krad, alpharad, dfloor;
+  /* > 0: BLONDIN at this constant ionisation parameter with t_x (the
+   * Cartesian cooling configuration) instead of xi from the state */
+  double xi_const;
 } or_config;
 
 typedef struct or_sim or_sim;

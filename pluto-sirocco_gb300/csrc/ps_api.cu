@@ -531,15 +531,33 @@ static int build_graph(ps_ctx *c, int nsteps, cudaGraphExec_t *out)
 
 static int finish_step(ps_ctx *c, int) { return launch_finish(c, ps::MODE_STEP); }
 
-// CUDA graphs of the wind step: [0] even step, [1] odd step, [2] even+odd
+int ps_cart_cool_launch(ps_ctx *c);
+
+// One step with the operator-split source: the source before (odd steps)
+// or after (even steps) AdvanceStep (Src/main.c:479-485), then the dt
+// kernel.  Wind or Cartesian cooling context.
+static int split_step_launches(ps_ctx *c, int odd)
+{
+  if (c->wind) return ps_wind_step_launches(c, odd, finish_step);
+  int r = 0;
+  if (odd) r = ps_cart_cool_launch(c);
+  if (!r) CK(launch_stage(c, 1));
+  if (!r) CK(launch_stage(c, 2));
+  if (!r && !odd) r = ps_cart_cool_launch(c);
+  if (!r) r = launch_finish(c, ps::MODE_STEP);
+  return r;
+}
+
+// CUDA graphs of a step with the split source: [0] even step, [1] odd
+// step, [2] even+odd
 static int build_wind_graph(ps_ctx *c, int kind, cudaGraphExec_t *out)
 {
   cudaGraph_t g;
   long before = c->launches;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int r = 0;
-  if (kind == 0 || kind == 2) r = ps_wind_step_launches(c, 0, finish_step);
-  if (!r && (kind == 1 || kind == 2)) r = ps_wind_step_launches(c, 1, finish_step);
+  if (kind == 0 || kind == 2) r = split_step_launches(c, 0);
+  if (!r && (kind == 1 || kind == 2)) r = split_step_launches(c, 1);
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->launches = before;
   if (r) return r;
@@ -552,7 +570,8 @@ static int build_wind_graph(ps_ctx *c, int kind, cudaGraphExec_t *out)
 
 static int run_wind(ps_ctx *c, int nsteps)
 {
-  long per_step = 7 + (c->p.cooling ? 1 : 0);
+  const int ncool = c->p.cooling ? (c->sg ? 2 : 1) + (c->wind ? 0 : 1) : 0;
+  const long per_step = (c->wind ? 7 : 3) + ncool;
   for (int k = 0; k < 3; k++)
     if (!c->gw[k]) {
       int r = build_wind_graph(c, k, &c->gw[k]);
@@ -589,6 +608,7 @@ extern "C" int ps_run(ps_ctx *c, int nsteps)
     }
     return run_wind(c, nsteps);
   }
+  if (c->cool_on && c->p.cooling) return run_wind(c, nsteps);
   const int G = 16;
   if (!c->g1) {
     r = build_graph(c, 1, &c->g1);
@@ -710,19 +730,27 @@ extern "C" int ps_time_step_kernels(ps_ctx *c, double *ms)
     ms[1] = t[3];
     ms[2] = t[0] + t[2] + t[4];
   } else {
+    // Cartesian: ms[0], ms[1] the stage kernels, ms[2] the dt kernel and
+    // (with the split source) the cooling step
+    const bool cool = c->cool_on && c->p.cooling;
+    const int odd = (int)(c->host_step & 1);
     CK(cudaEventRecord(ev[0], c->stream));
-    CK(launch_stage(c, 1));
+    if (cool && odd) r = ps_cart_cool_launch(c);
     CK(cudaEventRecord(ev[1], c->stream));
-    CK(launch_stage(c, 2));
+    CK(launch_stage(c, 1));
     CK(cudaEventRecord(ev[2], c->stream));
-    launch_finish(c, ps::MODE_STEP);
+    CK(launch_stage(c, 2));
     CK(cudaEventRecord(ev[3], c->stream));
-    CK(cudaEventSynchronize(ev[3]));
-    for (int i = 0; i < 3; i++) {
-      float t = 0.f;
-      CK(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
-      ms[i] = t;
-    }
+    if (!r && cool && !odd) r = ps_cart_cool_launch(c);
+    launch_finish(c, ps::MODE_STEP);
+    CK(cudaEventRecord(ev[4], c->stream));
+    CK(cudaEventSynchronize(ev[4]));
+    if (cool) c->host_step++;
+    float t[4];
+    for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&t[i], ev[i], ev[i + 1]));
+    ms[0] = t[1];
+    ms[1] = t[2];
+    ms[2] = t[0] + t[3];
   }
   for (int i = 0; i < 8; i++) cudaEventDestroy(ev[i]);
   return r;
@@ -733,7 +761,7 @@ extern "C" int ps_split_source(ps_ctx *c, double dt, double t)
 {
   int r = check_ready(c, "ps_split_source");
   if (r) return r;
-  if (!c->wind || !c->p.cooling) return 0;
+  if (!c->p.cooling || !(c->wind || c->cool_on)) return 0;
   ps::Scalars s;
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
@@ -741,7 +769,7 @@ extern "C" int ps_split_source(ps_ctx *c, double dt, double t)
   s.t = t;
   s.done = 0;
   CK(cudaMemcpy(c->sc, &s, sizeof(s), cudaMemcpyHostToDevice));
-  r = ps_wind_cool_launch(c);
+  r = c->wind ? ps_wind_cool_launch(c) : ps_cart_cool_launch(c);
   if (r) return r;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->stream));

@@ -4,6 +4,7 @@
 
 #include "ps_gb300.h"
 #include "ps_hydro.cuh"
+#include "ps_wind.cuh"
 
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -37,6 +38,8 @@ struct ps_ctx {
   long long host_step;      // host mirror of g_stepNumber (wind graph parity)
   long long host_step_save; // host_step at ps_save_state
   ps::WindDev *wind;        // line-driven wind terms (NULL for plain hydro)
+  int cool_on;              // Cartesian BLONDIN at constant xi (ps_set_cooling)
+  ps::WindParams coolw;     // its units and parameters
   struct ps_surrogate *sg;  // learned cooling step (NULL: reference BLONDIN)
   int sg_use_net;           // 0: Newton from the old temperature (no network)
   void *sg_queue;           // cells left to the reference method (int2 each)

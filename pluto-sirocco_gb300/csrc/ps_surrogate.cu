@@ -449,9 +449,10 @@ __global__ void k_sg_cool_fallback(SgCoolArgs A, const int2 *__restrict__ queue,
 // (n_H, T, xi, dt_s) of every cell BLONDIN would solve now.
 __global__ void k_sg_collect(SgCoolArgs A, double *__restrict__ out, long cap, int *count)
 {
-  const int ncell = A.p.nx[0] * A.p.nx[1];
+  const long long ncell = (long long)A.p.nx[0] * A.p.nx[1] * A.p.nx[2];
   const double dt = A.sc->dt, t = A.sc->t;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ncell; q += gridDim.x * blockDim.x) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < ncell;
+       q += (long long)gridDim.x * blockDim.x) {
     BlCtx b;
     double T;
     long long c;
@@ -893,13 +894,23 @@ static ps::SgCoolArgs sg_cool_args(ps_ctx *c)
 {
   ps::SgCoolArgs A;
   A.V = c->V;
-  A.xi = c->wind->xi;
-  A.tr = c->wind->tr;
-  A.x1 = c->wind->a.g.x1;
   A.p = c->p;
-  A.w = c->wind->a.w;
   A.sc = c->sc;
+  if (c->wind) {
+    A.xi = c->wind->xi;
+    A.tr = c->wind->tr;
+    A.x1 = c->wind->a.g.x1;
+    A.w = c->wind->a.w;
+  } else {  // Cartesian cooling at constant xi
+    A.xi = A.tr = A.x1 = nullptr;
+    A.w = c->coolw;
+  }
   return A;
+}
+
+static long long ctx_cells(const ps_ctx *c)
+{
+  return (long long)c->p.nx[0] * c->p.nx[1] * c->p.nx[2];
 }
 
 void ps_ctx_invalidate_graphs(ps_ctx *c);
@@ -907,11 +918,12 @@ void ps_ctx_invalidate_graphs(ps_ctx *c);
 extern "C" int ps_set_surrogate(ps_ctx *c, ps_surrogate *s, int use_net)
 {
   if (!c) return sg_fail("ps_set_surrogate: null context");
-  if (s && !c->wind) return sg_fail("ps_set_surrogate: needs ps_set_wind first");
+  if (s && !c->wind && !c->cool_on)
+    return sg_fail("ps_set_surrogate: needs ps_set_wind or ps_set_cooling first");
   SCK(cudaStreamSynchronize(c->stream));
   if (s) SCK(cudaStreamSynchronize(s->stream));
   if (s && !c->sg_queue) {
-    const size_t ncell = (size_t)c->p.nx[0] * c->p.nx[1];
+    const size_t ncell = (size_t)ctx_cells(c);
     const int nblk = (int)((ncell + ps::kSgRows - 1) / ps::kSgRows);
     std::vector<ps::BlockItem> items(nblk);
     for (int k = 0; k < nblk; k++) items[k] = ps::BlockItem{0, k};
@@ -931,9 +943,9 @@ int ps_sg_cool_launch(ps_ctx *c)
 {
   ps_surrogate *s = c->sg;
   const ps::SgCoolArgs A = sg_cool_args(c);
-  const int ncell = c->p.nx[0] * c->p.nx[1];
+  const long long ncell = ctx_cells(c);
   SCK(cudaMemsetAsync(c->sg_qcount, 0, sizeof(int), c->stream));
-  const int nblk = (ncell + ps::kSgRows - 1) / ps::kSgRows;
+  const int nblk = (int)((ncell + ps::kSgRows - 1) / ps::kSgRows);
   int dev = 0, nsm = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -959,7 +971,8 @@ void ps_sg_free_ctx(ps_ctx *c)
 
 extern "C" int ps_sg_collect(ps_ctx *c, double *tuples, long cap, long *n)
 {
-  if (!c || !c->wind || !tuples || !n || cap <= 0) return sg_fail("ps_sg_collect: bad arguments");
+  if (!c || !(c->wind || c->cool_on) || !tuples || !n || cap <= 0)
+    return sg_fail("ps_sg_collect: bad arguments");
   SCK(cudaStreamSynchronize(c->stream));
   double *d = nullptr;
   int *cnt = nullptr;

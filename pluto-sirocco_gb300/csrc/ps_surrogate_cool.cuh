@@ -111,11 +111,12 @@ __device__ __forceinline__ SgUnits sg_units(const SgCoolArgs &A)
 // left alone, as the reference does), 1 (to solve) or 2 (within 1e-12 of
 // 1e4 K: the exact path decides).
 __device__ __forceinline__ int sg_cell_ctx(const SgCoolArgs &A, const SgUnits &u, double dt,
-                                           double t, int q, SgCtx &b, double &T, long long &c)
+                                           double t, long long q, SgCtx &b, double &T, long long &c)
 {
   const Params &p = A.p;
-  const int gi = q % p.nx[0] + p.beg[0], gj = q / p.nx[0] + p.beg[1];
-  c = vcell(p, gj, gi);
+  int gi, gj, gk;
+  cell_of(p, q, gi, gj, gk);
+  c = vcell3(p, gk, gj, gi);
   const double rho = A.V[RHO * p.vstride + c], pr = A.V[PRS * p.vstride + c];
   T = pr / rho * u.t_of_pr;
   if (T < 1.e4 * (1.0 - 1e-12)) return 0;
@@ -123,7 +124,10 @@ __device__ __forceinline__ int sg_cell_ctx(const SgCoolArgs &A, const SgUnits &u
   b.E = pr * u.e_of_p;
   b.nH = rho * u.nh_of_rho;
   b.n = rho * u.n_of_rho;
-  if (t <= 3.0) {
+  if (A.w.xi_const > 0.0) {
+    b.xi = A.w.xi_const;
+    b.tx = A.w.t_x;
+  } else if (t <= 3.0) {
     const double r = A.x1[gi] * A.w.unit_length;
     b.xi = A.w.lx / (b.nH * r * r);
     b.tx = A.w.t_x;
@@ -152,8 +156,8 @@ __device__ __forceinline__ void sg_cool_items(const SgNet &net, const SgBox &bx,
     const SgCoolArgs A = args_of(bi.m);
     if (A.sc->done) continue;  // uniform over the CTA
     const SgUnits u = sg_units(A);
-    const int ncell = A.p.nx[0] * A.p.nx[1];
-    const int q = bi.b * kSgRows + threadIdx.x;
+    const long long ncell = (long long)A.p.nx[0] * A.p.nx[1] * A.p.nx[2];
+    const long long q = (long long)bi.b * kSgRows + threadIdx.x;
     const bool active = q < ncell;
     const double dt = A.sc->dt, t = A.sc->t;
     SgCtx b;

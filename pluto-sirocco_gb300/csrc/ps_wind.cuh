@@ -61,6 +61,9 @@ struct WindParams {
   // (code-unit rho and p): lf_a0 = log(krad) + alpharad log(C); the
   // acceleration per bin is (1 + M) F lf_cf
   double lf_a0, lf_cf;
+  // > 0: BLONDIN at this constant ionisation parameter with T_x (the
+  // Cartesian cooling configuration); 0: xi from the state / sirocco_xi
+  double xi_const;
 };
 
 struct WindStageArgs {

@@ -65,6 +65,20 @@ __device__ __forceinline__ long long vcell(const Params &p, int gj, int gi)
   return (long long)gj * p.px + gi;
 }
 
+__device__ __forceinline__ long long vcell3(const Params &p, int gk, int gj, int gi)
+{
+  return ((long long)gk * p.ntot[1] + gj) * p.px + gi;
+}
+
+// Active cell q (x fastest) -> (gi, gj, gk) of the total box.
+__device__ __forceinline__ void cell_of(const Params &p, long long q, int &gi, int &gj, int &gk)
+{
+  const long long r = q / p.nx[0];
+  gi = (int)(q - r * p.nx[0]) + p.beg[0];
+  gj = (int)(r % p.nx[1]) + p.beg[1];
+  gk = (int)(r / p.nx[1]) + p.beg[2];
+}
+
 // density / pressure floors of the problem's UserDefBoundary(side 0);
 // returns true if the cell was repaired.
 template <int NV>
@@ -203,21 +217,26 @@ __device__ __forceinline__ void init_xi_cell(const double *V, double *xi, double
 // ---------------------------------------------------------------
 
 // The cell's BLONDIN context from the state; false when the cell is below
-// the minimum cooling temperature and is left alone.
+// the minimum cooling temperature and is left alone.  q is the active cell
+// (x fastest, 2-D or 3-D); x1 is only read for the wind's xi.
 __device__ __forceinline__ bool blondin_ctx(const double *V, const double *xi_s, const double *tr_s,
                                             const Params &p, const WindParams &w,
-                                            const double *x1, double dt, double t, int q,
+                                            const double *x1, double dt, double t, long long q,
                                             BlCtx &b, double &T, long long &c)
 {
-  const int gi = q % p.nx[0] + p.beg[0], gj = q / p.nx[0] + p.beg[1];
-  c = vcell(p, gj, gi);
+  int gi, gj, gk;
+  cell_of(p, q, gi, gj, gk);
+  c = vcell3(p, gk, gj, gi);
   b.dt_share = dt * w.unit_time;
-  const double r = x1[gi] * w.unit_length;
   const double rho = V[RHO * p.vstride + c] * w.unit_density;
   const double pr = V[PRS * p.vstride + c];
   b.E = (pr * w.unit_pressure) / (p.gamma - 1);
   b.nH = rho / (1.43 * kMP);
-  if (t <= 3.0) {
+  if (w.xi_const > 0.0) {
+    b.xi = w.xi_const;
+    b.tx = w.t_x;
+  } else if (t <= 3.0) {
+    const double r = x1[gi] * w.unit_length;
     b.xi = w.lx / b.nH / r / r;
     b.tx = w.t_x;
   } else {
@@ -241,7 +260,7 @@ __device__ __forceinline__ void blondin_store(double *V, const Params &p, const 
 __device__ __forceinline__ void blondin_cell(double *V, const double *xi_s, const double *tr_s,
                                              const Params &p, const WindParams &w,
                                              const double *x1, Scalars *sc, double dt, double t,
-                                             int q)
+                                             long long q)
 {
   BlCtx b;
   double T;

@@ -32,7 +32,8 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_batch_get_shape", "ps_batch_autotune", "ps_batch_time_step_kernels",
            "ps_sg_create", "ps_sg_destroy", "ps_sg_set_params", "ps_sg_get_params",
            "ps_sg_label", "ps_sg_set_data", "ps_sg_train", "ps_sg_grad", "ps_sg_predict",
-           "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect"]
+           "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect",
+           "ps_set_cooling"]
 
 
 class Config(ctypes.Structure):
@@ -69,6 +70,12 @@ def make_wind(line_force=1, body_force=1, floors=1, nangles=36, **over):
 
 
 _lib = None
+
+
+class Cooling(ctypes.Structure):
+    _fields_ = [("unit_density", ctypes.c_double), ("unit_length", ctypes.c_double),
+                ("unit_velocity", ctypes.c_double), ("mu", ctypes.c_double),
+                ("t_x", ctypes.c_double), ("xi", ctypes.c_double)]
 
 
 class SgBox(ctypes.Structure):
@@ -145,6 +152,7 @@ def lib():
         L.ps_set_surrogate.argtypes = [P, P, I]
         L.ps_batch_set_surrogate.argtypes = [P, P, I]
         L.ps_sg_collect.argtypes = [P, DP, Lg, ctypes.POINTER(Lg)]
+        L.ps_set_cooling.argtypes = [P, ctypes.POINTER(Cooling)]
         _lib = L
     return _lib
 
@@ -249,6 +257,77 @@ def blast_state(cfg, grid, p_amb=0.1, p_in=10.0, r_in=0.1, noise=0.01, seed=1):
     return V
 
 
+# The 3-D periodic cooling configuration: BLONDIN at constant xi = 1e2 with
+# T_x = 5.6e7 K; code density 1 is 1e-10 g/cm^3 (n_H ~ 4e13 cm^-3), which
+# puts the cooling time of much of the 1e4-1e7 K gas near the time step
+# (code time unit 1 s).
+COOL_PARAMS = dict(unit_density=1e-10, unit_length=1e9, unit_velocity=1e9, mu=0.6, t_x=5.6e7,
+                   xi=1e2)
+AMU, KB = 1.66053886e-24, 1.3806505e-16
+
+
+def make_cooling(**over):
+    c = Cooling()
+    for k, v in dict(COOL_PARAMS, **over).items():
+        setattr(c, k, v)
+    return c
+
+
+def cube_config(n=512, cooling=1, first_dt=1e-3):
+    """n^3 on [0,1]^3, periodic, PLM-MC, HLLC, RK2, CFL 0.4, gamma 5/3."""
+    nx = n if isinstance(n, (tuple, list)) else (n, n, n)
+    return make_config(dims=3, nx=tuple(nx), limiter="mc", solver="hllc", bc="periodic", cfl=0.4,
+                       cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling)
+
+
+def cube_state(cfg, grid, seed=5, sigma=0.5, t_lo=1e4, t_hi=1e7, cooling=None):
+    """Initial state of the 3-D cooling configuration: rho = exp(sigma g -
+    sigma^2/2) with g a unit-variance Gaussian random field of power
+    spectrum k^-2 (white noise filtered by 1/|k| with numpy's FFT, seeded),
+    T drawn log-uniform in [t_lo, t_hi] per cell, v = 0,
+    p = rho T / (KELVIN mu) in code units; ghost cells periodic."""
+    cp = cooling or make_cooling()
+    nx, ny, nz = cfg.nx[0], cfg.nx[1], cfg.nx[2]
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((nz, ny, nx))
+    f = np.fft.rfftn(w)
+    del w
+    kz = np.fft.fftfreq(nz)[:, None, None]
+    ky = np.fft.fftfreq(ny)[None, :, None]
+    kx = np.fft.rfftfreq(nx)[None, None, :]
+    k2 = kz * kz + ky * ky + kx * kx
+    k2[0, 0, 0] = 1.0
+    f /= np.sqrt(k2)
+    f[0, 0, 0] = 0.0
+    del k2
+    g = np.fft.irfftn(f, s=(nz, ny, nx), axes=(0, 1, 2))
+    del f
+    g /= g.std()
+    rho = np.exp(sigma * g - 0.5 * sigma * sigma)
+    del g
+    T = 10.0 ** rng.uniform(np.log10(t_lo), np.log10(t_hi), (nz, ny, nx))
+    kelvin = cp.unit_velocity ** 2 * AMU / KB
+    V = np.zeros((cfg.nvar, nz + 4, ny + 4, nx + 4))
+    act = (slice(2, -2), slice(2, -2), slice(2, -2))
+    V[(0,) + act] = rho
+    V[(4,) + act] = rho * T / (kelvin * cp.mu)
+    del rho, T
+    for v in (0, 4):
+        V[v] = np.pad(V[(v,) + act], 2, mode="wrap")
+    return V
+
+
+def cube_solver(n, cooling=None, seed=5):
+    """Device context of the 3-D cooling configuration with its initial state."""
+    cfg = cube_config(n)
+    g = Grid(cfg)
+    s = Solver(cfg, g)
+    s.set_state(cube_state(cfg, g, seed=seed, cooling=cooling))
+    s.set_time(0.0, cfg.first_dt, 0)
+    s.set_cooling(cooling or make_cooling())
+    return s
+
+
 class Solver:
     """One device context (ps_ctx) on the current CUDA device."""
 
@@ -285,6 +364,9 @@ class Solver:
             raise ValueError("output array must be C-contiguous float64 of shape %s" % (shape,))
         check(lib().ps_get_state(self.ctx, _dp(V)), "ps_get_state")
         return V
+
+    def set_cooling(self, cooling):
+        check(lib().ps_set_cooling(self.ctx, ctypes.byref(cooling)), "ps_set_cooling")
 
     def set_wind(self, wind, flux=None):
         if flux is None:

@@ -76,3 +76,35 @@ def test_blondin_point_matches_grid_cooling(built):
     T1 = V1[4] * WIND["unit_density"] * WIND["unit_velocity"] ** 2 / (n1 * kKB)
     rel = np.abs(Tp - T1.ravel()) / T1.ravel()
     assert rel.max() < 1e-4, rel.max()
+
+
+def test_constant_xi_cooling_matches_point_solve(built):
+    """The oracle's cooling step at constant xi (3-D Cartesian) against the
+    point solve of every cell."""
+    from oracle import Oracle, blondin_points
+    import psgb
+    cp = psgb.COOL_PARAMS
+    cfg = psgb.cube_config((8, 6, 4))
+    V = psgb.cube_state(cfg, psgb.Grid(cfg), seed=7)
+    o = Oracle(dims=3, nx=(8, 6, 4), nvar=5, limiter="mc", solver="hllc", bc="periodic",
+               cooling=1, params=dict(unit_density=cp["unit_density"],
+                                      unit_length=cp["unit_length"],
+                                      unit_velocity=cp["unit_velocity"], mu=cp["mu"],
+                                      t_x=cp["t_x"], xi_const=cp["xi"]))
+    o.V[...] = V
+    a = o.active().copy()
+    kMP, kKB = 1.67262171e-24, 1.3806505e-16
+    rho = a[0] * cp["unit_density"]
+    prs = a[4] * cp["unit_density"] * cp["unit_velocity"] ** 2
+    n = rho / (cp["mu"] * kMP)
+    T = (prs / (2.0 / 3.0)) * (2.0 / 3.0) / (n * kKB)
+    dt = 1e-2
+    tup = np.stack([(rho / (1.43 * kMP)).ravel(), T.ravel(), np.full(T.size, cp["xi"]),
+                    np.full(T.size, dt * cp["unit_length"] / cp["unit_velocity"])], axis=1)
+    Tp = blondin_points(tup, tx=cp["t_x"], mu=cp["mu"])
+    o.cooling(dt, 10.0)
+    b = o.active()
+    T1 = b[4] * cp["unit_density"] * cp["unit_velocity"] ** 2 / (n * kKB)
+    rel = np.abs(Tp - T1.ravel()) / T1.ravel()
+    assert rel.max() < 1e-4, rel.max()
+    assert np.any(np.abs(T1 - T) > 1e-3 * T)
