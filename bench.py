@@ -71,7 +71,7 @@ class Workload:
             self.cpu_steps = 30
             self.desc = ("wind2d-512x256: 2-D spherical line-driven disk wind, PLM-VL, HLL, RK2, "
                          "CFL 0.4, BLONDIN cooling, line force (36 bins), 7 Msun, L_x 1e37")
-            self.profile = "stage_kernel_wind_512x256.md"
+            self.profile = "stage_kernel_wind_batch64.md"
         elif name == "batch":
             import psgb
             self.specs = psgb.batch_models(64, seed=4)
@@ -83,7 +83,7 @@ class Workload:
                          "drawn from 128x64, 256x128, 384x192, 512x256; L_x log-uniform "
                          "1e36..1e38 erg/s, k U(0.1,0.4), alpha U(0.5,0.7); seed 4), each as "
                          "the wind2d workload, all advanced together")
-            self.profile = "stage_kernel_wind_512x256.md"
+            self.profile = "stage_kernel_wind_batch64.md"
         elif name == "cube":
             self.nx = self.ny = self.nz = 512
             self.nvar = 5
@@ -94,7 +94,7 @@ class Workload:
                          "CFL 0.4, gamma 5/3, log-normal density (sigma 0.5, P(k) ~ k^-2, seed 5),"
                          " T log-uniform 1e4..1e7 K per cell, BLONDIN at xi = 1e2 (Strang split),"
                          " code density 1 = 1e-10 g/cm^3")
-            self.profile = "stage_kernel_cube3d_512.md"
+            self.profile = "stage_kernel_cube3d.md"
         else:
             self.nx, self.ny, self.nvar = 256, 256, 5
             self.steps = 100
@@ -729,7 +729,8 @@ def _rooflines(out, wl, stage_ms, per_kernel):
     achieved = alg_bytes_launch / (stage_ms * 1e-3) / 1e9
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                        "frac": achieved / hbm_peak,
-                       "traffic": _profile_value(wl, "traffic_bytes_per_launch"),
+                       "traffic": (lambda b: b * wl.cells if b else None)(
+                           _profile_value(wl, "traffic_bytes_per_cell_launch")),
                        "kernel": "stage kernel (fused PLM/Riemann/sources/update), per launch",
                        "stage_ms": [per_kernel[0], per_kernel[1]],
                        "other_ms_per_step": per_kernel[2],
@@ -778,8 +779,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="batch", choices=["wind", "blast", "batch", "cube"])
+    ap.add_argument("--cube-n", type=int, default=512,
+                    help="cells per direction of the cube workload (smaller cases for profiling)")
     a = ap.parse_args()
     wl = Workload(a.workload)
+    if a.workload == "cube" and a.cube_n != 512:
+        wl.nx = wl.ny = wl.nz = a.cube_n
+        wl.cells = a.cube_n ** 3
+        wl.desc = wl.desc.replace("cube3d-512", "cube3d-%d" % a.cube_n)
     steps = a.steps if a.steps is not None else wl.steps
     rank, world = _env_rank()
     if a.impl == "reference":
