@@ -251,7 +251,8 @@ int  ps_batch_sync(ps_batch *b);      /* OR of every model's PS_F_* flags */
 int  ps_batch_set_stream(ps_batch *b, void *stream);
 long ps_batch_launch_count(const ps_batch *b);
 /* Tile shape of the stage kernels per model: 0 = 32x8, 1 = 16x16,
- * 2 = 64x4 (model = -1: all models).  ps_batch_autotune times the stage
+ * 2 = 64x4, 3 = 16x16 with one extra warp sharing the halo work (model =
+ * -1: all models).  ps_batch_autotune times the stage
  * kernel of every distinct grid size with each shape and keeps the fastest
  * (`reps` timed launches each); the state is left unchanged. */
 int  ps_batch_set_shape(ps_batch *b, int model, int shape);

@@ -140,9 +140,13 @@ __global__ void k_batch_finish(const BatchModel *__restrict__ models)
 // kernel tables for the tile shapes the autotuner chooses from
 // ------------------------------------------------------------------
 
-constexpr int kNumShapes = 3;
-const int kShapeX[kNumShapes] = {32, 16, 64};
-const int kShapeY[kNumShapes] = {8, 16, 4};
+constexpr int kNumShapes = 4;
+const int kShapeX[kNumShapes] = {32, 16, 64, 16};
+const int kShapeY[kNumShapes] = {8, 16, 4, 16};
+// threads per CTA: one per cell, plus one warp for the halo work of the
+// 16x16 tile's PLM (18 x 16 items) in shape 3
+const int kShapeNT[kNumShapes] = {256, 256, 256, 288};
+using Shape3 = Tile2D<16, 16, 32>;
 
 template <int LIM, int SOLVER, class TL>
 static const void *pick_batch(int stage)
@@ -169,6 +173,7 @@ static const void *batch_kernel(int shape, int lim, int solver, int stage)
   switch (shape) {
     case 1: return pick_batch_shape<Tile2D<16, 16>>(lim, solver, stage);
     case 2: return pick_batch_shape<Tile2D<64, 4>>(lim, solver, stage);
+    case 3: return pick_batch_shape<Shape3>(lim, solver, stage);
     default: return pick_batch_shape<Tile2D<32, 8>>(lim, solver, stage);
   }
 }
@@ -178,6 +183,7 @@ static size_t batch_smem(int shape)
   switch (shape) {
     case 1: return stage_smem_bytes<6, Tile2D<16, 16>>();
     case 2: return stage_smem_bytes<6, Tile2D<64, 4>>();
+    case 3: return stage_smem_bytes<6, Shape3>();
     default: return stage_smem_bytes<6, Tile2D<32, 8>>();
   }
 }
@@ -195,8 +201,8 @@ struct ps_batch {
   std::vector<ps::BatchModel> h_models;
   std::vector<int> shape;              // chosen tile shape per model
   // per shape group: work list of tiles
-  ps::TileItem *d_items[ps::kNumShapes] = {nullptr, nullptr, nullptr};
-  int nitems[ps::kNumShapes] = {0, 0, 0};
+  ps::TileItem *d_items[ps::kNumShapes] = {};
+  int nitems[ps::kNumShapes] = {};
   ps::BlockItem *d_cells = nullptr, *d_x2 = nullptr;
   int ncells_blocks = 0, nx2_blocks = 0;
   const double **d_xi = nullptr, **d_tr = nullptr;
@@ -211,8 +217,8 @@ struct ps_batch {
   int lim = 0, solver = 0, cooling = 0;
   cudaStream_t stream = nullptr;      // stream the work is issued on
   cudaStream_t own_stream = nullptr;  // stream created by the batch
-  cudaStream_t side[ps::kNumShapes] = {nullptr, nullptr, nullptr};  // tile-shape groups
-  cudaEvent_t fork = nullptr, join[ps::kNumShapes] = {nullptr, nullptr, nullptr};
+  cudaStream_t side[ps::kNumShapes] = {};  // tile-shape groups
+  cudaEvent_t fork = nullptr, join[ps::kNumShapes] = {};
   cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};
   long long host_step = 0;
   long launches = 0;
@@ -357,7 +363,8 @@ static int batch_stage(ps_batch *b, int stage)
     if (s != first) BCK(cudaStreamWaitEvent(st, b->fork, 0));
     const void *k = ps::batch_kernel(s, b->lim, b->solver, stage);
     void *args[2] = {&b->d_models, &b->d_items[s]};
-    BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(256), args, ps::batch_smem(s), st));
+    BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(ps::kShapeNT[s]), args, ps::batch_smem(s),
+                         st));
     b->launches++;
     if (s != first) BCK(cudaEventRecord(b->join[s], st));
   }
@@ -575,12 +582,12 @@ extern "C" int ps_batch_autotune(ps_batch *b, int reps)
                      cudaMemcpyHostToDevice));
       const void *k = ps::batch_kernel(s, b->lim, b->solver, 1);
       void *args[2] = {&b->d_models, &d_items};
-      BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(256), args, ps::batch_smem(s),
-                           b->stream));
+      BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(ps::kShapeNT[s]), args,
+                           ps::batch_smem(s), b->stream));
       BCK(cudaEventRecord(e0, b->stream));
       for (int it = 0; it < reps; it++)
-        BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(256), args, ps::batch_smem(s),
-                             b->stream));
+        BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(ps::kShapeNT[s]), args,
+                             ps::batch_smem(s), b->stream));
       BCK(cudaEventRecord(e1, b->stream));
       BCK(cudaEventSynchronize(e1));
       float ms = 0.f;

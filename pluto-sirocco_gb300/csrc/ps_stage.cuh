@@ -31,15 +31,26 @@ template <> struct TileT<2> {
 template <> struct TileT<3> {
   static constexpr int X = 16, Y = 4, Z = 4, HX = 2, HY = 2, HZ = 2;
 };
-// 2-D tiles of other shapes (chosen per grid size by the batch autotuner)
-template <int TX, int TY> struct Tile2D {
-  static constexpr int X = TX, Y = TY, Z = 1, HX = 2, HY = 2, HZ = 0;
+// 2-D tiles of other shapes (chosen per grid size by the batch autotuner);
+// XT extra threads (whole warps) share the halo work of the PLM and
+// Riemann phases, which have more items than the tile has cells; they own
+// no cell.
+template <int TX, int TY, int XT = 0> struct Tile2D {
+  static constexpr int X = TX, Y = TY, Z = 1, HX = 2, HY = 2, HZ = 0, EXTRA = XT;
+};
+
+template <class TL, class = void> struct TileExtra {
+  static constexpr int value = 0;
+};
+template <class TL> struct TileExtra<TL, decltype((void)TL::EXTRA)> {
+  static constexpr int value = TL::EXTRA;
 };
 
 template <class TL> struct TileGeom {
   static constexpr int SX = TL::X + 2 * TL::HX, SY = TL::Y + 2 * TL::HY, SZ = TL::Z + 2 * TL::HZ;
   static constexpr int VS = SX * SY * SZ;            // cells in the haloed tile
-  static constexpr int NT = TL::X * TL::Y * TL::Z;   // threads per CTA
+  static constexpr int NC = TL::X * TL::Y * TL::Z;   // cells of the tile (owning threads)
+  static constexpr int NT = NC + TileExtra<TL>::value;  // threads per CTA
   __host__ __device__ static constexpr int t(int d)
   {
     return d == 0 ? TL::X : (d == 1 ? TL::Y : TL::Z);
@@ -256,7 +267,7 @@ __global__ void __launch_bounds__(TileGeom<TileT<DIMS>>::NT)
   }
 
   const int cx = tid % TL::X, cy = (tid / TL::X) % TL::Y, cz = tid / (TL::X * TL::Y);
-  const bool own = (ox + cx < p.nx[0]) && (oy + cy < p.nx[1]) && (oz + cz < p.nx[2]);
+  const bool own = tid < G::NC && (ox + cx < p.nx[0]) && (oy + cy < p.nx[1]) && (oz + cz < p.nx[2]);
   const int gi = p.beg[0] + ox + cx, gj = p.beg[1] + oy + cy, gk = p.beg[2] + oz + cz;
   const long long cell = ((long long)gk * p.ntot[1] + gj) * p.px + gi;
 

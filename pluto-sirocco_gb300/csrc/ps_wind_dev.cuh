@@ -499,7 +499,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
   }
 
   const int cx = tid % TL::X, cy = tid / TL::X;
-  const bool own = (ox + cx < p.nx[0]) && (oy + cy < p.nx[1]);
+  const bool own = tid < G::NC && (ox + cx < p.nx[0]) && (oy + cy < p.nx[1]);
   const int gi = p.beg[0] + ox + cx, gj = p.beg[1] + oy + cy;
   const long long cell = (long long)gj * p.px + gi;
   const double dt = a.sc->dt;
