@@ -323,6 +323,18 @@ int ps_batch_set_surrogate(ps_batch *b, ps_surrogate *s, int use_net);
  * wind context would solve (at most cap rows); *n = rows written. */
 int ps_sg_collect(ps_ctx *ctx, double *tuples, long cap, long *n);
 
+/* PLUTO's DBL snapshots of the device state: WriteData in single-file
+ * mode (Src/write_data.c:132-220, Src/bin_io.c:216-258) writes
+ * <dir>/data.<nfile>.dbl (every variable in Data.Vc order over the active
+ * cells, x fastest, little-endian doubles) and the dbl.out line
+ * "nfile t dt nstep single_file little <names>" (write_data.c:420-448),
+ * keeping the first nfile lines of an existing dbl.out.  names may be NULL
+ * (rho vx1 vx2 vx3 prs tr1 ...).  ps_read_dbl loads such a file into the
+ * context (the .dbl part of RestartFromFile, Src/restart.c:104-170); the
+ * time comes from restart.out on the host side (ps_set_time). */
+int ps_write_dbl(ps_ctx *ctx, const char *dir, int nfile, const char *names);
+int ps_read_dbl(ps_ctx *ctx, const char *path);
+
 /* Device-side checkpoint / restore of Data.Vc and the main-loop scalars:
  * the backup that FAILSAFE keeps before a step (Src/failsafe.c:5-160),
  * held on the GPU so that a step can be retried or a run replayed. */

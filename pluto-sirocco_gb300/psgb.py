@@ -33,7 +33,7 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_sg_create", "ps_sg_destroy", "ps_sg_set_params", "ps_sg_get_params",
            "ps_sg_label", "ps_sg_set_data", "ps_sg_train", "ps_sg_grad", "ps_sg_predict",
            "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect",
-           "ps_set_cooling"]
+           "ps_set_cooling", "ps_write_dbl", "ps_read_dbl"]
 
 
 class Config(ctypes.Structure):
@@ -153,6 +153,8 @@ def lib():
         L.ps_batch_set_surrogate.argtypes = [P, P, I]
         L.ps_sg_collect.argtypes = [P, DP, Lg, ctypes.POINTER(Lg)]
         L.ps_set_cooling.argtypes = [P, ctypes.POINTER(Cooling)]
+        L.ps_write_dbl.argtypes = [P, ctypes.c_char_p, I, ctypes.c_char_p]
+        L.ps_read_dbl.argtypes = [P, ctypes.c_char_p]
         _lib = L
     return _lib
 
@@ -364,6 +366,13 @@ class Solver:
             raise ValueError("output array must be C-contiguous float64 of shape %s" % (shape,))
         check(lib().ps_get_state(self.ctx, _dp(V)), "ps_get_state")
         return V
+
+    def write_dbl(self, directory, nfile, names=None):
+        check(lib().ps_write_dbl(self.ctx, os.fsencode(directory), nfile,
+                                 names.encode() if names else None), "ps_write_dbl")
+
+    def read_dbl(self, path):
+        check(lib().ps_read_dbl(self.ctx, os.fsencode(path)), "ps_read_dbl")
 
     def set_cooling(self, cooling):
         check(lib().ps_set_cooling(self.ctx, ctypes.byref(cooling)), "ps_set_cooling")
