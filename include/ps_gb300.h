@@ -140,6 +140,29 @@ int ps_wind_synthetic_flux(const ps_config *cfg, const ps_wind *w,
                            const double *x1, const double *x2,
                            double *fr, double *ft, double *fp);
 
+/* Readers of the files a SIROCCO run hands to the wind problem
+ * (Src/LineDriven/line_connect.c:43-497), host only.  Records are placed on
+ * the 2-D spherical grid (x1, x2: cell-centre arrays of the total box, x1 in
+ * code units) by their coordinates with the reference's tolerances, found by
+ * binary search instead of the reference's scan of every cell; arrays are
+ * [j][i] over the total box and cells without a record keep their values.
+ *   ps_read_sirocco_fluxes: <dir>/directional_flux_{r,theta,phi}.dat into
+ *     fr/ft/fp ([angle][j][i], at most max_angles planes); returns the
+ *     number of angle bins (read_sirocco_fluxes).
+ *   ps_read_sirocco_heatcool: py_heatcool.dat into xi and t_r with the
+ *     reference's floors xi >= 1, t_r >= 1e3 K.
+ *   ps_read_sirocco_prefactors: prefactors.dat into six arrays in the
+ *     file's order comp_h, comp_c, xray_h, brem_c, line_c, xi_ion.
+ * *matched (may be NULL) gets the number of records placed. */
+int ps_read_sirocco_fluxes(const ps_config *cfg, double unit_length, const double *x1,
+                           const double *x2, const char *dir, int max_angles, double *fr,
+                           double *ft, double *fp, long *matched);
+int ps_read_sirocco_heatcool(const ps_config *cfg, double unit_length, const double *x1,
+                             const double *x2, const char *path, double *xi, double *t_r,
+                             long *matched);
+int ps_read_sirocco_prefactors(const ps_config *cfg, double unit_length, const double *x1,
+                               const double *x2, const char *path, double *pre, long *matched);
+
 /* ---------------------------------------------------------------- */
 /* device context                                                    */
 /* ---------------------------------------------------------------- */
@@ -233,6 +256,16 @@ int ps_set_cooling(ps_ctx *ctx, const ps_cooling *c);
 /* ---------------------------------------------------------------- */
 /* batches of independent wind models                                */
 /* ---------------------------------------------------------------- */
+
+/* read_sirocco_heatcool with flag 1 (line_connect.c:267-497) on the
+ * device: per-cell xi and radiation temperature (BLONDIN uses them once
+ * g_time > 3) and the prefactors of the rates (six [j][i] arrays in the
+ * prefactors.dat order; xi_ion is not used by BLONDIN).  NULL leaves a part
+ * as it is; ps_set_wind starts from xi and T_x of the state and prefactors
+ * 1.  Call before ps_batch_create for contexts that go into a batch.  The
+ * learned cooling step leaves cells whose prefactors are not 1 to the
+ * reference method. */
+int ps_set_sirocco(ps_ctx *ctx, const double *xi, const double *t_r, const double *pre);
 
 /* No reference counterpart (the reference runs one model per process).
  * Advances n independent line-driven wind contexts (each already set up

@@ -70,6 +70,7 @@ def lib():
         L.or_cooling.argtypes = [P, D, D]
         L.or_blondin_point.restype = D
         L.or_blondin_point.argtypes = [D, D, D, D, D, D]
+        L.or_set_sirocco.argtypes = [P, DP, DP, DP]
         L.or_sirocco_xi.restype = DP
         L.or_sirocco_xi.argtypes = [P]
         _lib = L
@@ -171,6 +172,14 @@ class Oracle:
         dp = ctypes.POINTER(ctypes.c_double)
         lib().or_set_flux(self.s, fr.shape[0], fr.ctypes.data_as(dp), ft.ctypes.data_as(dp),
                           fp.ctypes.data_as(dp))
+
+    def set_sirocco(self, xi=None, t_r=None, pre=None):
+        """Per-cell sirocco_xi, sirocco_t_r and prefactors (6 arrays, file
+        order), each over the total box."""
+        dp = ctypes.POINTER(ctypes.c_double)
+        keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (xi, t_r, pre)]
+        lib().or_set_sirocco(self.s, *[None if a is None else a.ctypes.data_as(dp) for a in keep])
 
     def cooling(self, dt, t):
         lib().or_cooling(self.s, dt, t)

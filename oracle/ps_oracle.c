@@ -82,6 +82,7 @@ struct or_sim {
   int na;
   double *Fr, *Ft, *Fp;            /* [a][k][j][i] */
   double *xi_s, *tr_s;             /* sirocco_xi, sirocco_t_r */
+  double *pre;                     /* 6 prefactor arrays (file order) or NULL: all 1 */
   double *dvds, *roff, *toff, *moff; /* [a][k][j][i] */
   double *x11[2], *x22[2];
   int dvds_ready;
@@ -296,7 +297,7 @@ void or_destroy(or_sim *s)
   }
   free(s->rt); free(s->sp); free(s->sn); free(s->dmu); free(s->dVr);
   free(s->dV); free(s->Ax1); free(s->Ax2); free(s->rvc);
-  free(s->Fr); free(s->Ft); free(s->Fp); free(s->xi_s); free(s->tr_s);
+  free(s->Fr); free(s->Ft); free(s->Fp); free(s->xi_s); free(s->tr_s); free(s->pre);
   free(s->dvds); free(s->roff); free(s->toff); free(s->moff);
   free(s->x11[0]); free(s->x11[1]); free(s->x22[0]); free(s->x22[1]);
   free(s->V); free(s->U); free(s->U0); free(s->Cdt);
@@ -324,6 +325,21 @@ const double *or_grid(const or_sim *s, int dir, int which)
 }
 
 const double *or_sirocco_xi(const or_sim *s) { return s->xi_s; }
+
+/* read_sirocco_heatcool with flag 1 (line_connect.c:267-497) as data:
+ * sirocco_xi, sirocco_t_r and the prefactor arrays (file order comp_h,
+ * comp_c, xray_h, brem_c, line_c, xi_ion), each over the total box; NULL
+ * keeps that part. */
+void or_set_sirocco(or_sim *s, const double *xi, const double *t_r, const double *pre)
+{
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  if (xi) memcpy(s->xi_s, xi, nc * sizeof(double));
+  if (t_r) memcpy(s->tr_s, t_r, nc * sizeof(double));
+  if (pre) {
+    if (!s->pre) s->pre = malloc(6 * nc * sizeof(double));
+    memcpy(s->pre, pre, 6 * nc * sizeof(double));
+  }
+}
 
 void or_time(const or_sim *s, double *t, double *dt, long *step)
 {
@@ -1273,6 +1289,13 @@ void or_cooling(or_sim *s, double dt, double t)
   for (j = s->beg[1]; j <= s->end[1]; j++)
   for (i = s->beg[0]; i <= s->end[0]; i++) {
     size_t c = cidx(s, k, j, i);
+    if (s->pre) {   /* cooling.c:73-79 */
+      b.comp_h_pre = s->pre[0 * nc + c];
+      b.comp_c_pre = s->pre[1 * nc + c];
+      b.xray_h_pre = s->pre[2 * nc + c];
+      b.brem_c_pre = s->pre[3 * nc + c];
+      b.line_c_pre = s->pre[4 * nc + c];
+    }
     double r = s->x[0][i] * s->c.unit_length;
     double rho = s->V[RHO * nc + c] * s->c.unit_density;
     double p = s->V[PRS * nc + c], T, T_f, t_l, t_u, test, E_f, p_f;

@@ -107,6 +107,7 @@ double  or_blondin_point(double nH, double T, double xi, double tx, double dt_s,
 /* Frozen ionisation parameter and radiation temperature per cell
  * ([k][j][i], total box). */
 const double *or_sirocco_xi(const or_sim *s);
+void    or_set_sirocco(or_sim *s, const double *xi, const double *t_r, const double *pre);
 
 #ifdef __cplusplus
 }

@@ -80,7 +80,7 @@ __global__ void k_batch_bnd_x2(const BatchModel *__restrict__ models,
 
 __global__ void k_batch_blondin(const BatchModel *__restrict__ models,
                                 const BlockItem *__restrict__ blocks, const double *const *xi,
-                                const double *const *tr)
+                                const double *const *tr, const double *const *pre)
 {
   const BlockItem bi = blocks[blockIdx.x];
   const WindStageArgs &A = models[bi.m].st[0];
@@ -89,19 +89,20 @@ __global__ void k_batch_blondin(const BatchModel *__restrict__ models,
   const int q = bi.b * blockDim.x + threadIdx.x;
   if (q < A.s.p.nx[0] * A.s.p.nx[1])
     blondin_cell(const_cast<double *>(A.s.Vn), xi[bi.m], tr[bi.m], A.s.p, A.w, A.g.x1, sc, sc->dt,
-                 sc->t, q);
+                 sc->t, q, pre[bi.m]);
 }
 
 // The split-source step with the surrogate: one CTA per 128-cell block of
 // one model; the cells the judge rejects are queued as (model, cell).
 __device__ __forceinline__ SgCoolArgs batch_cool_args(const BatchModel &M, const double *xi,
-                                                      const double *tr)
+                                                      const double *tr, const double *pre)
 {
   const WindStageArgs &A = M.st[0];
   SgCoolArgs c;
   c.V = const_cast<double *>(A.s.Vn);
   c.xi = xi;
   c.tr = tr;
+  c.pre = pre;
   c.x1 = A.g.x1;
   c.p = A.s.p;
   c.w = A.w;
@@ -111,23 +112,24 @@ __device__ __forceinline__ SgCoolArgs batch_cool_args(const BatchModel &M, const
 
 __global__ void __launch_bounds__(128)
     k_batch_sg_cool(const BatchModel *__restrict__ models, const BlockItem *__restrict__ blocks,
-                    int nitems, const double *const *xi, const double *const *tr, SgNet net,
-                    SgBox bx, int use_net, int2 *queue, int *qcount, unsigned long long *stats)
+                    int nitems, const double *const *xi, const double *const *tr,
+                    const double *const *pre, SgNet net, SgBox bx, int use_net, int2 *queue,
+                    int *qcount, unsigned long long *stats)
 {
   extern __shared__ __align__(1024) unsigned char smem[];
-  auto args_of = [&](int m) { return batch_cool_args(models[m], xi[m], tr[m]); };
+  auto args_of = [&](int m) { return batch_cool_args(models[m], xi[m], tr[m], pre[m]); };
   sg_cool_items(net, bx, args_of, blocks, nitems, use_net, smem, queue, qcount, stats);
 }
 
 __global__ void k_batch_sg_fallback(const BatchModel *__restrict__ models, const double *const *xi,
-                                    const double *const *tr, const int2 *__restrict__ queue,
-                                    const int *__restrict__ qcount)
+                                    const double *const *tr, const double *const *pre,
+                                    const int2 *__restrict__ queue, const int *__restrict__ qcount)
 {
   const int cnt = *qcount;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
     const int2 e = queue[k];
-    const SgCoolArgs A = batch_cool_args(models[e.x], xi[e.x], tr[e.x]);
-    blondin_cell(A.V, A.xi, A.tr, A.p, A.w, A.x1, A.sc, A.sc->dt, A.sc->t, e.y);
+    const SgCoolArgs A = batch_cool_args(models[e.x], xi[e.x], tr[e.x], pre[e.x]);
+    blondin_cell(A.V, A.xi, A.tr, A.p, A.w, A.x1, A.sc, A.sc->dt, A.sc->t, e.y, A.pre);
   }
 }
 
@@ -205,7 +207,7 @@ struct ps_batch {
   int nitems[ps::kNumShapes] = {};
   ps::BlockItem *d_cells = nullptr, *d_x2 = nullptr;
   int ncells_blocks = 0, nx2_blocks = 0;
-  const double **d_xi = nullptr, **d_tr = nullptr;
+  const double **d_xi = nullptr, **d_tr = nullptr, **d_pre = nullptr;
   ps::BlockItem *d_cells128 = nullptr;  // 128-cell blocks (surrogate kernel)
   int ncells128 = 0;
   long total_cells = 0;
@@ -392,15 +394,15 @@ static int batch_cool(ps_batch *b)
     BCK(cudaMemsetAsync(b->sg_qcount, 0, sizeof(int), b->stream));
     const int grid = std::min(b->ncells128, b->num_sms * ps::kInfCtasPerSm);
     ps::k_batch_sg_cool<<<grid, 128, ps::kInfBytes, b->stream>>>(
-        b->d_models, b->d_cells128, b->ncells128, b->d_xi, b->d_tr, ps_sg_net(b->sg),
+        b->d_models, b->d_cells128, b->ncells128, b->d_xi, b->d_tr, b->d_pre, ps_sg_net(b->sg),
         ps_sg_boxv(b->sg), b->sg_use_net, b->sg_queue, b->sg_qcount, ps_sg_stats_dev(b->sg));
-    ps::k_batch_sg_fallback<<<1216, 128, 0, b->stream>>>(b->d_models, b->d_xi, b->d_tr, b->sg_queue,
-                                                         b->sg_qcount);
+    ps::k_batch_sg_fallback<<<1216, 128, 0, b->stream>>>(b->d_models, b->d_xi, b->d_tr, b->d_pre,
+                                                         b->sg_queue, b->sg_qcount);
     b->launches += 2;
     return 0;
   }
   ps::k_batch_blondin<<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, b->d_xi,
-                                                               b->d_tr);
+                                                               b->d_tr, b->d_pre);
   b->launches++;
   return 0;
 }
@@ -432,6 +434,7 @@ static void batch_free(ps_batch *b)
   cudaFree(b->d_x2);
   cudaFree(b->d_xi);
   cudaFree(b->d_tr);
+  cudaFree(b->d_pre);
   cudaFree(b->d_cells128);
   cudaFree(b->sg_queue);
   cudaFree(b->sg_qcount);
@@ -469,6 +472,7 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
       (e = cudaMalloc(&b->d_models, sizeof(ps::BatchModel) * n)) != cudaSuccess ||
       (e = cudaMalloc(&b->d_xi, sizeof(double *) * n)) != cudaSuccess ||
       (e = cudaMalloc(&b->d_tr, sizeof(double *) * n)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_pre, sizeof(double *) * n)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess) {
     batch_free(b);
     return batch_cuda(e, "ps_batch_create");
@@ -486,14 +490,16 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);
   }
-  std::vector<const double *> xi(n), tr(n);
+  std::vector<const double *> xi(n), tr(n), pre(n);
   for (int m = 0; m < n; m++) {
     xi[m] = ctxs[m]->wind->xi;
     tr[m] = ctxs[m]->wind->tr;
+    pre[m] = ctxs[m]->wind->pre;
     cudaStreamSynchronize(ctxs[m]->stream);
   }
   cudaMemcpy(b->d_xi, xi.data(), sizeof(double *) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_tr, tr.data(), sizeof(double *) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_pre, pre.data(), sizeof(double *) * n, cudaMemcpyHostToDevice);
   for (int s = 0; s < ps::kNumShapes; s++) {
     for (int st = 1; st <= 2; st++) {
       e = cudaFuncSetAttribute(ps::batch_kernel(s, b->lim, b->solver, st),

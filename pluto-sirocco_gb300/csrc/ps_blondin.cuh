@@ -1,5 +1,5 @@
 // ps_blondin.cuh -- BLONDIN heating/cooling on the device
-// (Src/Cooling/BLONDIN/cooling.c:50-319, prefactors 1): the per-cell
+// (Src/Cooling/BLONDIN/cooling.c:50-319): the per-cell
 // implicit trapezoidal energy equation in T solved by bracket expansion and
 // Brent's method, shared by the wind kernels, the batched kernels and the
 // surrogate (which uses it as its fallback and to label training pairs).
@@ -16,6 +16,10 @@ constexpr int kMaxCoolIter = 10000;  // the bracket search of the reference ends
 
 struct BlCtx {
   double xi, sqxi, sqsqxi, nH, n, tx, E, hc_init, dt_share;
+  // per-cell prefactors of the five rates (1 unless a SIROCCO prefactor
+  // file was read): Compton heating, Compton cooling, X-ray heating, line
+  // cooling, bremsstrahlung
+  double ch = 1.0, cc = 1.0, xh = 1.0, lc = 1.0, bc = 1.0;
 };
 
 // ne_rat (cooling.c:210-222)
@@ -26,17 +30,17 @@ __device__ __forceinline__ double bl_ne_rat(double T)
   return 1.21;
 }
 
-// heatcool (cooling.c:173-202), all prefactors 1
+// heatcool (cooling.c:173-202) with the cell's prefactors
 __device__ __forceinline__ double bl_heatcool(const BlCtx &b, double T)
 {
   const double sqT = sqrt(T);
   const double ne = b.nH * bl_ne_rat(T);
-  const double comp_heat = 1.0 * (8.9e-36 * b.xi * b.tx);
-  const double comp_cool = 1.0 * (8.9e-36 * b.xi * (4.0 * T));
-  const double xray_heat = 1.0 * (1.5e-21 * (b.sqsqxi / sqT));
+  const double comp_heat = b.ch * (8.9e-36 * b.xi * b.tx);
+  const double comp_cool = b.cc * (8.9e-36 * b.xi * (4.0 * T));
+  const double xray_heat = b.xh * (1.5e-21 * (b.sqsqxi / sqT));
   const double line_cool =
-      1.0 * ((1e-16 * exp(-1.3e5 / T) / b.sqxi / T) + fmin(fmin(1e-24, 5e-27 * sqT), 1.5e-17 / T));
-  const double brem_cool = 1.0 * (3.3e-27 * sqT);
+      b.lc * ((1e-16 * exp(-1.3e5 / T) / b.sqxi / T) + fmin(fmin(1e-24, 5e-27 * sqT), 1.5e-17 / T));
+  const double brem_cool = b.bc * (3.3e-27 * sqT);
   return b.nH *
          (ne * comp_heat + b.nH * xray_heat - ne * comp_cool - ne * line_cool - ne * brem_cool);
 }

@@ -26,7 +26,7 @@ __global__ void k_blondin_cart(double *V, const Params p, const WindParams w, Sc
   const long long n = (long long)p.nx[0] * p.nx[1] * p.nx[2];
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x)
-    blondin_cell(V, nullptr, nullptr, p, w, nullptr, sc, dt, t, q);
+    blondin_cell(V, nullptr, nullptr, p, w, nullptr, sc, dt, t, q, nullptr);
 }
 
 }  // namespace ps

@@ -443,7 +443,7 @@ __global__ void k_sg_cool_fallback(SgCoolArgs A, const int2 *__restrict__ queue,
   const int cnt = *qcount;
   const double dt = A.sc->dt, t = A.sc->t;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x)
-    blondin_cell(A.V, A.xi, A.tr, A.p, A.w, A.x1, A.sc, dt, t, queue[k].y);
+    blondin_cell(A.V, A.xi, A.tr, A.p, A.w, A.x1, A.sc, dt, t, queue[k].y, A.pre);
 }
 
 // (n_H, T, xi, dt_s) of every cell BLONDIN would solve now.
@@ -456,7 +456,7 @@ __global__ void k_sg_collect(SgCoolArgs A, double *__restrict__ out, long cap, i
     BlCtx b;
     double T;
     long long c;
-    if (!blondin_ctx(A.V, A.xi, A.tr, A.p, A.w, A.x1, dt, t, q, b, T, c)) continue;
+    if (!blondin_ctx(A.V, A.xi, A.tr, A.p, A.w, A.x1, dt, t, q, b, T, c, A.pre)) continue;
     const int k = atomicAdd(count, 1);
     if (k < cap) {
       out[4 * k] = b.nH;
@@ -900,9 +900,10 @@ static ps::SgCoolArgs sg_cool_args(ps_ctx *c)
     A.xi = c->wind->xi;
     A.tr = c->wind->tr;
     A.x1 = c->wind->a.g.x1;
+    A.pre = c->wind->pre;
     A.w = c->wind->a.w;
   } else {  // Cartesian cooling at constant xi
-    A.xi = A.tr = A.x1 = nullptr;
+    A.xi = A.tr = A.x1 = A.pre = nullptr;
     A.w = c->coolw;
   }
   return A;

@@ -82,6 +82,7 @@ __device__ __forceinline__ void sg_count(int st, bool active, int evals, bool st
 struct SgCoolArgs {
   double *V;
   const double *xi, *tr, *x1;
+  const double *pre;  // per-cell prefactors (5 arrays) or NULL
   Params p;
   WindParams w;
   Scalars *sc;
@@ -134,6 +135,10 @@ __device__ __forceinline__ int sg_cell_ctx(const SgCoolArgs &A, const SgUnits &u
   } else {
     b.xi = A.xi[c];
     b.tx = A.tr[c];
+  }
+  if (A.pre) {  // the network knows prefactors 1 only
+    for (int k = 0; k < 5; k++)
+      if (A.pre[k * p.vstride + c] != 1.0) return 2;
   }
   return T < 1.e4 * (1.0 + 1e-12) ? 2 : 1;
 }

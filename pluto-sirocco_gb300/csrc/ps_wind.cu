@@ -64,13 +64,13 @@ __global__ void k_wind_init_xi(const double *V, double *xi, double *tr, const Pa
 }
 
 __global__ void k_blondin(double *V, const double *xi_s, const double *tr_s, const Params p,
-                          const WindParams w, const double *x1, Scalars *sc)
+                          const WindParams w, const double *x1, Scalars *sc, const double *pre)
 {
   if (sc->done) return;
   const double dt = sc->dt, t = sc->t;
   const int n = p.nx[0] * p.nx[1];
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
-    blondin_cell(V, xi_s, tr_s, p, w, x1, sc, dt, t, q);
+    blondin_cell(V, xi_s, tr_s, p, w, x1, sc, dt, t, q, pre);
 }
 
 template <int NV, int LIM, int SOLVER, int STAGE>
@@ -130,6 +130,7 @@ void ps_wind_free(ps::WindDev *w)
   cudaFree(w->off);
   cudaFree(w->ent);
   cudaFree(w->dvds);
+  cudaFree(w->pre);
   cudaFree(w->xi);
   cudaFree(w->tr);
   delete w;
@@ -470,7 +471,8 @@ int ps_wind_cool_launch(ps_ctx *c)
   if (!p.cooling) return 0;
   if (c->sg) return ps_sg_cool_launch(c);
   const int nb = (p.nx[0] * p.nx[1] + 127) / 128;
-  ps::k_blondin<<<nb, 128, 0, c->stream>>>(c->V, w->xi, w->tr, p, w->a.w, w->a.g.x1, c->sc);
+  ps::k_blondin<<<nb, 128, 0, c->stream>>>(c->V, w->xi, w->tr, p, w->a.w, w->a.g.x1, c->sc,
+                                           w->pre);
   c->launches++;
   return 0;
 }
@@ -485,4 +487,45 @@ int ps_wind_step_launches(ps_ctx *c, int odd, int (*finish)(ps_ctx *, int))
   if (!r && !odd) r = ps_wind_cool_launch(c);
   if (!r) r = finish(c, 1);
   return r;
+}
+
+// read_sirocco_heatcool with flag 1 (Src/LineDriven/line_connect.c:267-497):
+// per-cell xi and radiation temperature (used by BLONDIN once g_time > 3)
+// and the prefactors of the five rates.  Arrays are [j][i] over the total
+// box (the prefactors: six such arrays in the file's order comp_h, comp_c,
+// xray_h, brem_c, line_c, xi_ion; xi_ion is not used by BLONDIN).  A NULL
+// argument leaves that part as it is; ps_set_wind starts from xi and T_x
+// of the initial state and prefactors 1.
+void ps_ctx_invalidate_graphs(ps_ctx *c);
+
+extern "C" int ps_set_sirocco(ps_ctx *c, const double *xi, const double *t_r, const double *pre)
+{
+  if (!c || !c->wind) return wind_fail("ps_set_sirocco: needs ps_set_wind first");
+  WindDev *w = c->wind;
+  const ps::Params &p = c->p;
+  const int n0 = p.ntot[0], n1 = p.ntot[1];
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return wind_cuda(e, "ps_set_sirocco");
+  auto upload = [&](const double *src, double *dst) -> cudaError_t {
+    // host [j][i] rows of n0 -> device rows of px
+    return cudaMemcpy2D(dst, (size_t)p.px * sizeof(double), src, (size_t)n0 * sizeof(double),
+                        (size_t)n0 * sizeof(double), (size_t)n1, cudaMemcpyHostToDevice);
+  };
+  if (xi && (e = upload(xi, w->xi)) != cudaSuccess) return wind_cuda(e, "ps_set_sirocco: xi");
+  if (t_r && (e = upload(t_r, w->tr)) != cudaSuccess) return wind_cuda(e, "ps_set_sirocco: t_r");
+  if (pre) {
+    if (!w->pre) {
+      if ((e = cudaMalloc(&w->pre, 5 * (size_t)p.vstride * sizeof(double))) != cudaSuccess)
+        return wind_cuda(e, "ps_set_sirocco: prefactors");
+      cudaMemset(w->pre, 0, 5 * (size_t)p.vstride * sizeof(double));
+    }
+    const size_t plane = (size_t)n0 * n1;
+    // file order comp_h, comp_c, xray_h, brem_c, line_c -> device order ch, cc, xh, lc, bc
+    const int src_of[5] = {0, 1, 2, 4, 3};
+    for (int k = 0; k < 5; k++)
+      if ((e = upload(pre + src_of[k] * plane, w->pre + (size_t)k * p.vstride)) != cudaSuccess)
+        return wind_cuda(e, "ps_set_sirocco: prefactors");
+  }
+  ps_ctx_invalidate_graphs(c);
+  return 0;
 }

@@ -31,6 +31,7 @@ struct WindDev {
   double *ent = nullptr; // Fr, Ft, fr1, fr2, c1a, c1b, c2a, c2b, inv_ds (SoA, nent each)
   double *dvds = nullptr; // per-entry stage values (LineList::lq)
   double *xi = nullptr, *tr = nullptr;
+  double *pre = nullptr;  // 5 prefactor arrays (ch, cc, xh, lc, bc), NULL: all 1
   long nent = 0;
   const void *k1 = nullptr, *k2 = nullptr;
   size_t smem = 0;
@@ -222,11 +223,19 @@ __device__ __forceinline__ void init_xi_cell(const double *V, double *xi, double
 __device__ __forceinline__ bool blondin_ctx(const double *V, const double *xi_s, const double *tr_s,
                                             const Params &p, const WindParams &w,
                                             const double *x1, double dt, double t, long long q,
-                                            BlCtx &b, double &T, long long &c)
+                                            BlCtx &b, double &T, long long &c,
+                                            const double *pre = nullptr)
 {
   int gi, gj, gk;
   cell_of(p, q, gi, gj, gk);
   c = vcell3(p, gk, gj, gi);
+  if (pre) {
+    b.ch = pre[c];
+    b.cc = pre[p.vstride + c];
+    b.xh = pre[2 * p.vstride + c];
+    b.lc = pre[3 * p.vstride + c];
+    b.bc = pre[4 * p.vstride + c];
+  }
   b.dt_share = dt * w.unit_time;
   const double rho = V[RHO * p.vstride + c] * w.unit_density;
   const double pr = V[PRS * p.vstride + c];
@@ -260,12 +269,12 @@ __device__ __forceinline__ void blondin_store(double *V, const Params &p, const 
 __device__ __forceinline__ void blondin_cell(double *V, const double *xi_s, const double *tr_s,
                                              const Params &p, const WindParams &w,
                                              const double *x1, Scalars *sc, double dt, double t,
-                                             long long q)
+                                             long long q, const double *pre = nullptr)
 {
   BlCtx b;
   double T;
   long long c;
-  if (!blondin_ctx(V, xi_s, tr_s, p, w, x1, dt, t, q, b, T, c)) return;
+  if (!blondin_ctx(V, xi_s, tr_s, p, w, x1, dt, t, q, b, T, c, pre)) return;
   bl_prepare(b, T);
   bool overflow;
   const double T_f = bl_solve(b, T, overflow);

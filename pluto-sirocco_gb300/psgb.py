@@ -33,7 +33,8 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_sg_create", "ps_sg_destroy", "ps_sg_set_params", "ps_sg_get_params",
            "ps_sg_label", "ps_sg_set_data", "ps_sg_train", "ps_sg_grad", "ps_sg_predict",
            "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect",
-           "ps_set_cooling", "ps_write_dbl", "ps_read_dbl"]
+           "ps_set_cooling", "ps_write_dbl", "ps_read_dbl", "ps_read_sirocco_fluxes",
+           "ps_read_sirocco_heatcool", "ps_read_sirocco_prefactors", "ps_set_sirocco"]
 
 
 class Config(ctypes.Structure):
@@ -155,6 +156,12 @@ def lib():
         L.ps_set_cooling.argtypes = [P, ctypes.POINTER(Cooling)]
         L.ps_write_dbl.argtypes = [P, ctypes.c_char_p, I, ctypes.c_char_p]
         L.ps_read_dbl.argtypes = [P, ctypes.c_char_p]
+        CP = ctypes.POINTER(Config)
+        LP = ctypes.POINTER(ctypes.c_long)
+        L.ps_read_sirocco_fluxes.argtypes = [CP, D, DP, DP, ctypes.c_char_p, I, DP, DP, DP, LP]
+        L.ps_read_sirocco_heatcool.argtypes = [CP, D, DP, DP, ctypes.c_char_p, DP, DP, LP]
+        L.ps_read_sirocco_prefactors.argtypes = [CP, D, DP, DP, ctypes.c_char_p, DP, LP]
+        L.ps_set_sirocco.argtypes = [P, DP, DP, DP]
         _lib = L
     return _lib
 
@@ -373,6 +380,13 @@ class Solver:
 
     def read_dbl(self, path):
         check(lib().ps_read_dbl(self.ctx, os.fsencode(path)), "ps_read_dbl")
+
+    def set_sirocco(self, xi=None, t_r=None, pre=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (xi, t_r, pre)]
+        self._sirocco = arrs
+        check(lib().ps_set_sirocco(self.ctx, *[None if a is None else _dp(a) for a in arrs]),
+              "ps_set_sirocco")
 
     def set_cooling(self, cooling):
         check(lib().ps_set_cooling(self.ctx, ctypes.byref(cooling)), "ps_set_cooling")
@@ -691,3 +705,35 @@ def train_surrogate(wind_tuples, n_draws=500000, steps=20000, batch=8192, seed=3
     sg.set_data(tup, lab)
     hist, _ = sg.train(steps, batch=batch, seed=seed)
     return sg, hist, tup, lab
+
+
+# ----------------------------------------------------------------------
+# SIROCCO files
+# ----------------------------------------------------------------------
+
+def read_sirocco_fluxes(cfg, grid, directory, unit_length=1e9, max_angles=64):
+    """(fr, ft, fp, matched): [angle][1][j][i] arrays over the total box."""
+    n0, n1 = cfg.nx[0] + 4, cfg.nx[1] + 4
+    arr = [np.zeros((max_angles, 1, n1, n0)) for _ in range(3)]
+    m = ctypes.c_long()
+    na = check(lib().ps_read_sirocco_fluxes(ctypes.byref(cfg), unit_length, _dp(grid.x(0)),
+                                            _dp(grid.x(1)), os.fsencode(directory), max_angles,
+                                            *[_dp(a) for a in arr], ctypes.byref(m)),
+               "ps_read_sirocco_fluxes")
+    return arr[0][:na].copy(), arr[1][:na].copy(), arr[2][:na].copy(), m.value
+
+
+def read_sirocco_heatcool(cfg, grid, path, xi, t_r, unit_length=1e9):
+    m = ctypes.c_long()
+    check(lib().ps_read_sirocco_heatcool(ctypes.byref(cfg), unit_length, _dp(grid.x(0)),
+                                         _dp(grid.x(1)), os.fsencode(path), _dp(xi), _dp(t_r),
+                                         ctypes.byref(m)), "ps_read_sirocco_heatcool")
+    return m.value
+
+
+def read_sirocco_prefactors(cfg, grid, path, pre, unit_length=1e9):
+    m = ctypes.c_long()
+    check(lib().ps_read_sirocco_prefactors(ctypes.byref(cfg), unit_length, _dp(grid.x(0)),
+                                           _dp(grid.x(1)), os.fsencode(path), _dp(pre),
+                                           ctypes.byref(m)), "ps_read_sirocco_prefactors")
+    return m.value
