@@ -69,7 +69,9 @@ typedef struct ps_config {
   double tstop;        /* [Time] tstop                                        */
   double first_dt;     /* [Time] first_dt                                     */
   int    cooling;      /* COOLING != NO: dt is recomputed after odd steps only */
-  int    reserved;
+  int    char_limiting; /* CHAR_LIMITING YES: PLM on characteristic variables
+                           (Src/States/plm_states.c:481-746; spherical
+                           contexts)                                      */
 } ps_config;
 
 typedef struct ps_ctx ps_ctx;

@@ -733,6 +733,70 @@ static inline double limit_general(int lim, double dvp, double dvm, double cp, d
   return dv;
 }
 
+/* PLM on characteristic variables for one cell (plm_states.c:481-746, the
+ * CHAR_LIMITING == YES States(), HD with an energy equation): primitive
+ * eigenvectors (HD/eigenv.c:92-240, PrimEigenvectors), projection of the
+ * one-sided differences (eigenv.c:575-617, PrimToChar), limiting of each
+ * characteristic difference, back-projection, the monotonicity bound in
+ * primitive variables, and the passive scalars limited as primitives.
+ * dR = v[i+1]-v[i], dL = v[i]-v[i-1]; general grid weights or the uniform
+ * Cartesian ones (cp = cm = 2, wp = wm = 1, dp = dm = 1/2). */
+static void char_states(int nvar, int d, int lim, int general, double gam, const double *v,
+                        const double *dR, const double *dL, double cp, double cm, double wp,
+                        double wm, double dp, double dm, double *vp, double *vm)
+{
+  const int nflx = 5, vn = VX1 + d;
+  const int vt = d == 0 ? VX2 : (d == 1 ? VX3 : VX1);
+  const int vb = d == 0 ? VX3 : (d == 1 ? VX1 : VX2);
+  double L[5][8], Rm[8][5], dvp[8], dvm[8], dwp[8], dwm[8], dwl[8], dvl[8];
+  int k, nv;
+  double cs2, cs, rhocs, rho_cs;
+  memset(L, 0, sizeof(L));
+  memset(Rm, 0, sizeof(Rm));
+  cs2 = gam * v[PRS] / v[RHO];             /* SoundSpeed2, IDEAL (eos.c:16-42) */
+  cs = sqrt(cs2);
+  rhocs = v[RHO] * cs;
+  rho_cs = v[RHO] / cs;
+  Rm[RHO][0] = 0.5 * rho_cs;  Rm[vn][0] = -0.5;  Rm[PRS][0] = 0.5 * rhocs;
+  Rm[RHO][1] = 0.5 * rho_cs;  Rm[vn][1] = 0.5;   Rm[PRS][1] = 0.5 * rhocs;
+  Rm[RHO][2] = 1.0;  Rm[vt][3] = 1.0;  Rm[vb][4] = 1.0;
+  L[0][vn] = -1.0;  L[0][PRS] = 1.0 / rhocs;
+  L[1][vn] = 1.0;   L[1][PRS] = 1.0 / rhocs;
+  L[2][RHO] = 1.0;  L[3][vt] = 1.0;  L[4][vb] = 1.0;
+  L[2][PRS] = -1.0 / cs2;
+  for (nv = 0; nv < nvar; nv++) {
+    dvp[nv] = general ? dR[nv] * wp : dR[nv];
+    dvm[nv] = general ? dL[nv] * wm : dL[nv];
+  }
+  /* PrimToChar */
+  dwm[0] = L[0][vn] * dvm[vn] + L[0][PRS] * dvm[PRS];
+  dwm[1] = L[1][vn] * dvm[vn] + L[1][PRS] * dvm[PRS];
+  dwm[2] = dvm[RHO] + L[2][PRS] * dvm[PRS];
+  dwm[3] = dvm[vt];
+  dwm[4] = dvm[vb];
+  dwp[0] = L[0][vn] * dvp[vn] + L[0][PRS] * dvp[PRS];
+  dwp[1] = L[1][vn] * dvp[vn] + L[1][PRS] * dvp[PRS];
+  dwp[2] = dvp[RHO] + L[2][PRS] * dvp[PRS];
+  dwp[3] = dvp[vt];
+  dwp[4] = dvp[vb];
+  for (k = nflx; k--;)
+    dwl[k] = general ? limit_general(lim, dwp[k], dwm[k], cp, cm) : limit(lim, dwp[k], dwm[k]);
+  for (nv = nflx; nv--;) {
+    double dc = 0.0;
+    for (k = 0; k < nflx; k++) dc += dwl[k] * Rm[nv][k];
+    if (dvp[nv] * dvm[nv] > 0.0) {
+      double d2v = ABS_MIN(cp * dvp[nv], cm * dvm[nv]);
+      dvl[nv] = (d2v * dc > 0.0 ? (fabs(d2v) < fabs(dc) ? d2v : dc) : 0.0);
+    } else dvl[nv] = 0.0;
+  }
+  for (nv = nflx; nv < nvar; nv++)
+    dvl[nv] = general ? limit_general(lim, dvp[nv], dvm[nv], cp, cm) : limit(lim, dvp[nv], dvm[nv]);
+  for (nv = nvar; nv--;) {
+    vp[nv] = v[nv] + dvl[nv] * dp;
+    vm[nv] = v[nv] - dvl[nv] * dm;
+  }
+}
+
 /* ------------------------------------------------------------------ */
 /* line force (Src/LineDriven/line_connect.c)                         */
 /* ------------------------------------------------------------------ */
@@ -978,7 +1042,14 @@ static void row_sweep(or_sim *s, int d, int k0, int j0, int i0, int stage,
   for (i = beg - 1; i <= end; i++)
     for (nv = 0; nv < nvar; nv++) R(dvv, i, nv) = R(v, i + 1, nv) - R(v, i, nv);
   for (i = beg; i <= end; i++) {
-    if (s->c.geometry == OR_CARTESIAN) {
+    if (s->c.char_limiting) {
+      const int general = s->c.geometry != OR_CARTESIAN;
+      char_states(nvar, d, s->c.limiter, general, gam, &R(v, i, 0), &R(dvv, i, 0),
+                  &R(dvv, i - 1, 0), general ? s->pcp[d][i] : 2.0, general ? s->pcm[d][i] : 2.0,
+                  general ? s->pwp[d][i] : 1.0, general ? s->pwm[d][i] : 1.0,
+                  general ? s->pdp[d][i] : 0.5, general ? s->pdm[d][i] : 0.5, &R(vp, i, 0),
+                  &R(vm, i, 0));
+    } else if (s->c.geometry == OR_CARTESIAN) {
       for (nv = 0; nv < nvar; nv++) {
         double dvp = R(dvv, i, nv), dvm = R(dvv, i - 1, nv);
         double dvl = limit(s->c.limiter, dvp, dvm);

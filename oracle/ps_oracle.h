@@ -53,6 +53,9 @@ typedef struct {
   /* > 0: BLONDIN at this constant ionisation parameter with t_x (the
    * Cartesian cooling configuration) instead of xi from the state */
   double xi_const;
+  /* CHAR_LIMITING YES: PLM limited on the characteristic variables of the
+   * primitive HD system (Src/States/plm_states.c:481-746) */
+  int    char_limiting;
 } or_config;
 
 typedef struct or_sim or_sim;

@@ -198,6 +198,10 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
       return PS_EINVAL;
     }
   }
+  if (cfg->char_limiting && !sph) {
+    ps_set_error_msg("ps_create: characteristic limiting is built for the spherical wind path");
+    return PS_EINVAL;
+  }
   for (int s = 0; s < 2 * cfg->dims; s++) {
     int b = cfg->bc[s];
     const bool userdef_ok = sph && s == 0 && b == PS_BC_USERDEF;
@@ -221,6 +225,7 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   p.limiter = cfg->limiter;
   p.solver = cfg->solver;
   p.cooling = cfg->cooling;
+  p.char_lim = cfg->char_limiting ? 1 : 0;
   for (int d = 0; d < 3; d++) {
     p.nx[d] = cfg->nx[d];
     p.beg[d] = d < cfg->dims ? 2 : 0;

@@ -61,6 +61,58 @@ __device__ __forceinline__ double limited_slope_general(double dvp, double dvm, 
   }
 }
 
+// Limited slopes on characteristic variables (CHAR_LIMITING YES,
+// Src/States/plm_states.c:481-746, HD with energy, general grid): the
+// one-sided differences projected on the left primitive eigenvectors
+// (HD/eigenv.c:92-240, PrimEigenvectors; eigenv.c:575-617, PrimToChar),
+// each characteristic difference limited, projected back on the right
+// eigenvectors, bounded by ABS_MIN(cp dvp, cm dvm) in primitive variables
+// (minmod), passive scalars limited as primitives.  D selects the normal
+// velocity (tangential ones: x1 sweep VX2, VX3; x2 sweep VX3, VX1).
+template <int D, int NV, int LIM>
+__device__ __forceinline__ void char_slopes(const double (&v)[NV], const double (&dvp)[NV],
+                                            const double (&dvm)[NV], double cp, double cm,
+                                            double gam, double (&dv)[NV])
+{
+  constexpr int vn = VX1 + D, vt = D == 0 ? VX2 : VX3, vb = D == 0 ? VX3 : VX1;
+  const double cs2 = gam * v[PRS] / v[RHO];
+  const double cs = sqrt(cs2);
+  const double rhocs = v[RHO] * cs, rho_cs = v[RHO] / cs;
+  const double l0p = 1.0 / rhocs, l2p = -1.0 / cs2;
+  double wp[5], wm[5], wl[5];
+  wm[0] = -1.0 * dvm[vn] + l0p * dvm[PRS];
+  wm[1] = 1.0 * dvm[vn] + l0p * dvm[PRS];
+  wm[2] = dvm[RHO] + l2p * dvm[PRS];
+  wm[3] = dvm[vt];
+  wm[4] = dvm[vb];
+  wp[0] = -1.0 * dvp[vn] + l0p * dvp[PRS];
+  wp[1] = 1.0 * dvp[vn] + l0p * dvp[PRS];
+  wp[2] = dvp[RHO] + l2p * dvp[PRS];
+  wp[3] = dvp[vt];
+  wp[4] = dvp[vb];
+#pragma unroll
+  for (int k = 0; k < 5; k++) wl[k] = limited_slope_general<LIM>(wp[k], wm[k], cp, cm);
+  // dc = sum_k wl[k] R[nv][k] with the nonzero entries of the right
+  // eigenvectors, in the order of k
+  double dc[5];
+  dc[RHO] = ((0.0 + wl[0] * (0.5 * rho_cs)) + wl[1] * (0.5 * rho_cs)) + wl[2] * 1.0;
+  dc[vn] = (0.0 + wl[0] * -0.5) + wl[1] * 0.5;
+  dc[PRS] = (0.0 + wl[0] * (0.5 * rhocs)) + wl[1] * (0.5 * rhocs);
+  dc[vt] = 0.0 + wl[3] * 1.0;
+  dc[vb] = 0.0 + wl[4] * 1.0;
+#pragma unroll
+  for (int nv = 0; nv < 5; nv++) {
+    if (dvp[nv] * dvm[nv] > 0.0) {
+      const double d2v = abs_min(cp * dvp[nv], cm * dvm[nv]);
+      dv[nv] = d2v * dc[nv] > 0.0 ? (fabs(d2v) < fabs(dc[nv]) ? d2v : dc[nv]) : 0.0;
+    } else {
+      dv[nv] = 0.0;
+    }
+  }
+#pragma unroll
+  for (int nv = 5; nv < NV; nv++) dv[nv] = limited_slope_general<LIM>(dvp[nv], dvm[nv], cp, cm);
+}
+
 __device__ __forceinline__ long long vcell(const Params &p, int gj, int gi)
 {
   return (long long)gj * p.px + gi;
@@ -339,7 +391,8 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
   const SphGeom &g = A.g;
   const double gam = p.gamma, gmm1 = p.gmm1;
 
-  // (1) PLM with the general-grid weights of the cell
+  // (1) PLM with the general-grid weights of the cell, on the primitive or
+  // (CHAR_LIMITING) the characteristic variables
   for (int q = threadIdx.x; q < NP; q += G::NT) {
     const int ix = q % PX, iy = q / PX;
     const int sx = ix + TL::HX - (D == 0), sy = iy + TL::HY - (D == 1);
@@ -349,6 +402,22 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
     const int gc = min(D == 0 ? p.beg[0] + ox + ix - 1 : p.beg[1] + oy + iy - 1, p.ntot[D] - 1);
     const double cp = g.cp[D][gc], cm = g.cm[D][gc], wp = g.wp[D][gc], wm = g.wm[D][gc];
     const double dp = g.dp[D][gc], dm = g.dm[D][gc];
+    if (p.char_lim) {
+      double v0[NV], dvp[NV], dvm[NV], dv[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        v0[nv] = sv[nv * G::VS + s0];
+        dvp[nv] = (sv[nv * G::VS + s0 + SST] - v0[nv]) * wp;
+        dvm[nv] = (v0[nv] - sv[nv * G::VS + s0 - SST]) * wm;
+      }
+      char_slopes<D, NV, LIM>(v0, dvp, dvm, cp, cm, gam, dv);
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        svp[nv * G::NPMAX + q] = v0[nv] + dv[nv] * dp;
+        svm[nv * G::NPMAX + q] = v0[nv] - dv[nv] * dm;
+      }
+      continue;
+    }
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       const double vm1 = sv[nv * G::VS + s0 - SST], v0 = sv[nv * G::VS + s0],

@@ -16,9 +16,9 @@ from conftest import assert_hydro_close, golden_cases
 pytestmark = pytest.mark.gpu
 
 
-def _wind_solver(nr, nt, cooling, line_force):
+def _wind_solver(nr, nt, cooling, line_force, char_limiting=0):
     import psgb
-    cfg = psgb.make_wind_config(nr, nt, cooling=cooling)
+    cfg = psgb.make_wind_config(nr, nt, cooling=cooling, char_limiting=char_limiting)
     w = psgb.make_wind(line_force=line_force)
     g = psgb.WindGrid(cfg)
     s = psgb.Solver(cfg, g)
@@ -50,6 +50,25 @@ def test_wind_hydro_matches_reference(built):
         print("step", step, "relative L1 per variable", r)
         t, dt, _, _ = s.time()
         assert abs(t - float(meta["t"][k])) <= 6e-7 * abs(t)
+
+
+def test_wind_char_limiting_matches_reference(built):
+    """CHAR_LIMITING YES (PLM on characteristic variables, as the production
+    cv_idl configuration uses it), hydro part of the wind."""
+    meta = _case("wind2d_char")
+    snaps = np.load(meta["npz"])["snaps"]
+    s = _wind_solver(meta["n"][0], meta["n"][1], cooling=0, line_force=0, char_limiting=1)
+    done = 0
+    for k, step in enumerate(meta["snap_steps"]):
+        if step > done:
+            s.run(step - done)
+            done = step
+        r = assert_hydro_close(_active(s.get_state()), snaps[k], f"step {step}")
+        print("char limiting, step", step, "relative L1 per variable", r)
+    # and it is not the primitive-variable limiter
+    h = _wind_solver(meta["n"][0], meta["n"][1], cooling=0, line_force=0)
+    h.run(meta["snap_steps"][-1])
+    assert not np.allclose(_active(h.get_state()), snaps[-1], rtol=1e-6)
 
 
 def _rel_l1(a, b):

@@ -61,7 +61,8 @@ def test_wind_oracle_matches_reference(built, meta):
     from oracle import wind_oracle
     snaps = np.load(meta["npz"])["snaps"]
     nr, nt = meta["n"][0], meta["n"][1]
-    o = wind_oracle(nr, nt, cooling=meta["cooling"], line_force=meta["line_force"])
+    o = wind_oracle(nr, nt, cooling=meta["cooling"], line_force=meta["line_force"],
+                    char_limiting=meta.get("char_limiting", 0))
     done = 0
     for k, step in enumerate(meta["snap_steps"]):
         if step > done:
