@@ -72,6 +72,9 @@ typedef struct ps_config {
   int    char_limiting; /* CHAR_LIMITING YES: PLM on characteristic variables
                            (Src/States/plm_states.c:481-746; spherical
                            contexts)                                      */
+  int    shock_flattening; /* SHOCK_FLATTENING MULTID: minmod reconstruction
+                           in and next to shocked zones (Src/flag_shock.c:
+                           81-250; spherical contexts, not in batches)    */
 } ps_config;
 
 typedef struct ps_ctx ps_ctx;

@@ -35,7 +35,7 @@ class OrConfig(ctypes.Structure):
                 ("f_x", ctypes.c_double), ("f_uv", ctypes.c_double), ("t_x", ctypes.c_double),
                 ("krad", ctypes.c_double), ("alpharad", ctypes.c_double),
                 ("dfloor", ctypes.c_double), ("xi_const", ctypes.c_double),
-                ("char_limiting", ctypes.c_int)]
+                ("char_limiting", ctypes.c_int), ("shock_flattening", ctypes.c_int)]
 
 
 _lib = None
@@ -110,7 +110,7 @@ class Oracle:
                  bc="outflow", gamma=5.0 / 3.0, cfl=0.4, cfl_max_var=1.1, tstop=10.0,
                  first_dt=1e-4, cooling=0, geometry=0, gridtype=("uniform",) * 3,
                  xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), body_force=0, line_force=0,
-                 floors=0, params=None, char_limiting=0):
+                 floors=0, params=None, char_limiting=0, shock_flattening=0):
         c = OrConfig()
         c.dims = dims
         n = list(nx) + [1] * (3 - len(nx))
@@ -133,6 +133,7 @@ class Oracle:
         c.cooling = cooling
         c.body_force, c.line_force, c.floors = body_force, line_force, floors
         c.char_limiting = char_limiting
+        c.shock_flattening = shock_flattening
         for k, v in (params or {}).items():
             setattr(c, k, v)
         self.cfg = c
@@ -207,7 +208,7 @@ class Oracle:
 
 
 def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, char_limiting=0,
-                **params):
+                shock_flattening=0, **params):
     """The 2-D spherical line-driven disk wind (PLM van Leer, HLL, RK2,
     userdef/outflow/axisymmetric/reflective boundaries, point-mass gravity,
     floors, BLONDIN cooling and the line force), initialised."""
@@ -216,7 +217,8 @@ def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, c
                cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling,
                geometry=3, gridtype=WIND_GRID["gridtype"], xbeg=WIND_GRID["xbeg"],
                xend=WIND_GRID["xend"], body_force=1, line_force=line_force, floors=1,
-               params=dict(WIND, **params), char_limiting=char_limiting)
+               params=dict(WIND, **params), char_limiting=char_limiting,
+               shock_flattening=shock_flattening)
     if line_force:
         prm = dict(WIND, **params)
         o.set_flux(*synthetic_flux(o.grid(0), o.grid(1), o.ntot,

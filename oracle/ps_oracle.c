@@ -46,6 +46,7 @@
 
 #define MAXD(a, b) ((a) >= (b) ? (a) : (b))
 #define MIND(a, b) ((a) <= (b) ? (a) : (b))
+#define OR_FLAG_MINMOD 1   /* FLAG_MINMOD (Src/pluto.h:212) */
 #define ABS_MIN(a, b) (fabs(a) < fabs(b) ? (a) : (b))
 
 static const double small_density = 1.e-12;
@@ -83,6 +84,7 @@ struct or_sim {
   double *Fr, *Ft, *Fp;            /* [a][k][j][i] */
   double *xi_s, *tr_s;             /* sirocco_xi, sirocco_t_r */
   double *pre;                     /* 6 prefactor arrays (file order) or NULL: all 1 */
+  unsigned char *flag;             /* FLAG_MINMOD bits of FlagShock, [k][j][i] */
   double *dvds, *roff, *toff, *moff; /* [a][k][j][i] */
   double *x11[2], *x22[2];
   int dvds_ready;
@@ -275,6 +277,7 @@ or_sim *or_create(const or_config *cfg)
 #undef ROW1
   s->rvc = calloc((size_t)(nmax + 2) * NVMAX, sizeof(double));
   build_geometry(s);
+  s->flag = calloc(ncell, 1);
   s->xi_s = calloc(ncell, sizeof(double));
   s->tr_s = calloc(ncell, sizeof(double));
   s->g_time = 0.0;
@@ -298,6 +301,7 @@ void or_destroy(or_sim *s)
   free(s->rt); free(s->sp); free(s->sn); free(s->dmu); free(s->dVr);
   free(s->dV); free(s->Ax1); free(s->Ax2); free(s->rvc);
   free(s->Fr); free(s->Ft); free(s->Fp); free(s->xi_s); free(s->tr_s); free(s->pre);
+  free(s->flag);
   free(s->dvds); free(s->roff); free(s->toff); free(s->moff);
   free(s->x11[0]); free(s->x11[1]); free(s->x22[0]); free(s->x22[1]);
   free(s->V); free(s->U); free(s->U0); free(s->Cdt);
@@ -743,7 +747,7 @@ static inline double limit_general(int lim, double dvp, double dvm, double cp, d
  * Cartesian ones (cp = cm = 2, wp = wm = 1, dp = dm = 1/2). */
 static void char_states(int nvar, int d, int lim, int general, double gam, const double *v,
                         const double *dR, const double *dL, double cp, double cm, double wp,
-                        double wm, double dp, double dm, double *vp, double *vm)
+                        double wm, double dp, double dm, int minmod, double *vp, double *vm)
 {
   const int nflx = 5, vn = VX1 + d;
   const int vt = d == 0 ? VX2 : (d == 1 ? VX3 : VX1);
@@ -779,8 +783,12 @@ static void char_states(int nvar, int d, int lim, int general, double gam, const
   dwp[2] = dvp[RHO] + L[2][PRS] * dvp[PRS];
   dwp[3] = dvp[vt];
   dwp[4] = dvp[vb];
-  for (k = nflx; k--;)
-    dwl[k] = general ? limit_general(lim, dwp[k], dwm[k], cp, cm) : limit(lim, dwp[k], dwm[k]);
+  for (k = nflx; k--;) {
+    if (minmod)   /* SHOCK_FLATTENING MULTID, FLAG_MINMOD (plm_states.c:617-620) */
+      dwl[k] = (dwp[k] * dwm[k] > 0.0 ? ABS_MIN(dwp[k], dwm[k]) : 0.0);
+    else
+      dwl[k] = general ? limit_general(lim, dwp[k], dwm[k], cp, cm) : limit(lim, dwp[k], dwm[k]);
+  }
   for (nv = nflx; nv--;) {
     double dc = 0.0;
     for (k = 0; k < nflx; k++) dc += dwl[k] * Rm[nv][k];
@@ -1042,13 +1050,25 @@ static void row_sweep(or_sim *s, int d, int k0, int j0, int i0, int stage,
   for (i = beg - 1; i <= end; i++)
     for (nv = 0; nv < nvar; nv++) R(dvv, i, nv) = R(v, i + 1, nv) - R(v, i, nv);
   for (i = beg; i <= end; i++) {
+    const int minmod = s->c.shock_flattening && (s->flag[base + i * stride] & OR_FLAG_MINMOD);
     if (s->c.char_limiting) {
       const int general = s->c.geometry != OR_CARTESIAN;
       char_states(nvar, d, s->c.limiter, general, gam, &R(v, i, 0), &R(dvv, i, 0),
                   &R(dvv, i - 1, 0), general ? s->pcp[d][i] : 2.0, general ? s->pcm[d][i] : 2.0,
                   general ? s->pwp[d][i] : 1.0, general ? s->pwm[d][i] : 1.0,
-                  general ? s->pdp[d][i] : 0.5, general ? s->pdm[d][i] : 0.5, &R(vp, i, 0),
-                  &R(vm, i, 0));
+                  general ? s->pdp[d][i] : 0.5, general ? s->pdm[d][i] : 0.5, minmod,
+                  &R(vp, i, 0), &R(vm, i, 0));
+    } else if (minmod) {   /* plm_states.c:176-193 */
+      const int general = s->c.geometry != OR_CARTESIAN;
+      double wp = general ? s->pwp[d][i] : 1.0, wm = general ? s->pwm[d][i] : 1.0;
+      double dp = general ? s->pdp[d][i] : 0.5, dm = general ? s->pdm[d][i] : 0.5;
+      for (nv = 0; nv < nvar; nv++) {
+        double dvp = general ? R(dvv, i, nv) * wp : R(dvv, i, nv);
+        double dvm = general ? R(dvv, i - 1, nv) * wm : R(dvv, i - 1, nv);
+        double dvl = (dvp * dvm > 0.0 ? ABS_MIN(dvp, dvm) : 0.0);
+        R(vp, i, nv) = R(v, i, nv) + dvl * dp;
+        R(vm, i, nv) = R(v, i, nv) - dvl * dm;
+      }
     } else if (s->c.geometry == OR_CARTESIAN) {
       for (nv = 0; nv < nvar; nv++) {
         double dvp = R(dvv, i, nv), dvm = R(dvv, i - 1, nv);
@@ -1453,11 +1473,69 @@ double or_blondin_point(double nH, double T, double xi, double tx, double dt_s, 
   return MAXD(T_f, 1.e4);
 }
 
+/* FlagShock with SHOCK_FLATTENING == MULTID (flag_shock.c:81-250): zones
+ * with div v < 0 and a pressure jump sum_d |p_{+1} - p_{-1}| above
+ * 5 min(p, neighbours) are shocked; they and their neighbours in every
+ * active direction get FLAG_MINMOD.  Flags start from zero every step
+ * (main.c:260). */
+static void flag_shock(or_sim *s)
+{
+  int i, j, k;
+  int n0 = s->ntot[0], n1 = s->ntot[1], n2 = s->ntot[2];
+  int ik = s->c.dims == 3, ij = s->c.dims >= 2;
+  size_t nc = (size_t)n0 * n1 * n2, sx = 1, sy = n0, sz = (size_t)n0 * n1;
+  const double *vx1 = s->V + VX1 * nc, *vx2 = s->V + VX2 * nc, *vx3 = s->V + VX3 * nc;
+  const double *pt = s->V + PRS * nc;
+  memset(s->flag, 0, nc);
+  for (k = ik; k < n2 - ik; k++)
+  for (j = ij; j < n1 - ij; j++)
+  for (i = 1; i < n0 - 1; i++) {
+    size_t c = cidx(s, k, j, i);
+    double divv, dvx1, dvx2 = 0.0, dvx3 = 0.0, pt_min, gradp;
+    if (s->c.geometry == OR_CARTESIAN) {
+      dvx1 = (vx1[c + sx] - vx1[c - sx]) / s->dx[0][i];
+      if (ij) dvx2 = (vx2[c + sy] - vx2[c - sy]) / s->dx[1][j];
+      if (ik) dvx3 = (vx3[c + sz] - vx3[c - sz]) / s->dx[2][k];
+      divv = s->c.dims == 1 ? dvx1 : (s->c.dims == 2 ? dvx1 + dvx2 : dvx1 + dvx2 + dvx3);
+    } else {
+      double a1p = s->Ax1[((size_t)k * n1 + j) * (n0 + 1) + (i + 1)];
+      double a1m = s->Ax1[((size_t)k * n1 + j) * (n0 + 1) + i];
+      double a2p = s->Ax2[((size_t)k * (n1 + 1) + (j + 1)) * n0 + i];
+      double a2m = s->Ax2[((size_t)k * (n1 + 1) + j) * n0 + i];
+      dvx1 = a1p * (vx1[c + sx] + vx1[c]) - a1m * (vx1[c - sx] + vx1[c]);
+      dvx2 = a2p * (vx2[c + sy] + vx2[c]) - a2m * (vx2[c - sy] + vx2[c]);
+      divv = (dvx1 + dvx2) / s->dV[c];
+    }
+    if (divv < 0.0) {
+      double pmin1, pmin2 = 0.0, pmin3 = 0.0, dpx1, dpx2 = 0.0, dpx3 = 0.0;
+      pt_min = pt[c];
+      pmin1 = MIND(pt[c + sx], pt[c - sx]);
+      if (ij) pmin2 = MIND(pt[c + sy], pt[c - sy]);
+      if (ik) pmin3 = MIND(pt[c + sz], pt[c - sz]);
+      pt_min = MIND(pt_min, pmin1);
+      if (ij) pt_min = MIND(pt_min, pmin2);
+      if (ik) pt_min = MIND(pt_min, pmin3);
+      dpx1 = fabs(pt[c + sx] - pt[c - sx]);
+      if (ij) dpx2 = fabs(pt[c + sy] - pt[c - sy]);
+      if (ik) dpx3 = fabs(pt[c + sz] - pt[c - sz]);
+      gradp = s->c.dims == 1 ? dpx1 : (s->c.dims == 2 ? dpx1 + dpx2 : dpx1 + dpx2 + dpx3);
+      if (gradp > 5.0 * pt_min) {
+        s->flag[c] |= OR_FLAG_MINMOD;
+        s->flag[c + sx] |= OR_FLAG_MINMOD;
+        s->flag[c - sx] |= OR_FLAG_MINMOD;
+        if (ij) { s->flag[c - sy] |= OR_FLAG_MINMOD; s->flag[c + sy] |= OR_FLAG_MINMOD; }
+        if (ik) { s->flag[c - sz] |= OR_FLAG_MINMOD; s->flag[c + sz] |= OR_FLAG_MINMOD; }
+      }
+    }
+  }
+}
+
 /* RK2 AdvanceStep (rk_step.c:29-384) */
 static int advance_step(or_sim *s)
 {
   int i, j, k, nv, nvar = s->c.nvar, flags;
   boundary(s);
+  if (s->c.shock_flattening) flag_shock(s);
   prim_to_cons_dom(s);
   for (k = s->beg[2]; k <= s->end[2]; k++)
   for (j = s->beg[1]; j <= s->end[1]; j++)

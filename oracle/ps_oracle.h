@@ -56,6 +56,9 @@ typedef struct {
   /* CHAR_LIMITING YES: PLM limited on the characteristic variables of the
    * primitive HD system (Src/States/plm_states.c:481-746) */
   int    char_limiting;
+  /* SHOCK_FLATTENING MULTID: minmod reconstruction in and next to shocked
+   * zones (Src/flag_shock.c:81-250, plm_states.c:176-193, 613-625) */
+  int    shock_flattening;
 } or_config;
 
 typedef struct or_sim or_sim;

@@ -198,8 +198,9 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
       return PS_EINVAL;
     }
   }
-  if (cfg->char_limiting && !sph) {
-    ps_set_error_msg("ps_create: characteristic limiting is built for the spherical wind path");
+  if ((cfg->char_limiting || cfg->shock_flattening) && !sph) {
+    ps_set_error_msg("ps_create: characteristic limiting and shock flattening are built for the "
+                     "spherical wind path");
     return PS_EINVAL;
   }
   for (int s = 0; s < 2 * cfg->dims; s++) {
@@ -226,6 +227,7 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   p.solver = cfg->solver;
   p.cooling = cfg->cooling;
   p.char_lim = cfg->char_limiting ? 1 : 0;
+  p.shock = cfg->shock_flattening ? 1 : 0;
   for (int d = 0; d < 3; d++) {
     p.nx[d] = cfg->nx[d];
     p.beg[d] = d < cfg->dims ? 2 : 0;
@@ -576,7 +578,7 @@ static int build_wind_graph(ps_ctx *c, int kind, cudaGraphExec_t *out)
 static int run_wind(ps_ctx *c, int nsteps)
 {
   const int ncool = c->p.cooling ? (c->sg ? 2 : 1) + (c->wind ? 0 : 1) : 0;
-  const long per_step = (c->wind ? 7 : 3) + ncool;
+  const long per_step = (c->wind ? 7 + (c->p.shock ? 1 : 0) : 3) + ncool;
   for (int k = 0; k < 3; k++)
     if (!c->gw[k]) {
       int r = build_wind_graph(c, k, &c->gw[k]);

@@ -78,6 +78,21 @@ __global__ void k_batch_bnd_x2(const BatchModel *__restrict__ models,
     bnd_x2_item<NV>(stage == 1 ? const_cast<double *>(A.s.Vn) : A.s.Vout, A.s.p, q);
 }
 
+// FlagShock of the models with SHOCK_FLATTENING MULTID, before stage 1
+__global__ void k_batch_shock(const BatchModel *__restrict__ models,
+                              const BlockItem *__restrict__ blocks)
+{
+  const BlockItem bi = blocks[blockIdx.x];
+  const WindStageArgs &A = models[bi.m].st[0];
+  if (A.s.sc->done) return;
+  const Params &p = A.s.p;
+  const int q = bi.b * blockDim.x + threadIdx.x;
+  if (q < p.ntot[0] * p.ntot[1]) {
+    const int i = q % p.ntot[0], j = q / p.ntot[0];
+    const_cast<unsigned char *>(A.shock)[vcell(p, j, i)] = shock_zone(A.s.Vn, p, A.g, i, j);
+  }
+}
+
 __global__ void k_batch_blondin(const BatchModel *__restrict__ models,
                                 const BlockItem *__restrict__ blocks, const double *const *xi,
                                 const double *const *tr, const double *const *pre)
@@ -207,6 +222,8 @@ struct ps_batch {
   int nitems[ps::kNumShapes] = {};
   ps::BlockItem *d_cells = nullptr, *d_x2 = nullptr;
   int ncells_blocks = 0, nx2_blocks = 0;
+  ps::BlockItem *d_shock = nullptr;  // total-box blocks of the MULTID models
+  int nshock_blocks = 0;
   const double **d_xi = nullptr, **d_tr = nullptr, **d_pre = nullptr;
   ps::BlockItem *d_cells128 = nullptr;  // 128-cell blocks (surrogate kernel)
   int ncells128 = 0;
@@ -276,7 +293,7 @@ static int encode_box(const ps::Params &p, double *base, int tx, int ty, CUtenso
 static int batch_upload(ps_batch *b)
 {
   std::vector<ps::TileItem> items[ps::kNumShapes];
-  std::vector<ps::BlockItem> cells, x2, cells128;
+  std::vector<ps::BlockItem> cells, x2, cells128, shock;
   b->total_cells = 0;
   for (int m = 0; m < b->n; m++) {
     ps_ctx *c = b->ctx[m];
@@ -317,6 +334,8 @@ static int batch_upload(ps_batch *b)
     for (int k = 0; k < nc128; k++) cells128.push_back({m, k});
     b->total_cells += (long)p.nx[0] * p.nx[1];
     for (int k = 0; k < n2; k++) x2.push_back({m, k});
+    if (p.shock)
+      for (int k = 0; k < (p.ntot[0] * p.ntot[1] + 255) / 256; k++) shock.push_back({m, k});
   }
   BCK(cudaMemcpy(b->d_models, b->h_models.data(), sizeof(ps::BatchModel) * b->n,
                  cudaMemcpyHostToDevice));
@@ -341,6 +360,14 @@ static int batch_upload(ps_batch *b)
   BCK(cudaMemcpy(b->d_cells128, cells128.data(), cells128.size() * sizeof(ps::BlockItem),
                  cudaMemcpyHostToDevice));
   b->ncells128 = (int)cells128.size();
+  cudaFree(b->d_shock);
+  b->d_shock = nullptr;
+  if (!shock.empty()) {
+    BCK(cudaMalloc(&b->d_shock, shock.size() * sizeof(ps::BlockItem)));
+    BCK(cudaMemcpy(b->d_shock, shock.data(), shock.size() * sizeof(ps::BlockItem),
+                   cudaMemcpyHostToDevice));
+  }
+  b->nshock_blocks = (int)shock.size();
   b->ncells_blocks = (int)cells.size();
   b->nx2_blocks = (int)x2.size();
   for (int k = 0; k < 3; k++) {
@@ -380,6 +407,10 @@ static int batch_bnd(ps_batch *b, int stage)
   ps::k_batch_bnd_x1<6><<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, stage);
   ps::k_batch_bnd_x2<6><<<b->nx2_blocks, 256, 0, b->stream>>>(b->d_models, b->d_x2, stage);
   b->launches += 2;
+  if (stage == 1 && b->nshock_blocks) {
+    ps::k_batch_shock<<<b->nshock_blocks, 256, 0, b->stream>>>(b->d_models, b->d_shock);
+    b->launches++;
+  }
   return 0;
 }
 
@@ -436,6 +467,7 @@ static void batch_free(ps_batch *b)
   cudaFree(b->d_tr);
   cudaFree(b->d_pre);
   cudaFree(b->d_cells128);
+  cudaFree(b->d_shock);
   cudaFree(b->sg_queue);
   cudaFree(b->sg_qcount);
   for (int k = 0; k < ps::kNumShapes; k++) {
@@ -637,7 +669,8 @@ extern "C" int ps_batch_run(ps_batch *b, int nsteps)
   if (!b || nsteps < 0) return PS_EINVAL;
   int nshape = 0;
   for (int s = 0; s < ps::kNumShapes; s++) nshape += b->nitems[s] > 0;
-  const long per_step = 4 + 2 * nshape + (b->cooling ? (b->sg ? 2 : 1) : 0) + 1;
+  const long per_step = 4 + 2 * nshape + (b->cooling ? (b->sg ? 2 : 1) : 0) + 1 +
+                        (b->nshock_blocks ? 1 : 0);
   for (int k = 0; k < 3; k++)
     if (!b->g[k]) {
       int r = batch_graph(b, k, &b->g[k]);

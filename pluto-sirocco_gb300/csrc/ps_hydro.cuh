@@ -29,6 +29,7 @@ constexpr int kHist = 4096;  // per-step dt history kept on the device
 struct Params {
   int dims, nvar, limiter, solver, cooling;
   int char_lim;           // PLM on characteristic variables (spherical path)
+  int shock;              // MULTID shock flattening (spherical path)
   int nx[3], ntot[3], beg[3];
   int px;                 // row pitch of device arrays (elements)
   long long vstride;      // elements between variables

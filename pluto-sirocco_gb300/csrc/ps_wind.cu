@@ -55,6 +55,19 @@ __global__ void k_wind_bnd_x2(double *V, const Params p, Scalars *sc)
     bnd_x2_item<NV>(V, p, q);
 }
 
+// FlagShock (Src/flag_shock.c:38-200) at the start of a step: the shocked
+// zones of the total box, read by the PLM of both stages.
+__global__ void k_wind_shock(unsigned char *S, const double *V, const Params p, const SphGeom g,
+                             Scalars *sc)
+{
+  if (sc->done) return;
+  const int n = p.ntot[0] * p.ntot[1];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int i = q % p.ntot[0], j = q / p.ntot[0];
+    S[vcell(p, j, i)] = shock_zone(V, p, g, i, j);
+  }
+}
+
 __global__ void k_wind_init_xi(const double *V, double *xi, double *tr, const Params p,
                                const WindParams w, const double *x1)
 {
@@ -133,6 +146,7 @@ void ps_wind_free(ps::WindDev *w)
   cudaFree(w->pre);
   cudaFree(w->xi);
   cudaFree(w->tr);
+  cudaFree(w->shock);
   delete w;
 }
 
@@ -311,6 +325,11 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   WTRY(cudaMalloc(&w->tr, (size_t)p.vstride * sizeof(double)));
   WTRY(cudaMemset(w->xi, 0, (size_t)p.vstride * sizeof(double)));
   WTRY(cudaMemset(w->tr, 0, (size_t)p.vstride * sizeof(double)));
+  if (p.shock) {
+    WTRY(cudaMalloc(&w->shock, (size_t)p.vstride));
+    WTRY(cudaMemset(w->shock, 0, (size_t)p.vstride));
+  }
+  w->a.shock = w->shock;
   w->nent = nent;
 
   ps::SphGeom &G = w->a.g;
@@ -414,7 +433,8 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   return 0;
 }
 
-// Boundary() before stage `stage` of the wind (floors, x1 then x2 ghosts).
+// Boundary() before stage `stage` of the wind (floors, x1 then x2 ghosts);
+// before stage 1 with SHOCK_FLATTENING MULTID also FlagShock.
 int ps_wind_bnd_launch(ps_ctx *c, int stage)
 {
   WindDev *w = c->wind;
@@ -425,6 +445,11 @@ int ps_wind_bnd_launch(ps_ctx *c, int stage)
   ps::k_wind_bnd_x1<6><<<nb, 256, 0, c->stream>>>(Vin, c->Us, p, w->a.w, c->sc, stage);
   ps::k_wind_bnd_x2<6><<<nb2, 256, 0, c->stream>>>(Vin, p, c->sc);
   c->launches += 2;
+  if (stage == 1 && p.shock) {
+    const int nb3 = (p.ntot[0] * p.ntot[1] + 255) / 256;
+    ps::k_wind_shock<<<nb3, 256, 0, c->stream>>>(w->shock, c->V, p, w->a.g, c->sc);
+    c->launches++;
+  }
   return 0;
 }
 

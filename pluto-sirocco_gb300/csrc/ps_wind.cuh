@@ -71,6 +71,7 @@ struct WindStageArgs {
   SphGeom g;
   LineList L;
   WindParams w;
+  const unsigned char *shock;  // MULTID: 1 where FlagShock finds a shock (total box)
 };
 
 }  // namespace ps

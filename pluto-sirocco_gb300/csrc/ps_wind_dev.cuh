@@ -32,6 +32,7 @@ struct WindDev {
   double *dvds = nullptr; // per-entry stage values (LineList::lq)
   double *xi = nullptr, *tr = nullptr;
   double *pre = nullptr;  // 5 prefactor arrays (ch, cc, xh, lc, bc), NULL: all 1
+  unsigned char *shock = nullptr;  // SHOCK_FLATTENING MULTID: shocked zones, total box
   long nent = 0;
   const void *k1 = nullptr, *k2 = nullptr;
   size_t smem = 0;
@@ -72,7 +73,7 @@ __device__ __forceinline__ double limited_slope_general(double dvp, double dvm, 
 template <int D, int NV, int LIM>
 __device__ __forceinline__ void char_slopes(const double (&v)[NV], const double (&dvp)[NV],
                                             const double (&dvm)[NV], double cp, double cm,
-                                            double gam, double (&dv)[NV])
+                                            double gam, bool minmod, double (&dv)[NV])
 {
   constexpr int vn = VX1 + D, vt = D == 0 ? VX2 : VX3, vb = D == 0 ? VX3 : VX1;
   const double cs2 = gam * v[PRS] / v[RHO];
@@ -91,7 +92,9 @@ __device__ __forceinline__ void char_slopes(const double (&v)[NV], const double 
   wp[3] = dvp[vt];
   wp[4] = dvp[vb];
 #pragma unroll
-  for (int k = 0; k < 5; k++) wl[k] = limited_slope_general<LIM>(wp[k], wm[k], cp, cm);
+  for (int k = 0; k < 5; k++)
+    wl[k] = minmod ? (wp[k] * wm[k] > 0.0 ? abs_min(wp[k], wm[k]) : 0.0)   // FLAG_MINMOD
+                   : limited_slope_general<LIM>(wp[k], wm[k], cp, cm);
   // dc = sum_k wl[k] R[nv][k] with the nonzero entries of the right
   // eigenvectors, in the order of k
   double dc[5];
@@ -116,6 +119,30 @@ __device__ __forceinline__ void char_slopes(const double (&v)[NV], const double 
 __device__ __forceinline__ long long vcell(const Params &p, int gj, int gi)
 {
   return (long long)gj * p.px + gi;
+}
+
+// FlagShock's test for one zone of the 2-D spherical grid with
+// SHOCK_FLATTENING MULTID (Src/flag_shock.c:147-200): div v < 0 from the
+// face areas and volume, and a pressure jump sum_d |p_{+1} - p_{-1}| above
+// 5 min(p, neighbours).  Zones of the outer ring are never tested.
+__device__ __forceinline__ unsigned char shock_zone(const double *V, const Params &p,
+                                                    const SphGeom &g, int gi, int gj)
+{
+  if (gi < 1 || gi > p.ntot[0] - 2 || gj < 1 || gj > p.ntot[1] - 2) return 0;
+  const long long c = vcell(p, gj, gi), sx = 1, sy = p.px;
+  const double *vx1 = V + VX1 * p.vstride, *vx2 = V + VX2 * p.vstride, *pt = V + PRS * p.vstride;
+  const double dvx1 = g.A1f[gi] * g.dmu[gj] * (vx1[c + sx] + vx1[c]) -
+                      g.A1f[gi - 1] * g.dmu[gj] * (vx1[c - sx] + vx1[c]);
+  const double dvx2 = g.rdr[gi] * g.sxp[gj] * (vx2[c + sy] + vx2[c]) -
+                      g.rdr[gi] * g.sxp[gj - 1] * (vx2[c - sy] + vx2[c]);
+  const double divv = (dvx1 + dvx2) / (g.dVr[gi] * g.dmu[gj]);
+  if (!(divv < 0.0)) return 0;
+  double pt_min = pt[c];
+  const double pmin1 = dmin(pt[c + sx], pt[c - sx]), pmin2 = dmin(pt[c + sy], pt[c - sy]);
+  pt_min = dmin(pt_min, pmin1);
+  pt_min = dmin(pt_min, pmin2);
+  const double gradp = fabs(pt[c + sx] - pt[c - sx]) + fabs(pt[c + sy] - pt[c - sy]);
+  return gradp > 5.0 * pt_min ? 1 : 0;
 }
 
 __device__ __forceinline__ long long vcell3(const Params &p, int gk, int gj, int gi)
@@ -402,6 +429,16 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
     const int gc = min(D == 0 ? p.beg[0] + ox + ix - 1 : p.beg[1] + oy + iy - 1, p.ntot[D] - 1);
     const double cp = g.cp[D][gc], cm = g.cm[D][gc], wp = g.wp[D][gc], wm = g.wm[D][gc];
     const double dp = g.dp[D][gc], dm = g.dm[D][gc];
+    bool minmod = false;
+    if (p.shock) {
+      // FLAG_MINMOD: this zone or a neighbour in either direction is shocked
+      const int ci = p.beg[0] + ox + sx - TL::HX, cj = p.beg[1] + oy + sy - TL::HY;
+      if (ci >= 1 && cj >= 1 && ci <= p.ntot[0] - 2 && cj <= p.ntot[1] - 2) {
+        const unsigned char *S = A.shock;
+        const long long c = vcell(p, cj, ci);
+        minmod = (S[c] | S[c - 1] | S[c + 1] | S[c - p.px] | S[c + p.px]) != 0;
+      }
+    }
     if (p.char_lim) {
       double v0[NV], dvp[NV], dvm[NV], dv[NV];
 #pragma unroll
@@ -410,7 +447,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
         dvp[nv] = (sv[nv * G::VS + s0 + SST] - v0[nv]) * wp;
         dvm[nv] = (v0[nv] - sv[nv * G::VS + s0 - SST]) * wm;
       }
-      char_slopes<D, NV, LIM>(v0, dvp, dvm, cp, cm, gam, dv);
+      char_slopes<D, NV, LIM>(v0, dvp, dvm, cp, cm, gam, minmod, dv);
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) {
         svp[nv * G::NPMAX + q] = v0[nv] + dv[nv] * dp;
@@ -423,7 +460,8 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
       const double vm1 = sv[nv * G::VS + s0 - SST], v0 = sv[nv * G::VS + s0],
                    vp1 = sv[nv * G::VS + s0 + SST];
       const double dvp = (vp1 - v0) * wp, dvm = (v0 - vm1) * wm;
-      const double dv = limited_slope_general<LIM>(dvp, dvm, cp, cm);
+      const double dv = minmod ? (dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0)   // FLAG_MINMOD
+                               : limited_slope_general<LIM>(dvp, dvm, cp, cm);
       svp[nv * G::NPMAX + q] = v0 + dv * dp;
       svm[nv * G::NPMAX + q] = v0 - dv * dm;
     }

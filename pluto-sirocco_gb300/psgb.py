@@ -43,7 +43,7 @@ class Config(ctypes.Structure):
                 ("bc", ctypes.c_int * 6), ("gamma", ctypes.c_double), ("cfl", ctypes.c_double),
                 ("cfl_max_var", ctypes.c_double), ("tstop", ctypes.c_double),
                 ("first_dt", ctypes.c_double), ("cooling", ctypes.c_int),
-                ("char_limiting", ctypes.c_int)]
+                ("char_limiting", ctypes.c_int), ("shock_flattening", ctypes.c_int)]
 
 
 class Wind(ctypes.Structure):
@@ -199,12 +199,13 @@ def check(rc, what):
 
 
 def make_wind_config(nr=512, nt=256, cooling=1, limiter="vl", solver="hll", cfl=0.4,
-                     first_dt=1e-4, char_limiting=0):
+                     first_dt=1e-4, char_limiting=0, shock_flattening=0):
     c = make_config(dims=2, nx=(nr, nt, 1), nvar=6, limiter=limiter, solver=solver,
                     bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
                     cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling)
     c.geometry = SPHERICAL
     c.char_limiting = char_limiting
+    c.shock_flattening = shock_flattening
     return c
 
 
@@ -523,10 +524,11 @@ def batch_models(n=64, seed=4):
     return out
 
 
-def wind_model_solver(spec, cooling=1, line_force=1):
+def wind_model_solver(spec, cooling=1, line_force=1, char_limiting=0, shock_flattening=0):
     """One wind context for a batch spec (see batch_models)."""
     nr, nt = spec["grid"]
-    cfg = make_wind_config(nr, nt, cooling=cooling)
+    cfg = make_wind_config(nr, nt, cooling=cooling, char_limiting=char_limiting,
+                           shock_flattening=shock_flattening)
     w = make_wind(line_force=line_force, l_star=spec["l_star"], krad=spec["krad"],
                   alpharad=spec["alpharad"])
     g = WindGrid(cfg)

@@ -221,6 +221,7 @@ WIND_CASES = [
     ("wind2d_full_64x32", "wind2d", (64, 32), 200, 20, True),
     ("wind2d_hydro_64x32", "wind2d_hydro", (64, 32), 100, 20, False),
     ("wind2d_char_64x32", "wind2d_char", (64, 32), 100, 20, False),
+    ("wind2d_multid_64x32", "wind2d_multid", (64, 32), 100, 20, False),
 ]
 
 
@@ -245,7 +246,8 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux):
     keep = sorted({0, 1, len(snaps) // 2, len(snaps) - 1})
     meta = dict(name=name, ref_config=cfg, kind="wind", dims=2, n=[n[0], n[1], 1],
                 steps=steps, snap_steps=[k * every for k in keep], cooling=int(flux),
-                line_force=int(flux), char_limiting=int("char" in cfg),
+                line_force=int(flux), char_limiting=int("char" in cfg or "multid" in cfg),
+                shock_flattening=int("multid" in cfg),
                 t=[lines[k][1] for k in keep],
                 dt=[lines[k][2] for k in keep], final_sha256=digest(snaps[-1]))
     snaps = np.stack([snaps[k] for k in keep])

@@ -68,6 +68,24 @@ def test_batch_tile_shapes_and_autotune(built):
     batch.close()
 
 
+def test_batch_production_limiting_matches_individual_runs(built):
+    """Characteristic limiting and MULTID shock flattening (the limiting of
+    the production wind configuration) with cooling and the line force:
+    the batch's FlagShock pass and PLM give what each model gives alone."""
+    import psgb
+    kw = dict(cooling=1, line_force=1, char_limiting=1, shock_flattening=1)
+    solo = [psgb.wind_model_solver(s, **kw) for s in SPECS]
+    inb = [psgb.wind_model_solver(s, **kw) for s in SPECS]
+    batch = psgb.Batch(inb)
+    for chunk in (5, 8):
+        flags = 0
+        for s in solo:
+            flags |= s.run(chunk)
+        assert batch.run(chunk) == flags
+        _check_equal(solo, inb)
+    batch.close()
+
+
 def test_batch_rejects_mixed_models(built):
     import psgb
     a = psgb.wind_model_solver(SPECS[0], cooling=1)

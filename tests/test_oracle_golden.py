@@ -62,7 +62,8 @@ def test_wind_oracle_matches_reference(built, meta):
     snaps = np.load(meta["npz"])["snaps"]
     nr, nt = meta["n"][0], meta["n"][1]
     o = wind_oracle(nr, nt, cooling=meta["cooling"], line_force=meta["line_force"],
-                    char_limiting=meta.get("char_limiting", 0))
+                    char_limiting=meta.get("char_limiting", 0),
+                    shock_flattening=meta.get("shock_flattening", 0))
     done = 0
     for k, step in enumerate(meta["snap_steps"]):
         if step > done:
