@@ -73,9 +73,19 @@ typedef struct ps_config {
                            (Src/States/plm_states.c:481-746; spherical
                            contexts)                                      */
   int    shock_flattening; /* SHOCK_FLATTENING MULTID: minmod reconstruction
-                           in and next to shocked zones (Src/flag_shock.c:
-                           81-250; spherical contexts, not in batches)    */
+                           in and next to shocked zones, HLL next to them
+                           with HLLC (Src/flag_shock.c:81-250; spherical
+                           contexts).  Such contexts carry 3 ghost zones
+                           per side instead of 2 (Src/get_nghost.c)       */
+  int    entropy_switch; /* ENTROPY_SWITCH: 0 NO, 1 SELECTIVE, 2 ALWAYS.
+                           The entropy s = p / rho^gamma is the last of the
+                           nvar variables (nvar = 7 for the wind); pressure
+                           is recovered from rho s in the tagged zones
+                           (Src/HD/mappers.c:185-221; spherical contexts) */
 } ps_config;
+
+/* Ghost zones per side of an active direction: PS_NGHOST(cfg) */
+#define PS_NGHOST(cfg) ((cfg)->shock_flattening ? 3 : 2)
 
 typedef struct ps_ctx ps_ctx;
 

@@ -35,7 +35,8 @@ class OrConfig(ctypes.Structure):
                 ("f_x", ctypes.c_double), ("f_uv", ctypes.c_double), ("t_x", ctypes.c_double),
                 ("krad", ctypes.c_double), ("alpharad", ctypes.c_double),
                 ("dfloor", ctypes.c_double), ("xi_const", ctypes.c_double),
-                ("char_limiting", ctypes.c_int), ("shock_flattening", ctypes.c_int)]
+                ("char_limiting", ctypes.c_int), ("shock_flattening", ctypes.c_int),
+                ("entropy_switch", ctypes.c_int)]
 
 
 _lib = None
@@ -59,6 +60,7 @@ def lib():
         L.or_state.restype = DP
         L.or_state.argtypes = [P]
         L.or_ntot.argtypes = [P, I]
+        L.or_nghost.argtypes = [P, I]
         L.or_grid.restype = DP
         L.or_grid.argtypes = [P, I, I]
         L.or_init_blast.argtypes = [P, D, D, D, D, ctypes.c_long]
@@ -89,7 +91,7 @@ WIND_GRID = dict(xbeg=(10.0, 0.0, 0.0), xend=(1000.0, 1.5707963267948966, 1.0),
 NANGLES = 36
 
 
-def synthetic_flux(x1, x2, ntot, l_uv=1.0e37, unit_length=1e9, na=NANGLES):
+def synthetic_flux(x1, x2, ntot, l_uv=1.0e37, unit_length=1e9, na=NANGLES, ngh=2):
     """Synthetic directional UV flux: L_UV/(4 pi r^2) in the angle bin that
     contains the radial direction of each active cell, zero elsewhere; the
     values are rounded through the 13-significant-digit text of the
@@ -97,9 +99,9 @@ def synthetic_flux(x1, x2, ntot, l_uv=1.0e37, unit_length=1e9, na=NANGLES):
     [angle][k][j][i] over the total box (ghost cells zero)."""
     import math
     fr = np.zeros((na, ntot[2], ntot[1], ntot[0]))
-    for j in range(2, ntot[1] - 2):
+    for j in range(ngh, ntot[1] - ngh):
         a = int(math.floor(x2[j] / (2 * 3.14159265358979 / 36)))
-        for i in range(2, ntot[0] - 2):
+        for i in range(ngh, ntot[0] - ngh):
             r = x1[i] * unit_length
             fr[a, :, j, i] = float("%.12e" % (l_uv / (4 * math.pi * r * r)))
     return fr, np.zeros_like(fr), np.zeros_like(fr)
@@ -110,7 +112,7 @@ class Oracle:
                  bc="outflow", gamma=5.0 / 3.0, cfl=0.4, cfl_max_var=1.1, tstop=10.0,
                  first_dt=1e-4, cooling=0, geometry=0, gridtype=("uniform",) * 3,
                  xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), body_force=0, line_force=0,
-                 floors=0, params=None, char_limiting=0, shock_flattening=0):
+                 floors=0, params=None, char_limiting=0, shock_flattening=0, entropy_switch=0):
         c = OrConfig()
         c.dims = dims
         n = list(nx) + [1] * (3 - len(nx))
@@ -134,6 +136,7 @@ class Oracle:
         c.body_force, c.line_force, c.floors = body_force, line_force, floors
         c.char_limiting = char_limiting
         c.shock_flattening = shock_flattening
+        c.entropy_switch = entropy_switch
         for k, v in (params or {}).items():
             setattr(c, k, v)
         self.cfg = c
@@ -141,6 +144,7 @@ class Oracle:
         self.dims = dims
         self.s = lib().or_create(ctypes.byref(c))
         self.ntot = [lib().or_ntot(self.s, d) for d in range(3)]
+        self.ngh = [lib().or_nghost(self.s, d) for d in range(3)]
 
     def __del__(self):
         try:
@@ -202,27 +206,28 @@ class Oracle:
     def active(self, V=None):
         """Active-cell view [nv, (k,) j, i] as written to .dbl files."""
         V = self.V if V is None else V
-        g = [2 if d < self.dims else 0 for d in range(3)]
+        g = [self.ngh[d] for d in range(3)]
         a = V[:, g[2]:self.ntot[2] - g[2], g[1]:self.ntot[1] - g[1], g[0]:self.ntot[0] - g[0]]
         return a[:, 0] if self.dims == 2 else a
 
 
 def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, char_limiting=0,
-                shock_flattening=0, **params):
+                shock_flattening=0, solver="hll", entropy_switch=0, **params):
     """The 2-D spherical line-driven disk wind (PLM van Leer, HLL, RK2,
     userdef/outflow/axisymmetric/reflective boundaries, point-mass gravity,
     floors, BLONDIN cooling and the line force), initialised."""
-    o = Oracle(dims=2, nx=(nr, nt, 1), nvar=6, limiter="vl", solver="hll",
+    o = Oracle(dims=2, nx=(nr, nt, 1), nvar=7 if entropy_switch else 6, limiter="vl",
+               solver=solver,
                bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
                cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling,
                geometry=3, gridtype=WIND_GRID["gridtype"], xbeg=WIND_GRID["xbeg"],
                xend=WIND_GRID["xend"], body_force=1, line_force=line_force, floors=1,
                params=dict(WIND, **params), char_limiting=char_limiting,
-               shock_flattening=shock_flattening)
+               shock_flattening=shock_flattening, entropy_switch=entropy_switch)
     if line_force:
         prm = dict(WIND, **params)
         o.set_flux(*synthetic_flux(o.grid(0), o.grid(1), o.ntot,
-                                   l_uv=prm["l_star"] * prm["f_uv"]))
+                                   l_uv=prm["l_star"] * prm["f_uv"], ngh=o.ngh[0]))
     o.init_wind()
     return o
 

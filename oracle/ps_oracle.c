@@ -47,6 +47,8 @@
 #define MAXD(a, b) ((a) >= (b) ? (a) : (b))
 #define MIND(a, b) ((a) <= (b) ? (a) : (b))
 #define OR_FLAG_MINMOD 1   /* FLAG_MINMOD (Src/pluto.h:212) */
+#define OR_FLAG_HLL    4   /* FLAG_HLL (Src/pluto.h:214) */
+#define OR_FLAG_ENTROPY 8  /* FLAG_ENTROPY (Src/pluto.h:215) */
 #define ABS_MIN(a, b) (fabs(a) < fabs(b) ? (a) : (b))
 
 static const double small_density = 1.e-12;
@@ -254,7 +256,8 @@ or_sim *or_create(const or_config *cfg)
   size_t ncell;
   s->c = *cfg;
   for (d = 0; d < 3; d++) {
-    s->ngh[d] = (d < cfg->dims) ? 2 : 0;
+    /* GetNghost (Src/get_nghost.c:15-60): 2 for PLM, 3 with MULTID */
+    s->ngh[d] = (d < cfg->dims) ? (cfg->shock_flattening ? 3 : 2) : 0;
     s->ntot[d] = cfg->nx[d] + 2 * s->ngh[d];
     s->beg[d] = s->ngh[d];
     s->end[d] = s->ngh[d] + cfg->nx[d] - 1;
@@ -498,6 +501,8 @@ static void wind_init_point(const or_sim *s, double *v, double x1, double x2)
   v[PRS] = v[RHO] * T / (KELVIN_OF(s) * mu);
 }
 
+static void compute_entropy(or_sim *s);
+
 void or_init_wind(or_sim *s)
 {
   int i, j, k, nv;
@@ -524,6 +529,7 @@ void or_init_wind(or_sim *s)
     s->tr_s[c] = s->c.t_x;
   }
   s->dvds_ready = 0;
+  if (s->c.entropy_switch) compute_entropy(s);   /* Startup's Boundary */
 }
 
 void or_set_flux(or_sim *s, int nangles, const double *fr, const double *ft, const double *fp)
@@ -590,6 +596,16 @@ static void wind_floors(or_sim *s)
   }
 }
 
+/* ComputeEntropy (Src/entropy_switch.c:14-37 with Entropy, Src/EOS/Ideal/
+ * eos.c:77-103): s = p / rho^gamma over the total box, into the last
+ * variable. */
+static void compute_entropy(or_sim *s)
+{
+  size_t c, nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  double *S = s->V + (size_t)(s->c.nvar - 1) * nc;
+  for (c = 0; c < nc; c++) S[c] = s->V[PRS * nc + c] / pow(s->V[RHO * nc + c], s->c.gamma);
+}
+
 static void boundary(or_sim *s)
 {
   int side, nv, i, j, k;
@@ -646,6 +662,7 @@ static void boundary(or_sim *s)
         s->V[vidx(s, nv, k, j, i)] = vsign[nv] * val;
     }
   }
+  if (s->c.entropy_switch) compute_entropy(s);   /* boundary.c:487-493 */
 }
 
 /* ------------------------------------------------------------------ */
@@ -665,8 +682,11 @@ static inline void prim_to_cons(const double *v, double *u, int nvar, double gmm
   for (nv = NFLX; nv < nvar; nv++) u[nv] = rho * v[nv];
 }
 
-/* returns nonzero flag bits on failure (64 = cons2prim fail) */
-static inline int cons_to_prim(double *u, double *v, int nvar, double gmm1)
+/* returns nonzero flag bits on failure (64 = cons2prim fail).  entr: index
+ * of the entropy variable (ENTROPY_SWITCH) or -1; use_entropy: the zone is
+ * tagged FLAG_ENTROPY, p = (rho s) rho^(gamma-1) (mappers.c:185-221). */
+static inline int cons_to_prim(double *u, double *v, int nvar, double gmm1, int entr,
+                               int use_entropy)
 {
   int flag = 0, nv;
   double m2 = u[VX1] * u[VX1] + u[VX2] * u[VX2] + u[VX3] * u[VX3];
@@ -685,13 +705,23 @@ static inline int cons_to_prim(double *u, double *v, int nvar, double gmm1)
     u[PRS] = small_pressure / gmm1 + kin;
     flag |= 64;
   }
-  v[PRS] = gmm1 * (u[PRS] - kin);
-  if (v[PRS] < 0.0) {
-    v[PRS] = small_pressure;
-    u[PRS] = v[PRS] / gmm1 + kin;
-    flag |= 64;
+  if (use_entropy) {
+    double rhog1 = pow(rho, gmm1);
+    v[PRS] = u[entr] * rhog1;
+    if (v[PRS] < 0.0) {
+      v[PRS] = small_pressure;
+      flag |= 64;
+    }
+    u[PRS] = v[PRS] / gmm1 + kin;   /* redefine energy */
+  } else {
+    v[PRS] = gmm1 * (u[PRS] - kin);
+    if (v[PRS] < 0.0) {
+      v[PRS] = small_pressure;
+      u[PRS] = v[PRS] / gmm1 + kin;
+      flag |= 64;
+    }
+    if (entr >= 0) u[entr] = v[PRS] / pow(rho, gmm1);
   }
-  (void)rho;
   for (nv = NFLX; nv < nvar; nv++) v[nv] = u[nv] * tau;
   return flag;
 }
@@ -1125,7 +1155,10 @@ static void row_sweep(or_sim *s, int d, int k0, int j0, int i0, int stage,
     } else if (SR[i] < 0.0) {
       for (nv = 0; nv < NFLX; nv++) f[nv] = FR[nv];
       pr[i] = pR[i];
-    } else if (s->c.solver == OR_HLL) {
+    } else if (s->c.solver == OR_HLL ||
+               (s->c.shock_flattening && ((s->flag[base + i * stride] & OR_FLAG_HLL) ||
+                                          (s->flag[base + (i + 1) * stride] & OR_FLAG_HLL)))) {
+      /* HLL, or HLLC's switch to HLL next to a shocked zone (hllc.c:93-104) */
       double scrh = 1.0 / (SR[i] - SL[i]);
       for (nv = 0; nv < NFLX; nv++) {
         f[nv] = SL[i] * SR[i] * (uR[nv] - uL[nv]) + SR[i] * FL[nv] - SL[i] * FR[nv];
@@ -1248,7 +1281,9 @@ static int cons_to_prim_dom(or_sim *s)
   for (j = s->beg[1]; j <= s->end[1]; j++)
   for (i = s->beg[0]; i <= s->end[0]; i++) {
     size_t c = cidx(s, k, j, i);
-    flags |= cons_to_prim(&s->U[c * nvar], v, nvar, gmm1);
+    const int entr = s->c.entropy_switch ? nvar - 1 : -1;
+    flags |= cons_to_prim(&s->U[c * nvar], v, nvar, gmm1, entr,
+                          entr >= 0 && (s->flag[c] & OR_FLAG_ENTROPY));
     for (nv = 0; nv < nvar; nv++) s->V[nv * nc + c] = v[nv];
   }
   return flags;
@@ -1487,6 +1522,7 @@ static void flag_shock(or_sim *s)
   const double *vx1 = s->V + VX1 * nc, *vx2 = s->V + VX2 * nc, *vx3 = s->V + VX3 * nc;
   const double *pt = s->V + PRS * nc;
   memset(s->flag, 0, nc);
+  if (s->c.entropy_switch) memset(s->flag, OR_FLAG_ENTROPY, nc);   /* flag_shock.c:146-148 */
   for (k = ik; k < n2 - ik; k++)
   for (j = ij; j < n1 - ij; j++)
   for (i = 1; i < n0 - 1; i++) {
@@ -1519,7 +1555,15 @@ static void flag_shock(or_sim *s)
       if (ij) dpx2 = fabs(pt[c + sy] - pt[c - sy]);
       if (ik) dpx3 = fabs(pt[c + sz] - pt[c - sz]);
       gradp = s->c.dims == 1 ? dpx1 : (s->c.dims == 2 ? dpx1 + dpx2 : dpx1 + dpx2 + dpx3);
-      if (gradp > 5.0 * pt_min) {
+      if (s->c.entropy_switch == 1 && gradp > 0.05 * pt_min) {   /* flag_shock.c:251-267 */
+        s->flag[c] &= ~OR_FLAG_ENTROPY;
+        s->flag[c - sx] &= ~OR_FLAG_ENTROPY;
+        s->flag[c + sx] &= ~OR_FLAG_ENTROPY;
+        if (ij) { s->flag[c + sy] &= ~OR_FLAG_ENTROPY; s->flag[c - sy] &= ~OR_FLAG_ENTROPY; }
+        if (ik) { s->flag[c + sz] &= ~OR_FLAG_ENTROPY; s->flag[c - sz] &= ~OR_FLAG_ENTROPY; }
+      }
+      if (s->c.shock_flattening && gradp > 5.0 * pt_min) {
+        s->flag[c] |= OR_FLAG_HLL;
         s->flag[c] |= OR_FLAG_MINMOD;
         s->flag[c + sx] |= OR_FLAG_MINMOD;
         s->flag[c - sx] |= OR_FLAG_MINMOD;
@@ -1535,7 +1579,7 @@ static int advance_step(or_sim *s)
 {
   int i, j, k, nv, nvar = s->c.nvar, flags;
   boundary(s);
-  if (s->c.shock_flattening) flag_shock(s);
+  if (s->c.shock_flattening || s->c.entropy_switch) flag_shock(s);
   prim_to_cons_dom(s);
   for (k = s->beg[2]; k <= s->end[2]; k++)
   for (j = s->beg[1]; j <= s->end[1]; j++)

@@ -59,6 +59,11 @@ typedef struct {
   /* SHOCK_FLATTENING MULTID: minmod reconstruction in and next to shocked
    * zones (Src/flag_shock.c:81-250, plm_states.c:176-193, 613-625) */
   int    shock_flattening;
+  /* ENTROPY_SWITCH: 0 NO, 1 SELECTIVE, 2 ALWAYS.  The entropy s = p/rho^gamma
+   * is the last variable; pressure is recovered from rho s in the zones
+   * tagged FLAG_ENTROPY (Src/entropy_switch.c, Src/HD/mappers.c:185-221,
+   * Src/flag_shock.c:138-148, 251-267) */
+  int    entropy_switch;
 } or_config;
 
 typedef struct or_sim or_sim;

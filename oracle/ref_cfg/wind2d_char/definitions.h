@@ -1,7 +1,7 @@
 /* Problem configuration for the reference CPU build of the 2-D
-   spherical (r, theta) line-driven disk wind: PLM (van Leer, primitive),
-   HLL, RK2, point-mass gravity, (no cooling, no line
-   force): the hydro, geometry, gravity and boundaries alone.
+   spherical (r, theta) line-driven disk wind, hydro part only: PLM (van
+   Leer) on characteristic variables, HLL, RK2, point-mass gravity; no
+   cooling, no line force.
    Test infrastructure only: compiled by oracle/ref.mk into oracle/_ref. */
 #define  PHYSICS                        HD
 #define  DIMENSIONS                     2

@@ -94,8 +94,9 @@ static int encode_map(ps_ctx *c, double *base, CUtensorMap *tm)
     encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }
   const ps::Params &p = c->p;
-  cuuint64_t dims[4] = {(cuuint64_t)p.ntot[0], (cuuint64_t)p.ntot[1], (cuuint64_t)p.ntot[2],
-                        (cuuint64_t)p.nvar};
+  // x runs over the memory columns of a row (cell i at column i + xoff)
+  cuuint64_t dims[4] = {(cuuint64_t)(p.ntot[0] + p.xoff), (cuuint64_t)p.ntot[1],
+                        (cuuint64_t)p.ntot[2], (cuuint64_t)p.nvar};
   cuuint64_t strides[3] = {(cuuint64_t)p.px * 8, (cuuint64_t)p.px * p.ntot[1] * 8,
                            (cuuint64_t)p.vstride * 8};
   cuuint32_t box[4] = {(cuuint32_t)(c->tile[0] + 2 * c->tile[3]),
@@ -180,12 +181,16 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   }
   *out = nullptr;
   const bool sph = cfg->geometry == PS_SPHERICAL;
-  if ((cfg->dims != 2 && cfg->dims != 3) || (cfg->nvar != 5 && cfg->nvar != 6) ||
-      (cfg->geometry != PS_CARTESIAN && !sph) || (sph && (cfg->dims != 2 || cfg->nvar != 6)) ||
+  const int sph_nvar = cfg->entropy_switch ? 7 : 6;
+  if ((cfg->dims != 2 && cfg->dims != 3) || (cfg->nvar < 5 || cfg->nvar > 7) ||
+      (!sph && cfg->nvar == 7) || (cfg->geometry != PS_CARTESIAN && !sph) ||
+      (sph && (cfg->dims != 2 || cfg->nvar != sph_nvar)) ||
+      cfg->entropy_switch < 0 || cfg->entropy_switch > 2 ||
       cfg->limiter < 0 || cfg->limiter > 2 ||
       (cfg->solver != PS_HLLC && cfg->solver != PS_HLL) || cfg->gamma <= 1.0) {
     ps_set_error_msg("ps_create: unsupported configuration (Cartesian: dims 2/3, nvar 5/6; "
-                     "spherical: dims 2, nvar 6; MC/VL/MM limiter, HLLC/HLL)");
+                     "spherical: dims 2, nvar 6, or 7 with the entropy switch; MC/VL/MM "
+                     "limiter, HLLC/HLL)");
     return PS_EINVAL;
   }
   for (int d = 0; d < 3; d++) {
@@ -198,9 +203,9 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
       return PS_EINVAL;
     }
   }
-  if ((cfg->char_limiting || cfg->shock_flattening) && !sph) {
-    ps_set_error_msg("ps_create: characteristic limiting and shock flattening are built for the "
-                     "spherical wind path");
+  if ((cfg->char_limiting || cfg->shock_flattening || cfg->entropy_switch) && !sph) {
+    ps_set_error_msg("ps_create: characteristic limiting, shock flattening and the entropy "
+                     "switch are built for the spherical wind path");
     return PS_EINVAL;
   }
   for (int s = 0; s < 2 * cfg->dims; s++) {
@@ -228,13 +233,17 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   p.cooling = cfg->cooling;
   p.char_lim = cfg->char_limiting ? 1 : 0;
   p.shock = cfg->shock_flattening ? 1 : 0;
+  p.entropy = cfg->entropy_switch;
   for (int d = 0; d < 3; d++) {
     p.nx[d] = cfg->nx[d];
-    p.beg[d] = d < cfg->dims ? 2 : 0;
+    // GetNghost (Src/get_nghost.c:15-60): 2 ghost zones for PLM, 3 with
+    // SHOCK_FLATTENING MULTID
+    p.beg[d] = d < cfg->dims ? (cfg->shock_flattening ? 3 : 2) : 0;
     p.ntot[d] = cfg->nx[d] + 2 * p.beg[d];
   }
   for (int s = 0; s < 6; s++) p.bc[s] = cfg->bc[s];
-  p.px = (p.ntot[0] + 3) & ~3;
+  p.xoff = (p.beg[0] & 1) ? 1 : 0;
+  p.px = (p.ntot[0] + p.xoff + 3) & ~3;
   p.vstride = (long long)p.px * p.ntot[1] * p.ntot[2];
   p.gamma = cfg->gamma;
   p.gmm1 = cfg->gamma - 1.0;
@@ -419,10 +428,16 @@ extern "C" int ps_set_state(ps_ctx *c, const double *Vc)
   if (r) return r;
   if (!Vc) return PS_EINVAL;
   const ps::Params &p = c->p;
-  CK(cudaMemcpy2DAsync(c->V, (size_t)p.px * 8, Vc, (size_t)p.ntot[0] * 8, (size_t)p.ntot[0] * 8,
+  CK(cudaMemcpy2DAsync(c->V + p.xoff, (size_t)p.px * 8, Vc, (size_t)p.ntot[0] * 8,
+                       (size_t)p.ntot[0] * 8,
                        (size_t)p.ntot[1] * p.ntot[2] * p.nvar, cudaMemcpyHostToDevice, c->stream));
-  ps::launch_fill_ghosts(c, c->V, c->stream);
-  c->launches++;
+  // Cartesian contexts: the stage kernels read ghost zones written by the
+  // previous stage, so they are filled here; the wind's ghost zones are
+  // filled by its boundary kernels before every stage
+  if (c->cfg.geometry != PS_SPHERICAL) {
+    ps::launch_fill_ghosts(c, c->V, c->stream);
+    c->launches++;
+  }
   CK(cudaGetLastError());
   launch_finish(c, ps::MODE_BEGIN);
   CK(cudaGetLastError());
@@ -434,7 +449,8 @@ extern "C" int ps_get_state(ps_ctx *c, double *Vc)
 {
   if (!c || !Vc) return PS_EINVAL;
   const ps::Params &p = c->p;
-  CK(cudaMemcpy2DAsync(Vc, (size_t)p.ntot[0] * 8, c->V, (size_t)p.px * 8, (size_t)p.ntot[0] * 8,
+  CK(cudaMemcpy2DAsync(Vc, (size_t)p.ntot[0] * 8, c->V + p.xoff, (size_t)p.px * 8,
+                       (size_t)p.ntot[0] * 8,
                        (size_t)p.ntot[1] * p.ntot[2] * p.nvar, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return 0;
@@ -578,7 +594,7 @@ static int build_wind_graph(ps_ctx *c, int kind, cudaGraphExec_t *out)
 static int run_wind(ps_ctx *c, int nsteps)
 {
   const int ncool = c->p.cooling ? (c->sg ? 2 : 1) + (c->wind ? 0 : 1) : 0;
-  const long per_step = (c->wind ? 7 + (c->p.shock ? 1 : 0) : 3) + ncool;
+  const long per_step = (c->wind ? 7 + (ps::needs_shock_flags(c->p) ? 1 : 0) : 3) + ncool;
   for (int k = 0; k < 3; k++)
     if (!c->gw[k]) {
       int r = build_wind_graph(c, k, &c->gw[k]);
@@ -645,7 +661,7 @@ extern "C" double *ps_device_state(ps_ctx *c, int *pitch)
 {
   if (!c) return nullptr;
   if (pitch) *pitch = c->p.px;
-  return c->V;
+  return c->V + c->p.xoff;
 }
 
 extern "C" long ps_launch_count(const ps_ctx *c) { return c ? c->launches : -1; }

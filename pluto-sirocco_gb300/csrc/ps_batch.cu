@@ -10,9 +10,9 @@
 // and TMA descriptors and the work lists that map CTAs to (model, tile) or
 // (model, cell block).  Results are identical to advancing each model on
 // its own (the per-cell arithmetic does not depend on the tile shape).
+#include "ps_batch_dev.cuh"
 #include "ps_finish.cuh"
 #include "ps_surrogate_cool.cuh"
-#include "ps_wind_dev.cuh"
 
 #include <cudaTypedefs.h>
 
@@ -25,33 +25,6 @@
 extern "C" void ps_set_error_msg(const char *msg);
 
 namespace ps {
-
-struct BatchModel {
-  CUtensorMap tm[2];     // V (stage-1 input) and V* (stage-2 input), tile box of the model
-  WindStageArgs st[2];   // stage 1 and stage 2 arguments
-  FinishArgs fin;        // dt kernel arguments (MODE_STEP)
-};
-
-struct TileItem {
-  int m, bx, by, pad;
-};
-
-__device__ __forceinline__ void tensormap_acquire(const CUtensorMap *tm)
-{
-  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm) : "memory");
-}
-
-template <int NV, int LIM, int SOLVER, int STAGE, class TL>
-__global__ void __launch_bounds__(TileGeom<TL>::NT)
-    k_batch_stage(const BatchModel *__restrict__ models, const TileItem *__restrict__ items)
-{
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  const TileItem it = items[blockIdx.x];
-  const BatchModel &M = models[it.m];
-  const CUtensorMap *tm = &M.tm[STAGE - 1];
-  if (threadIdx.x == 0) tensormap_acquire(tm);
-  stage_sph_tile<NV, LIM, SOLVER, STAGE, TL>(tm, M.st[STAGE - 1], it.bx, it.by, smem_raw);
-}
 
 template <int NV>
 __global__ void k_batch_bnd_x1(const BatchModel *__restrict__ models,
@@ -74,7 +47,7 @@ __global__ void k_batch_bnd_x2(const BatchModel *__restrict__ models,
   const WindStageArgs &A = models[bi.m].st[0];
   if (A.s.sc->done) return;
   const int q = bi.b * blockDim.x + threadIdx.x;
-  if (q < A.s.p.ntot[0] * 4)
+  if (q < A.s.p.ntot[0] * 2 * A.s.p.beg[1])
     bnd_x2_item<NV>(stage == 1 ? const_cast<double *>(A.s.Vn) : A.s.Vout, A.s.p, q);
 }
 
@@ -153,56 +126,20 @@ __global__ void k_batch_finish(const BatchModel *__restrict__ models)
   finish_block(models[blockIdx.x].fin);
 }
 
-// ------------------------------------------------------------------
-// kernel tables for the tile shapes the autotuner chooses from
-// ------------------------------------------------------------------
+// stage kernels for the 6-variable state; the 7-variable ones (with the
+// entropy of ENTROPY_SWITCH) are instantiated in ps_batch7.cu
+const void *batch_kernel7(int shape, int lim, int solver, int stage);
+size_t batch_smem7(int shape);
 
-constexpr int kNumShapes = 4;
-const int kShapeX[kNumShapes] = {32, 16, 64, 16};
-const int kShapeY[kNumShapes] = {8, 16, 4, 16};
-// threads per CTA: one per cell, plus one warp for the halo work of the
-// 16x16 tile's PLM (18 x 16 items) in shape 3
-const int kShapeNT[kNumShapes] = {256, 256, 256, 288};
-using Shape3 = Tile2D<16, 16, 32>;
-
-template <int LIM, int SOLVER, class TL>
-static const void *pick_batch(int stage)
+static const void *batch_kernel(int nv, int shape, int lim, int solver, int stage)
 {
-  return stage == 1 ? reinterpret_cast<const void *>(&k_batch_stage<6, LIM, SOLVER, 1, TL>)
-                    : reinterpret_cast<const void *>(&k_batch_stage<6, LIM, SOLVER, 2, TL>);
+  return nv == 7 ? batch_kernel7(shape, lim, solver, stage)
+                 : batch_kernel_nv<6>(shape, lim, solver, stage);
 }
 
-template <class TL>
-static const void *pick_batch_shape(int lim, int solver, int stage)
+static size_t batch_smem(int nv, int shape)
 {
-  if (solver == HLL) {
-    if (lim == LIM_VL) return pick_batch<LIM_VL, HLL, TL>(stage);
-    if (lim == LIM_MM) return pick_batch<LIM_MM, HLL, TL>(stage);
-    return pick_batch<LIM_MC, HLL, TL>(stage);
-  }
-  if (lim == LIM_VL) return pick_batch<LIM_VL, HLLC, TL>(stage);
-  if (lim == LIM_MM) return pick_batch<LIM_MM, HLLC, TL>(stage);
-  return pick_batch<LIM_MC, HLLC, TL>(stage);
-}
-
-static const void *batch_kernel(int shape, int lim, int solver, int stage)
-{
-  switch (shape) {
-    case 1: return pick_batch_shape<Tile2D<16, 16>>(lim, solver, stage);
-    case 2: return pick_batch_shape<Tile2D<64, 4>>(lim, solver, stage);
-    case 3: return pick_batch_shape<Shape3>(lim, solver, stage);
-    default: return pick_batch_shape<Tile2D<32, 8>>(lim, solver, stage);
-  }
-}
-
-static size_t batch_smem(int shape)
-{
-  switch (shape) {
-    case 1: return stage_smem_bytes<6, Tile2D<16, 16>>();
-    case 2: return stage_smem_bytes<6, Tile2D<64, 4>>();
-    case 3: return stage_smem_bytes<6, Shape3>();
-    default: return stage_smem_bytes<6, Tile2D<32, 8>>();
-  }
+  return nv == 7 ? batch_smem7(shape) : batch_smem_nv<6>(shape);
 }
 
 }  // namespace ps
@@ -233,7 +170,7 @@ struct ps_batch {
   int num_sms = 148;
   int2 *sg_queue = nullptr;
   int *sg_qcount = nullptr;
-  int lim = 0, solver = 0, cooling = 0;
+  int lim = 0, solver = 0, cooling = 0, nvar = 6;
   cudaStream_t stream = nullptr;      // stream the work is issued on
   cudaStream_t own_stream = nullptr;  // stream created by the batch
   cudaStream_t side[ps::kNumShapes] = {};  // tile-shape groups
@@ -275,8 +212,8 @@ static int encode_box(const ps::Params &p, double *base, int tx, int ty, CUtenso
       return batch_fail("cuTensorMapEncodeTiled entry point not available");
     encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }
-  cuuint64_t dims[4] = {(cuuint64_t)p.ntot[0], (cuuint64_t)p.ntot[1], (cuuint64_t)p.ntot[2],
-                        (cuuint64_t)p.nvar};
+  cuuint64_t dims[4] = {(cuuint64_t)(p.ntot[0] + p.xoff), (cuuint64_t)p.ntot[1],
+                        (cuuint64_t)p.ntot[2], (cuuint64_t)p.nvar};
   cuuint64_t strides[3] = {(cuuint64_t)p.px * 8, (cuuint64_t)p.px * p.ntot[1] * 8,
                            (cuuint64_t)p.vstride * 8};
   cuuint32_t box[4] = {(cuuint32_t)(tx + 4), (cuuint32_t)(ty + 4), 1u, (cuuint32_t)p.nvar};
@@ -328,13 +265,13 @@ static int batch_upload(ps_batch *b)
     const int ntx = (p.nx[0] + tx - 1) / tx, nty = (p.nx[1] + ty - 1) / ty;
     for (int by = 0; by < nty; by++)
       for (int bx = 0; bx < ntx; bx++) items[sh].push_back({m, bx, by, 0});
-    const int nc = (p.nx[0] * p.nx[1] + 255) / 256, n2 = (p.ntot[0] * 4 + 255) / 256;
+    const int nc = (p.nx[0] * p.nx[1] + 255) / 256, n2 = (p.ntot[0] * 2 * p.beg[1] + 255) / 256;
     for (int k = 0; k < nc; k++) cells.push_back({m, k});
     const int nc128 = (p.nx[0] * p.nx[1] + 127) / 128;
     for (int k = 0; k < nc128; k++) cells128.push_back({m, k});
     b->total_cells += (long)p.nx[0] * p.nx[1];
     for (int k = 0; k < n2; k++) x2.push_back({m, k});
-    if (p.shock)
+    if (ps::needs_shock_flags(p))
       for (int k = 0; k < (p.ntot[0] * p.ntot[1] + 255) / 256; k++) shock.push_back({m, k});
   }
   BCK(cudaMemcpy(b->d_models, b->h_models.data(), sizeof(ps::BatchModel) * b->n,
@@ -390,9 +327,9 @@ static int batch_stage(ps_batch *b, int stage)
     if (!b->nitems[s]) continue;
     cudaStream_t st = s == first ? b->stream : b->side[s];
     if (s != first) BCK(cudaStreamWaitEvent(st, b->fork, 0));
-    const void *k = ps::batch_kernel(s, b->lim, b->solver, stage);
+    const void *k = ps::batch_kernel(b->nvar, s, b->lim, b->solver, stage);
     void *args[2] = {&b->d_models, &b->d_items[s]};
-    BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(ps::kShapeNT[s]), args, ps::batch_smem(s),
+    BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(ps::kShapeNT[s]), args, ps::batch_smem(b->nvar, s),
                          st));
     b->launches++;
     if (s != first) BCK(cudaEventRecord(b->join[s], st));
@@ -404,8 +341,15 @@ static int batch_stage(ps_batch *b, int stage)
 
 static int batch_bnd(ps_batch *b, int stage)
 {
-  ps::k_batch_bnd_x1<6><<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, stage);
-  ps::k_batch_bnd_x2<6><<<b->nx2_blocks, 256, 0, b->stream>>>(b->d_models, b->d_x2, stage);
+  if (b->nvar == 7) {
+    ps::k_batch_bnd_x1<7><<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells,
+                                                                    stage);
+    ps::k_batch_bnd_x2<7><<<b->nx2_blocks, 256, 0, b->stream>>>(b->d_models, b->d_x2, stage);
+  } else {
+    ps::k_batch_bnd_x1<6><<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells,
+                                                                    stage);
+    ps::k_batch_bnd_x2<6><<<b->nx2_blocks, 256, 0, b->stream>>>(b->d_models, b->d_x2, stage);
+  }
   b->launches += 2;
   if (stage == 1 && b->nshock_blocks) {
     ps::k_batch_shock<<<b->nshock_blocks, 256, 0, b->stream>>>(b->d_models, b->d_shock);
@@ -487,8 +431,10 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
     ps_ctx *c = ctxs[m];
     if (!c || !c->wind) return batch_fail("ps_batch_create: every model needs ps_set_wind");
     if (c->p.limiter != ctxs[0]->p.limiter || c->p.solver != ctxs[0]->p.solver ||
-        c->p.cooling != ctxs[0]->p.cooling || c->host_step != ctxs[0]->host_step)
-      return batch_fail("ps_batch_create: models must share limiter, solver, cooling and step");
+        c->p.cooling != ctxs[0]->p.cooling || c->host_step != ctxs[0]->host_step ||
+        c->p.nvar != ctxs[0]->p.nvar)
+      return batch_fail("ps_batch_create: models must share limiter, solver, cooling, variables "
+                        "and step");
   }
   ps_batch *b = new ps_batch();
   b->n = n;
@@ -498,6 +444,7 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
   b->lim = ctxs[0]->p.limiter;
   b->solver = ctxs[0]->p.solver;
   b->cooling = ctxs[0]->p.cooling;
+  b->nvar = ctxs[0]->p.nvar;
   b->host_step = ctxs[0]->host_step;
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -534,9 +481,9 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
   cudaMemcpy(b->d_pre, pre.data(), sizeof(double *) * n, cudaMemcpyHostToDevice);
   for (int s = 0; s < ps::kNumShapes; s++) {
     for (int st = 1; st <= 2; st++) {
-      e = cudaFuncSetAttribute(ps::batch_kernel(s, b->lim, b->solver, st),
+      e = cudaFuncSetAttribute(ps::batch_kernel(b->nvar, s, b->lim, b->solver, st),
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)ps::batch_smem(s));
+                               (int)ps::batch_smem(b->nvar, s));
       if (e != cudaSuccess) {
         batch_free(b);
         return batch_cuda(e, "ps_batch_create: smem attribute");
@@ -618,14 +565,14 @@ extern "C" int ps_batch_autotune(ps_batch *b, int reps)
       BCK(cudaMalloc(&d_items, items.size() * sizeof(ps::TileItem)));
       BCK(cudaMemcpy(d_items, items.data(), items.size() * sizeof(ps::TileItem),
                      cudaMemcpyHostToDevice));
-      const void *k = ps::batch_kernel(s, b->lim, b->solver, 1);
+      const void *k = ps::batch_kernel(b->nvar, s, b->lim, b->solver, 1);
       void *args[2] = {&b->d_models, &d_items};
       BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(ps::kShapeNT[s]), args,
-                           ps::batch_smem(s), b->stream));
+                           ps::batch_smem(b->nvar, s), b->stream));
       BCK(cudaEventRecord(e0, b->stream));
       for (int it = 0; it < reps; it++)
         BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(ps::kShapeNT[s]), args,
-                             ps::batch_smem(s), b->stream));
+                             ps::batch_smem(b->nvar, s), b->stream));
       BCK(cudaEventRecord(e1, b->stream));
       BCK(cudaEventSynchronize(e1));
       float ms = 0.f;

@@ -1,0 +1,96 @@
+// ps_batch_dev.cuh -- device side of the batch of wind models: the
+// per-model descriptor table entry, the work items of the stage kernels,
+// the stage kernel itself and its tables over the tile shapes the
+// autotuner chooses from (instantiated per variable count in ps_batch.cu
+// and ps_batch7.cu).
+#pragma once
+
+#include "ps_finish.cuh"
+#include "ps_wind_dev.cuh"
+
+#include <cudaTypedefs.h>
+
+namespace ps {
+
+struct BatchModel {
+  CUtensorMap tm[2];     // V (stage-1 input) and V* (stage-2 input), tile box of the model
+  WindStageArgs st[2];   // stage 1 and stage 2 arguments
+  FinishArgs fin;        // dt kernel arguments (MODE_STEP)
+};
+
+struct TileItem {
+  int m, bx, by, pad;
+};
+
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap *tm)
+{
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm) : "memory");
+}
+
+template <int NV, int LIM, int SOLVER, int STAGE, class TL>
+__global__ void __launch_bounds__(TileGeom<TL>::NT)
+    k_batch_stage(const BatchModel *__restrict__ models, const TileItem *__restrict__ items)
+{
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const TileItem it = items[blockIdx.x];
+  const BatchModel &M = models[it.m];
+  const CUtensorMap *tm = &M.tm[STAGE - 1];
+  if (threadIdx.x == 0) tensormap_acquire(tm);
+  stage_sph_tile<NV, LIM, SOLVER, STAGE, TL>(tm, M.st[STAGE - 1], it.bx, it.by, smem_raw);
+}
+
+// ------------------------------------------------------------------
+// kernel tables for the tile shapes the autotuner chooses from
+// ------------------------------------------------------------------
+
+constexpr int kNumShapes = 4;
+const int kShapeX[kNumShapes] = {32, 16, 64, 16};
+const int kShapeY[kNumShapes] = {8, 16, 4, 16};
+// threads per CTA: one per cell, plus one warp for the halo work of the
+// 16x16 tile's PLM (18 x 16 items) in shape 3
+const int kShapeNT[kNumShapes] = {256, 256, 256, 288};
+using Shape3 = Tile2D<16, 16, 32>;
+
+template <int NV, int LIM, int SOLVER, class TL>
+const void *pick_batch(int stage)
+{
+  return stage == 1 ? reinterpret_cast<const void *>(&k_batch_stage<NV, LIM, SOLVER, 1, TL>)
+                    : reinterpret_cast<const void *>(&k_batch_stage<NV, LIM, SOLVER, 2, TL>);
+}
+
+template <int NV, class TL>
+const void *pick_batch_shape(int lim, int solver, int stage)
+{
+  if (solver == HLL) {
+    if (lim == LIM_VL) return pick_batch<NV, LIM_VL, HLL, TL>(stage);
+    if (lim == LIM_MM) return pick_batch<NV, LIM_MM, HLL, TL>(stage);
+    return pick_batch<NV, LIM_MC, HLL, TL>(stage);
+  }
+  if (lim == LIM_VL) return pick_batch<NV, LIM_VL, HLLC, TL>(stage);
+  if (lim == LIM_MM) return pick_batch<NV, LIM_MM, HLLC, TL>(stage);
+  return pick_batch<NV, LIM_MC, HLLC, TL>(stage);
+}
+
+template <int NV>
+const void *batch_kernel_nv(int shape, int lim, int solver, int stage)
+{
+  switch (shape) {
+    case 1: return pick_batch_shape<NV, Tile2D<16, 16>>(lim, solver, stage);
+    case 2: return pick_batch_shape<NV, Tile2D<64, 4>>(lim, solver, stage);
+    case 3: return pick_batch_shape<NV, Shape3>(lim, solver, stage);
+    default: return pick_batch_shape<NV, Tile2D<32, 8>>(lim, solver, stage);
+  }
+}
+
+template <int NV>
+size_t batch_smem_nv(int shape)
+{
+  switch (shape) {
+    case 1: return stage_smem_bytes<NV, Tile2D<16, 16>>();
+    case 2: return stage_smem_bytes<NV, Tile2D<64, 4>>();
+    case 3: return stage_smem_bytes<NV, Shape3>();
+    default: return stage_smem_bytes<NV, Tile2D<32, 8>>();
+  }
+}
+
+}  // namespace ps

@@ -30,13 +30,24 @@ struct Params {
   int dims, nvar, limiter, solver, cooling;
   int char_lim;           // PLM on characteristic variables (spherical path)
   int shock;              // MULTID shock flattening (spherical path)
+  int entropy;            // ENTROPY_SWITCH: 0 NO, 1 SELECTIVE, 2 ALWAYS (entropy = last var)
   int nx[3], ntot[3], beg[3];
   int px;                 // row pitch of device arrays (elements)
+  int xoff;               // column of cell i = 0 within a pitched row: 1 when the
+                          // ghost count is odd (3 with MULTID), so that every stage
+                          // tile's TMA load starts on a 16-byte boundary; else 0
   long long vstride;      // elements between variables
   int bc[6];
   double gamma, gmm1;
   double cfl, cfl_max_var, tstop, first_dt;
 };
+
+// FlagShock runs at the start of a step for MULTID shock flattening and
+// for ENTROPY_SWITCH SELECTIVE
+__host__ __device__ inline bool needs_shock_flags(const Params &p)
+{
+  return p.shock || p.entropy == 1;
+}
 
 struct StageArgs {
   const double *Vn;       // V^n (stage 2 reads it at the own cell)

@@ -4,9 +4,14 @@
 // the dbl.out log line (write_data.c:420-448), and reading such a file back
 // into a context, as RestartFromFile does for .dbl data (Src/restart.c:104-
 // 170).  The layout: every variable in Data.Vc order, each over the active
-// cells with x fastest, as native little-endian doubles.
+// cells with x fastest, as native little-endian doubles.  The entropy of
+// ENTROPY_SWITCH contexts is not written (Src/set_output.c:177-179); on
+// reading it is set from the pressure and density, as the next Boundary()
+// would.
 #include "ps_ctx.cuh"
+#include "ps_physics.cuh"
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -33,6 +38,9 @@ static size_t total_cells(const ps_ctx *c)
   return (size_t)c->p.ntot[0] * c->p.ntot[1] * c->p.ntot[2];
 }
 
+// variables written to / read from .dbl files
+static int dumped_vars(const ps_ctx *c) { return c->p.entropy ? c->p.nvar - 1 : c->p.nvar; }
+
 extern "C" int ps_write_dbl(ps_ctx *c, const char *dir, int nfile, const char *names)
 {
   if (!c || !dir || nfile < 0) return io_fail("ps_write_dbl: bad arguments");
@@ -47,7 +55,7 @@ extern "C" int ps_write_dbl(ps_ctx *c, const char *dir, int nfile, const char *n
   if (!f) return io_fail(std::string("ps_write_dbl: cannot open ") + fname);
   const size_t plane = (size_t)p.ntot[0] * p.ntot[1];
   bool ok = true;
-  for (int nv = 0; nv < p.nvar && ok; nv++)
+  for (int nv = 0; nv < dumped_vars(c) && ok; nv++)
     for (int k = p.beg[2]; k < p.beg[2] + p.nx[2] && ok; k++)
       for (int j = p.beg[1]; j < p.beg[1] + p.nx[1] && ok; j++) {
         const double *row = V.data() + nv * total_cells(c) + k * plane + (size_t)j * p.ntot[0] +
@@ -79,7 +87,7 @@ extern "C" int ps_write_dbl(ps_ctx *c, const char *dir, int nfile, const char *n
     if (vars.back() != ' ') vars += ' ';
   } else {
     static const char *base[5] = {"rho", "vx1", "vx2", "vx3", "prs"};
-    for (int nv = 0; nv < p.nvar; nv++) {
+    for (int nv = 0; nv < dumped_vars(c); nv++) {
       if (nv < 5)
         vars += base[nv];
       else
@@ -110,10 +118,10 @@ extern "C" int ps_read_dbl(ps_ctx *c, const char *path)
   std::fseek(f, 0, SEEK_END);
   const long size = std::ftell(f);
   std::fseek(f, 0, SEEK_SET);
-  if (size != (long)(nact * p.nvar * sizeof(double))) {
+  if (size != (long)(nact * dumped_vars(c) * sizeof(double))) {
     std::fclose(f);
     return io_fail(std::string("ps_read_dbl: ") + path + " does not hold " +
-                   std::to_string(p.nvar) + " variables over " + std::to_string(nact) +
+                   std::to_string(dumped_vars(c)) + " variables over " + std::to_string(nact) +
                    " active cells");
   }
   std::vector<double> V((size_t)p.nvar * total_cells(c));
@@ -124,7 +132,7 @@ extern "C" int ps_read_dbl(ps_ctx *c, const char *path)
   }
   const size_t plane = (size_t)p.ntot[0] * p.ntot[1];
   bool ok = true;
-  for (int nv = 0; nv < p.nvar && ok; nv++)
+  for (int nv = 0; nv < dumped_vars(c) && ok; nv++)
     for (int k = p.beg[2]; k < p.beg[2] + p.nx[2] && ok; k++)
       for (int j = p.beg[1]; j < p.beg[1] + p.nx[1] && ok; j++) {
         double *row = V.data() + nv * total_cells(c) + k * plane + (size_t)j * p.ntot[0] + p.beg[0];
@@ -132,5 +140,10 @@ extern "C" int ps_read_dbl(ps_ctx *c, const char *path)
       }
   std::fclose(f);
   if (!ok) return io_fail(std::string("ps_read_dbl: short read: ") + path);
+  if (p.entropy) {
+    const size_t n = total_cells(c);
+    for (size_t q = 0; q < n; q++)
+      V[(p.nvar - 1) * n + q] = V[ps::PRS * n + q] / std::pow(V[ps::RHO * n + q], p.gamma);
+  }
   return ps_set_state(c, V.data());
 }

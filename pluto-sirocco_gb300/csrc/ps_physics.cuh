@@ -79,8 +79,12 @@ __device__ __forceinline__ void prim_to_cons(const double (&v)[NV], double (&u)[
 // Returns device flag bits; u may be repaired in place as in the reference.
 template <int NV>
 __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV],
-                                                 double gmm1)
+                                                 double gmm1, int ent = 0)
 {
+  // ent (ENTROPY_SWITCH, the entropy is variable NV-1): 0 switch off;
+  // 1 pressure from the energy, then rho s redefined from it; 2 the zone is
+  // tagged FLAG_ENTROPY, p = (rho s) rho^(gamma-1) and the energy redefined
+  // (Src/HD/mappers.c:185-221)
   unsigned flag = 0;
   const double m2 = u[VX1] * u[VX1] + u[VX2] * u[VX2] + u[VX3] * u[VX3];
   if (u[RHO] < 0.0) {
@@ -97,11 +101,27 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
     u[PRS] = kSmallPressure / gmm1 + kin;
     flag |= F_CONS2PRIM;
   }
-  v[PRS] = gmm1 * (u[PRS] - kin);
-  if (v[PRS] < 0.0) {
-    v[PRS] = kSmallPressure;
-    u[PRS] = v[PRS] / gmm1 + kin;
-    flag |= F_CONS2PRIM;
+  if constexpr (NV > NFLX + 1) {
+    if (ent == 2) {
+      const double rhog1 = pow(u[RHO], gmm1);
+      v[PRS] = u[NV - 1] * rhog1;
+      if (v[PRS] < 0.0) {
+        v[PRS] = kSmallPressure;
+        flag |= F_CONS2PRIM;
+      }
+      u[PRS] = v[PRS] / gmm1 + kin;
+    }
+  }
+  if (ent != 2) {
+    v[PRS] = gmm1 * (u[PRS] - kin);
+    if (v[PRS] < 0.0) {
+      v[PRS] = kSmallPressure;
+      u[PRS] = v[PRS] / gmm1 + kin;
+      flag |= F_CONS2PRIM;
+    }
+    if constexpr (NV > NFLX + 1) {
+      if (ent == 1) u[NV - 1] = v[PRS] / pow(u[RHO], gmm1);
+    }
   }
 #pragma unroll
   for (int nv = NFLX; nv < NV; nv++) v[nv] = u[nv] * tau;
@@ -112,10 +132,12 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
 // vR the - state of the right cell, VN the normal velocity index.
 // Outputs the numerical flux (pressure kept apart, as with
 // USE_PRS_GRADIENT), the interface pressure and cmax = max(|SL|, |SR|).
+// `hll`: HLLC takes the HLL flux at this interface (FLAG_HLL on either
+// side with SHOCK_FLATTENING MULTID, Src/HD/hllc.c:93-104).
 template <int NV, int SOLVER, int VN>
 __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&vR)[NV],
                                         double gam, double gmm1, double (&f)[NV],
-                                        double &pr, double &cmax)
+                                        double &pr, double &cmax, bool hll = false)
 {
   double uL[NV], uR[NV];
   prim_to_cons<NV>(vL, uL, gmm1);
@@ -141,7 +163,7 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
     f[VX3] = uR[VX3] * vR[VN];
     f[PRS] = (uR[PRS] + vR[PRS]) * vR[VN];
     pr = vR[PRS];
-  } else if constexpr (SOLVER == HLL) {
+  } else if (SOLVER == HLL || hll) {
     double fL[NFLX], fR[NFLX];
     fL[RHO] = uL[VN];
     fL[VX1] = uL[VX1] * vL[VN];

@@ -50,7 +50,7 @@ template <int NV>
 __global__ void k_wind_bnd_x2(double *V, const Params p, Scalars *sc)
 {
   if (sc->done) return;
-  const int n = p.ntot[0] * 4;
+  const int n = p.ntot[0] * 2 * p.beg[1];
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
     bnd_x2_item<NV>(V, p, q);
 }
@@ -101,17 +101,25 @@ static const void *pick_sph(int stage)
                     : reinterpret_cast<const void *>(&k_stage_sph<NV, LIM, SOLVER, 2>);
 }
 
+template <int NV>
+static const void *stage_kernel_sph_nv(int lim, int solver, int stage)
+{
+  if (solver == HLL) {
+    if (lim == LIM_VL) return pick_sph<NV, LIM_VL, HLL>(stage);
+    if (lim == LIM_MM) return pick_sph<NV, LIM_MM, HLL>(stage);
+    return pick_sph<NV, LIM_MC, HLL>(stage);
+  }
+  if (lim == LIM_VL) return pick_sph<NV, LIM_VL, HLLC>(stage);
+  if (lim == LIM_MM) return pick_sph<NV, LIM_MM, HLLC>(stage);
+  return pick_sph<NV, LIM_MC, HLLC>(stage);
+}
+
+// nv 6: rho, v1, v2, v3, p, tracer; 7: and the entropy (ENTROPY_SWITCH)
 static const void *stage_kernel_sph(int nv, int lim, int solver, int stage)
 {
-  if (nv != 6) return nullptr;
-  if (solver == HLL) {
-    if (lim == LIM_VL) return pick_sph<6, LIM_VL, HLL>(stage);
-    if (lim == LIM_MM) return pick_sph<6, LIM_MM, HLL>(stage);
-    return pick_sph<6, LIM_MC, HLL>(stage);
-  }
-  if (lim == LIM_VL) return pick_sph<6, LIM_VL, HLLC>(stage);
-  if (lim == LIM_MM) return pick_sph<6, LIM_MM, HLLC>(stage);
-  return pick_sph<6, LIM_MC, HLLC>(stage);
+  if (nv == 6) return stage_kernel_sph_nv<6>(lim, solver, stage);
+  if (nv == 7) return stage_kernel_sph_nv<7>(lim, solver, stage);
+  return nullptr;
 }
 
 }  // namespace ps
@@ -155,8 +163,9 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
 {
   if (!c || !wp) return wind_fail("ps_set_wind: null argument");
   const ps::Params &p = c->p;
-  if (c->cfg.geometry != PS_SPHERICAL || p.dims != 2 || p.nvar != 6)
-    return wind_fail("ps_set_wind: needs a 2-D spherical context with NVAR = 6");
+  if (c->cfg.geometry != PS_SPHERICAL || p.dims != 2 || p.nvar != (p.entropy ? 7 : 6))
+    return wind_fail("ps_set_wind: needs a 2-D spherical context with NVAR = 6 (7 with the "
+                     "entropy switch)");
   if (c->grid_mask != 3) return wind_fail("ps_set_wind: call ps_set_grid for both directions first");
   if (wp->line_force && (!flux_r || !flux_t || !flux_p))
     return wind_fail("ps_set_wind: the line force needs the three flux arrays");
@@ -325,7 +334,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   WTRY(cudaMalloc(&w->tr, (size_t)p.vstride * sizeof(double)));
   WTRY(cudaMemset(w->xi, 0, (size_t)p.vstride * sizeof(double)));
   WTRY(cudaMemset(w->tr, 0, (size_t)p.vstride * sizeof(double)));
-  if (p.shock) {
+  if (ps::needs_shock_flags(p)) {
     WTRY(cudaMalloc(&w->shock, (size_t)p.vstride));
     WTRY(cudaMemset(w->shock, 0, (size_t)p.vstride));
   }
@@ -411,7 +420,8 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
 
   w->k1 = ps::stage_kernel_sph(p.nvar, p.limiter, p.solver, 1);
   w->k2 = ps::stage_kernel_sph(p.nvar, p.limiter, p.solver, 2);
-  w->smem = ps::stage_smem_bytes<6, ps::TileT<2>>();
+  w->smem = p.nvar == 7 ? ps::stage_smem_bytes<7, ps::TileT<2>>()
+                        : ps::stage_smem_bytes<6, ps::TileT<2>>();
   if (!w->k1 || !w->k2) {
     ps_wind_free(w);
     return wind_fail("ps_set_wind: no kernel for this configuration");
@@ -440,12 +450,17 @@ int ps_wind_bnd_launch(ps_ctx *c, int stage)
   WindDev *w = c->wind;
   const ps::Params &p = c->p;
   const int nb = (p.nx[0] * p.nx[1] + 255) / 256;
-  const int nb2 = (p.ntot[0] * 4 + 255) / 256;
+  const int nb2 = (p.ntot[0] * 2 * p.beg[1] + 255) / 256;
   double *Vin = stage == 1 ? c->V : c->Vs;
-  ps::k_wind_bnd_x1<6><<<nb, 256, 0, c->stream>>>(Vin, c->Us, p, w->a.w, c->sc, stage);
-  ps::k_wind_bnd_x2<6><<<nb2, 256, 0, c->stream>>>(Vin, p, c->sc);
+  if (p.nvar == 7) {
+    ps::k_wind_bnd_x1<7><<<nb, 256, 0, c->stream>>>(Vin, c->Us, p, w->a.w, c->sc, stage);
+    ps::k_wind_bnd_x2<7><<<nb2, 256, 0, c->stream>>>(Vin, p, c->sc);
+  } else {
+    ps::k_wind_bnd_x1<6><<<nb, 256, 0, c->stream>>>(Vin, c->Us, p, w->a.w, c->sc, stage);
+    ps::k_wind_bnd_x2<6><<<nb2, 256, 0, c->stream>>>(Vin, p, c->sc);
+  }
   c->launches += 2;
-  if (stage == 1 && p.shock) {
+  if (stage == 1 && ps::needs_shock_flags(p)) {
     const int nb3 = (p.ntot[0] * p.ntot[1] + 255) / 256;
     ps::k_wind_shock<<<nb3, 256, 0, c->stream>>>(w->shock, c->V, p, w->a.g, c->sc);
     c->launches++;
@@ -533,7 +548,8 @@ extern "C" int ps_set_sirocco(ps_ctx *c, const double *xi, const double *t_r, co
   if (e != cudaSuccess) return wind_cuda(e, "ps_set_sirocco");
   auto upload = [&](const double *src, double *dst) -> cudaError_t {
     // host [j][i] rows of n0 -> device rows of px
-    return cudaMemcpy2D(dst, (size_t)p.px * sizeof(double), src, (size_t)n0 * sizeof(double),
+    return cudaMemcpy2D(dst + p.xoff, (size_t)p.px * sizeof(double), src,
+                        (size_t)n0 * sizeof(double),
                         (size_t)n0 * sizeof(double), (size_t)n1, cudaMemcpyHostToDevice);
   };
   if (xi && (e = upload(xi, w->xi)) != cudaSuccess) return wind_cuda(e, "ps_set_sirocco: xi");

@@ -118,13 +118,13 @@ __device__ __forceinline__ void char_slopes(const double (&v)[NV], const double 
 
 __device__ __forceinline__ long long vcell(const Params &p, int gj, int gi)
 {
-  return (long long)gj * p.px + gi;
+  return (long long)gj * p.px + gi + p.xoff;
 }
 
-// FlagShock's test for one zone of the 2-D spherical grid with
-// SHOCK_FLATTENING MULTID (Src/flag_shock.c:147-200): div v < 0 from the
-// face areas and volume, and a pressure jump sum_d |p_{+1} - p_{-1}| above
-// 5 min(p, neighbours).  Zones of the outer ring are never tested.
+// FlagShock's test for one zone of the 2-D spherical grid
+// (Src/flag_shock.c:156-270): div v < 0 from the face areas and volume, and
+// the pressure jump sum_d |p_{+1} - p_{-1}| against min(p, neighbours).
+// Zones of the outer ring are never tested.
 __device__ __forceinline__ unsigned char shock_zone(const double *V, const Params &p,
                                                     const SphGeom &g, int gi, int gj)
 {
@@ -142,12 +142,14 @@ __device__ __forceinline__ unsigned char shock_zone(const double *V, const Param
   pt_min = dmin(pt_min, pmin1);
   pt_min = dmin(pt_min, pmin2);
   const double gradp = fabs(pt[c + sx] - pt[c - sx]) + fabs(pt[c + sy] - pt[c - sy]);
-  return gradp > 5.0 * pt_min ? 1 : 0;
+  // bit 0: shocked for the flattening (EPS_PSHOCK_FLATTEN 5); bit 1: taken
+  // off the entropy with ENTROPY_SWITCH SELECTIVE (EPS_PSHOCK_ENTROPY 0.05)
+  return (gradp > 5.0 * pt_min ? 1 : 0) | (gradp > 0.05 * pt_min ? 2 : 0);
 }
 
 __device__ __forceinline__ long long vcell3(const Params &p, int gk, int gj, int gi)
 {
-  return ((long long)gk * p.ntot[1] + gj) * p.px + gi;
+  return ((long long)gk * p.ntot[1] + gj) * p.px + gi + p.xoff;
 }
 
 // Active cell q (x fastest) -> (gi, gj, gk) of the total box.
@@ -210,27 +212,30 @@ __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params 
         for (int nv = 0; nv < NV; nv++) Us[nv * p.vstride + c] = u[nv];
       }
     }
-    const int b = p.beg[0], e = p.beg[0] + p.nx[0] - 1, nn = p.nx[0];
+    // ghost layers: 2, or 3 with SHOCK_FLATTENING MULTID (GetNghost)
+    const int b = p.beg[0], e = p.beg[0] + p.nx[0] - 1, nn = p.nx[0], ng = p.beg[0];
 #pragma unroll
     for (int side = 0; side < 2; side++) {
       const int type = p.bc[side];
-      int t0 = -1, t1 = -1;
+      int tg[3] = {-1, -1, -1};
       bool flip = false, inflow = false;
       if (type == BC_OUTFLOW || type == PS_BC_USERDEF) {
-        if (side == 0 && gi == b) { t0 = b - 1; t1 = b - 2; }
-        if (side == 1 && gi == e) { t0 = e + 1; t1 = e + 2; }
+        for (int k = 0; k < ng; k++) {
+          if (side == 0 && gi == b) tg[k] = b - 1 - k;
+          if (side == 1 && gi == e) tg[k] = e + 1 + k;
+        }
         inflow = (type == PS_BC_USERDEF) && side == 0;
       } else if (type == BC_PERIODIC) {
-        if (side == 0 && gi >= e - 1) t0 = gi - nn;
-        if (side == 1 && gi <= b + 1) t0 = gi + nn;
+        if (side == 0 && gi >= e - (ng - 1)) tg[0] = gi - nn;
+        if (side == 1 && gi <= b + (ng - 1)) tg[0] = gi + nn;
       } else if (type == BC_REFLECTIVE || type == BC_AXISYM || type == BC_EQTSYM) {
         flip = true;
-        if (side == 0 && gi <= b + 1) t0 = 2 * b - 1 - gi;
-        if (side == 1 && gi >= e - 1) t0 = 2 * e + 1 - gi;
+        if (side == 0 && gi <= b + (ng - 1)) tg[0] = 2 * b - 1 - gi;
+        if (side == 1 && gi >= e - (ng - 1)) tg[0] = 2 * e + 1 - gi;
       }
 #pragma unroll
-      for (int wi = 0; wi < 2; wi++) {
-        const int t = wi == 0 ? t0 : t1;
+      for (int wi = 0; wi < 3; wi++) {
+        const int t = tg[wi];
         if (t < 0) continue;
         const long long g = vcell(p, gj, t);
 #pragma unroll
@@ -252,9 +257,9 @@ __device__ __forceinline__ void bnd_x2_item(double *V, const Params &p, int q)
 {
   {
     const int gi = q % p.ntot[0], r = q / p.ntot[0];
-    const int side = r / 2;
+    const int ng = p.beg[1], side = r / ng, layer = r % ng;
     const int b = p.beg[1], e = p.beg[1] + p.nx[1] - 1, nn = p.nx[1];
-    const int gj = side == 0 ? b - 1 - (r & 1) : e + 1 + (r & 1);
+    const int gj = side == 0 ? b - 1 - layer : e + 1 + layer;
     const int type = p.bc[2 + side];
     int src;
     bool flip = false;
@@ -436,7 +441,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
       if (ci >= 1 && cj >= 1 && ci <= p.ntot[0] - 2 && cj <= p.ntot[1] - 2) {
         const unsigned char *S = A.shock;
         const long long c = vcell(p, cj, ci);
-        minmod = (S[c] | S[c - 1] | S[c + 1] | S[c - p.px] | S[c + p.px]) != 0;
+        minmod = ((S[c] | S[c - 1] | S[c + 1] | S[c - p.px] | S[c + p.px]) & 1) != 0;
       }
     }
     if (p.char_lim) {
@@ -479,7 +484,18 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
       vL[nv] = svp[nv * G::NPMAX + pl];
       vR[nv] = svm[nv * G::NPMAX + pl + PST];
     }
-    riemann<NV, SOLVER, VN>(vL, vR, gam, gmm1, f, pr, cmx);
+    bool hll = false;
+    if constexpr (SOLVER == HLLC) {
+      if (p.shock) {
+        // FLAG_HLL: the zone on either side of the face is shocked
+        const int ci = p.beg[0] + ox + fx - (D == 0), cj = p.beg[1] + oy + fy - (D == 1);
+        if (ci + (D == 0) <= p.ntot[0] - 1 && cj + (D == 1) <= p.ntot[1] - 1) {
+          const long long c = vcell(p, cj, ci);
+          hll = ((A.shock[c] | A.shock[c + (D == 0 ? 1 : p.px)]) & 1) != 0;
+        }
+      }
+    }
+    riemann<NV, SOLVER, VN>(vL, vR, gam, gmm1, f, pr, cmx, hll);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) sf[nv * G::NFMAX + q] = f[nv];
     spr[q] = pr;
@@ -603,7 +619,8 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
   __syncthreads();
   if (tid == 0) {
     mbar_expect_tx(bar, (uint32_t)(NV * G::VS * sizeof(double)));
-    tma_load_4d(sv, tm, ox + p.beg[0] - TL::HX, oy + p.beg[1] - TL::HY, 0, 0, bar);
+    // x counts memory columns: an even x (16-byte start) for every tile
+    tma_load_4d(sv, tm, ox + p.beg[0] - TL::HX + p.xoff, oy + p.beg[1] - TL::HY, 0, 0, bar);
   }
   const bool landed = mbar_wait_bounded(bar, 0, 1u << 22);
   if (!__syncthreads_and(landed)) {
@@ -613,11 +630,19 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
     }
     return;
   }
+  if constexpr (NV == NFLX + 2) {
+    // ENTROPY_SWITCH: the entropy of every zone of the tile, s = p / rho^gamma,
+    // as ComputeEntropy leaves it after Boundary (Src/entropy_switch.c:14-37);
+    // the stored entropy plane is not read
+    for (int k = tid; k < G::VS; k += G::NT)
+      sv[(NV - 1) * G::VS + k] = sv[PRS * G::VS + k] / pow(sv[RHO * G::VS + k], p.gamma);
+    __syncthreads();
+  }
 
   const int cx = tid % TL::X, cy = tid / TL::X;
   const bool own = tid < G::NC && (ox + cx < p.nx[0]) && (oy + cy < p.nx[1]);
   const int gi = p.beg[0] + ox + cx, gj = p.beg[1] + oy + cy;
-  const long long cell = (long long)gj * p.px + gi;
+  const long long cell = vcell(p, gj, gi);
   const double dt = a.sc->dt;
   const SphGeom &g = A.g;
 
@@ -684,11 +709,24 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       double v0[NV], U0[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
+      if constexpr (NV == NFLX + 2) v0[NV - 1] = v0[PRS] / pow(v0[RHO], p.gamma);
       prim_to_cons<NV>(v0, U0, p.gmm1);
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = 0.5 * U0[nv] + 0.5 * U[nv];
     }
-    flags |= cons_to_prim<NV>(U, v, p.gmm1);
+    int ent = 0;
+    if constexpr (NV == NFLX + 2) {
+      // FLAG_ENTROPY: every zone with ALWAYS; with SELECTIVE not in or next
+      // to a compressive zone with a pressure jump above 0.05 min(p)
+      ent = 2;
+      if (p.entropy == 1) {
+        const unsigned char *S = A.shock;
+        const unsigned char e = S[cell] | S[cell - 1] | S[cell + 1] | S[cell - p.px] |
+                                S[cell + p.px];
+        if (e & 2) ent = 1;
+      }
+    }
+    flags |= cons_to_prim<NV>(U, v, p.gmm1, ent);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++)
       if (is_nan_bits(v[nv])) flags |= F_NAN;

@@ -176,12 +176,14 @@ int ps_init_wind(const ps_config *cfg, const ps_wind *w, const double *x1,
   size_t nc;
   double gm_cgs, kelvin, rho_a;
   if (!cfg || !w || !x1 || !xl1 || !xr1 || !dx1 || !x2 || !xl2 || !xr2 || !Vc ||
-      cfg->dims != 2 || cfg->nvar != 6 || cfg->geometry != PS_SPHERICAL) {
-    ps_set_error_msg("ps_init_wind: needs a 2-D spherical configuration with nvar = 6");
+      cfg->dims != 2 || cfg->nvar != (cfg->entropy_switch ? 7 : 6) ||
+      cfg->geometry != PS_SPHERICAL) {
+    ps_set_error_msg("ps_init_wind: needs a 2-D spherical configuration with nvar = 6 "
+                     "(7 with the entropy switch)");
     return PS_EINVAL;
   }
-  n0 = cfg->nx[0] + 4;
-  n1 = cfg->nx[1] + 4;
+  n0 = cfg->nx[0] + 2 * PS_NGHOST(cfg);
+  n1 = cfg->nx[1] + 2 * PS_NGHOST(cfg);
   nc = (size_t)n0 * n1;
   gm_cgs = W_G * w->cent_mass;
   kelvin = w->unit_velocity * w->unit_velocity * W_AMU / W_KB;
@@ -216,6 +218,8 @@ int ps_init_wind(const ps_config *cfg, const ps_wind *w, const double *x1,
       Vc[3 * nc + c] = sqrt(gm_cgs / r) * sin(th) / w->unit_velocity;
       Vc[4 * nc + c] = rho * w->t_iso / (kelvin * w->mu);
       Vc[5 * nc + c] = trc;
+      /* ComputeEntropy of Startup's Boundary (Src/entropy_switch.c) */
+      if (cfg->entropy_switch) Vc[6 * nc + c] = Vc[4 * nc + c] / pow(rho, cfg->gamma);
     }
   }
   return 0;
@@ -234,18 +238,19 @@ int ps_wind_synthetic_flux(const ps_config *cfg, const ps_wind *w,
     ps_set_error_msg("ps_wind_synthetic_flux: bad arguments");
     return PS_EINVAL;
   }
-  n0 = cfg->nx[0] + 4;
-  n1 = cfg->nx[1] + 4;
+  const int ng = PS_NGHOST(cfg);
+  n0 = cfg->nx[0] + 2 * ng;
+  n1 = cfg->nx[1] + 2 * ng;
   nc = (size_t)n0 * n1;
   na = w->nangles;
   memset(fr, 0, (size_t)na * nc * sizeof(double));
   memset(ft, 0, (size_t)na * nc * sizeof(double));
   memset(fp, 0, (size_t)na * nc * sizeof(double));
   l_uv = w->l_star * w->f_uv;
-  for (j = 2; j < n1 - 2; j++) {
+  for (j = ng; j < n1 - ng; j++) {
     a = (int)floor(x2[j] / (2 * W_PI / 36));
     if (a < 0 || a >= na) continue;
-    for (i = 2; i < n0 - 2; i++) {
+    for (i = ng; i < n0 - ng; i++) {
       double r = x1[i] * w->unit_length;
       snprintf(buf, sizeof(buf), "%.12e", l_uv / (4 * 3.141592653589793 * r * r));
       fr[(size_t)a * nc + (size_t)j * n0 + i] = strtod(buf, NULL);

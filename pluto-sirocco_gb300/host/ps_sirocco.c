@@ -70,7 +70,7 @@ int ps_read_sirocco_fluxes(const ps_config *cfg, double unit_length, const doubl
   long count = 0;
   if (!cfg || !x1 || !x2 || !dir || !fr || !ft || !fp || max_angles <= 0 || !(unit_length > 0))
     return fail("ps_read_sirocco_fluxes: bad arguments");
-  const int n0 = cfg->nx[0] + 4, n1 = cfg->nx[1] + 4;
+  const int ng = PS_NGHOST(cfg), n0 = cfg->nx[0] + 2 * ng, n1 = cfg->nx[1] + 2 * ng;
   const size_t plane = (size_t)n0 * n1;
   char *line = (char *)malloc(PS_LINE);
   double *vals = (double *)malloc(sizeof(double) * (size_t)max_angles);
@@ -118,8 +118,8 @@ int ps_read_sirocco_fluxes(const ps_config *cfg, double unit_length, const doubl
         if (fscanf(f, "%le", &vals[a]) != 1)
           rc = fail("ps_read_sirocco_fluxes: error in reading a flux file");
       if (rc) break;
-      const int i = find_cell(x1, 2, cfg->nx[0], x1in / unit_length, match_ratio, 1e-6);
-      const int j = find_cell(x2, 2, cfg->nx[1], x2in, match_ratio, 1e-6);
+      const int i = find_cell(x1, ng, cfg->nx[0], x1in / unit_length, match_ratio, 1e-6);
+      const int j = find_cell(x2, ng, cfg->nx[1], x2in, match_ratio, 1e-6);
       if (i < 0 || j < 0) continue;
       for (int a = 0; a < na; a++) out[ax][(size_t)a * plane + (size_t)j * n0 + i] = vals[a];
       if (ax == 0) count++;
@@ -141,7 +141,7 @@ int ps_read_sirocco_heatcool(const ps_config *cfg, double unit_length, const dou
     return fail("ps_read_sirocco_heatcool: bad arguments");
   FILE *f = fopen(path, "r");
   if (!f) return fail("ps_read_sirocco_heatcool: cannot open the file");
-  const int n0 = cfg->nx[0] + 4;
+  const int ng = PS_NGHOST(cfg), n0 = cfg->nx[0] + 2 * ng;
   char *line = (char *)malloc(PS_LINE);
   if (!line) {
     fclose(f);
@@ -160,8 +160,8 @@ int ps_read_sirocco_heatcool(const ps_config *cfg, double unit_length, const dou
       rc = fail("ps_read_sirocco_heatcool: py_heatcool file incorrectly formatted");
       break;
     }
-    const int i = find_cell(x1, 2, cfg->nx[0], rcen / unit_length, match_rel, 1e-5);
-    const int j = find_cell(x2, 2, cfg->nx[1], thetacen, match_rel, 1e-5);
+    const int i = find_cell(x1, ng, cfg->nx[0], rcen / unit_length, match_rel, 1e-5);
+    const int j = find_cell(x2, ng, cfg->nx[1], thetacen, match_rel, 1e-5);
     if (i < 0 || j < 0) continue;
     const size_t c = (size_t)j * n0 + i;
     xi[c] = x < 1.0 ? 1.0 : x;
@@ -182,7 +182,7 @@ int ps_read_sirocco_prefactors(const ps_config *cfg, double unit_length, const d
     return fail("ps_read_sirocco_prefactors: bad arguments");
   FILE *f = fopen(path, "r");
   if (!f) return fail("ps_read_sirocco_prefactors: cannot open the file");
-  const int n0 = cfg->nx[0] + 4, n1 = cfg->nx[1] + 4;
+  const int ng = PS_NGHOST(cfg), n0 = cfg->nx[0] + 2 * ng, n1 = cfg->nx[1] + 2 * ng;
   const size_t plane = (size_t)n0 * n1;
   char *line = (char *)malloc(PS_LINE);
   if (!line) {
@@ -201,8 +201,8 @@ int ps_read_sirocco_prefactors(const ps_config *cfg, double unit_length, const d
       rc = fail("ps_read_sirocco_prefactors: prefactor file incorrectly formatted");
       break;
     }
-    const int i = find_cell(x1, 2, cfg->nx[0], rcen / unit_length, match_rel, 1e-5);
-    const int j = find_cell(x2, 2, cfg->nx[1], thetacen, match_rel, 1e-5);
+    const int i = find_cell(x1, ng, cfg->nx[0], rcen / unit_length, match_rel, 1e-5);
+    const int j = find_cell(x2, ng, cfg->nx[1], thetacen, match_rel, 1e-5);
     if (i < 0 || j < 0) continue;
     const size_t c = (size_t)j * n0 + i;
     for (int k = 0; k < 6; k++) pre[(size_t)k * plane + c] = v[k];

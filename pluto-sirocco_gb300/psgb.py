@@ -43,7 +43,8 @@ class Config(ctypes.Structure):
                 ("bc", ctypes.c_int * 6), ("gamma", ctypes.c_double), ("cfl", ctypes.c_double),
                 ("cfl_max_var", ctypes.c_double), ("tstop", ctypes.c_double),
                 ("first_dt", ctypes.c_double), ("cooling", ctypes.c_int),
-                ("char_limiting", ctypes.c_int), ("shock_flattening", ctypes.c_int)]
+                ("char_limiting", ctypes.c_int), ("shock_flattening", ctypes.c_int),
+                ("entropy_switch", ctypes.c_int)]
 
 
 class Wind(ctypes.Structure):
@@ -199,13 +200,17 @@ def check(rc, what):
 
 
 def make_wind_config(nr=512, nt=256, cooling=1, limiter="vl", solver="hll", cfl=0.4,
-                     first_dt=1e-4, char_limiting=0, shock_flattening=0):
-    c = make_config(dims=2, nx=(nr, nt, 1), nvar=6, limiter=limiter, solver=solver,
+                     first_dt=1e-4, char_limiting=0, shock_flattening=0, entropy_switch=0):
+    """The wind's configuration.  entropy_switch: 0 NO, 1 SELECTIVE, 2 ALWAYS
+    (the entropy becomes a seventh variable)."""
+    c = make_config(dims=2, nx=(nr, nt, 1), nvar=7 if entropy_switch else 6, limiter=limiter,
+                    solver=solver,
                     bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
                     cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling)
     c.geometry = SPHERICAL
     c.char_limiting = char_limiting
     c.shock_flattening = shock_flattening
+    c.entropy_switch = entropy_switch
     return c
 
 
@@ -213,18 +218,25 @@ class WindGrid:
     """r log-spaced on [10, 1000] x UNIT_LENGTH, theta uniform on [0, pi/2]."""
 
     def __init__(self, cfg):
-        self.ngh = [2, 2, 0]
-        self.ntot = [cfg.nx[0] + 4, cfg.nx[1] + 4, 1]
-        self.arrays = [build_grid(cfg.nx[0], 2, 10.0, 1000.0, "log"),
-                       build_grid(cfg.nx[1], 2, 0.0, 1.5707963267948966, "uniform"),
+        g = nghost(cfg)
+        self.ngh = [g, g, 0]
+        self.ntot = [cfg.nx[0] + 2 * g, cfg.nx[1] + 2 * g, 1]
+        self.arrays = [build_grid(cfg.nx[0], g, 10.0, 1000.0, "log"),
+                       build_grid(cfg.nx[1], g, 0.0, 1.5707963267948966, "uniform"),
                        build_grid(1, 0, 0.0, 1.0, "uniform")]
 
     def x(self, d):
         return self.arrays[d][0]
 
 
+def nghost(cfg):
+    """Ghost zones per side of an active direction (GetNghost): 2, or 3
+    with MULTID shock flattening."""
+    return 3 if cfg.shock_flattening else 2
+
+
 def wind_state(cfg, wind, grid):
-    V = np.zeros((6, 1, grid.ntot[1], grid.ntot[0]))
+    V = np.zeros((cfg.nvar, 1, grid.ntot[1], grid.ntot[0]))
     a1, a2 = grid.arrays[0], grid.arrays[1]
     check(lib().ps_init_wind(ctypes.byref(cfg), ctypes.byref(wind), _dp(a1[0]), _dp(a1[1]),
                              _dp(a1[2]), _dp(a1[3]), _dp(a2[0]), _dp(a2[1]), _dp(a2[2]),
@@ -524,11 +536,12 @@ def batch_models(n=64, seed=4):
     return out
 
 
-def wind_model_solver(spec, cooling=1, line_force=1, char_limiting=0, shock_flattening=0):
+def wind_model_solver(spec, cooling=1, line_force=1, char_limiting=0, shock_flattening=0,
+                      entropy_switch=0):
     """One wind context for a batch spec (see batch_models)."""
     nr, nt = spec["grid"]
     cfg = make_wind_config(nr, nt, cooling=cooling, char_limiting=char_limiting,
-                           shock_flattening=shock_flattening)
+                           shock_flattening=shock_flattening, entropy_switch=entropy_switch)
     w = make_wind(line_force=line_force, l_star=spec["l_star"], krad=spec["krad"],
                   alpharad=spec["alpharad"])
     g = WindGrid(cfg)

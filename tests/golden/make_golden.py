@@ -44,7 +44,7 @@ first_dt         1.e-4
 
 [Solver]
 
-Solver         hll
+Solver         {solver}
 
 [Boundary]
 
@@ -216,16 +216,26 @@ def write_flux_files(wd, nr, nt):
                             f"{x2[j]:.12e} {vals}\n")
 
 
-# name, ref config, (nr, nt), steps, snapshot every, with flux files
+# name, ref config, (nr, nt), steps, snapshot every, with flux files, and
+# the numerics switches of the ref config's definitions.h / pluto.ini
 WIND_CASES = [
-    ("wind2d_full_64x32", "wind2d", (64, 32), 200, 20, True),
-    ("wind2d_hydro_64x32", "wind2d_hydro", (64, 32), 100, 20, False),
-    ("wind2d_char_64x32", "wind2d_char", (64, 32), 100, 20, False),
-    ("wind2d_multid_64x32", "wind2d_multid", (64, 32), 100, 20, False),
+    ("wind2d_full_64x32", "wind2d", (64, 32), 200, 20, True, {}),
+    ("wind2d_hydro_64x32", "wind2d_hydro", (64, 32), 100, 20, False, {}),
+    ("wind2d_char_64x32", "wind2d_char", (64, 32), 100, 20, False, dict(char_limiting=1)),
+    ("wind2d_multid_64x32", "wind2d_multid", (64, 32), 100, 20, False,
+     dict(char_limiting=1, shock_flattening=1)),
+    ("wind2d_multid_hllc_64x32", "wind2d_multid_hllc", (64, 32), 100, 20, False,
+     dict(shock_flattening=1, solver="hllc")),
+    ("wind2d_entsel_64x32", "wind2d_entsel", (64, 32), 100, 20, False,
+     dict(entropy_switch=1)),
+    ("wind2d_idl_hydro_64x32", "wind2d_idl_hydro", (64, 32), 100, 20, False,
+     dict(char_limiting=1, shock_flattening=1, entropy_switch=2)),
+    ("wind2d_idl_64x32", "wind2d_idl", (64, 32), 200, 20, True,
+     dict(char_limiting=1, shock_flattening=1, entropy_switch=2)),
 ]
 
 
-def run_wind_case(ref, name, cfg, n, steps, every, flux):
+def run_wind_case(ref, name, cfg, n, steps, every, flux, opts):
     subprocess.run(["make", "-s", "-f", os.path.join(ORACLE, "ref.mk"), f"CFG={cfg}",
                     f"REF={ref}", "-j8"], check=True)
     exe = os.path.join(ORACLE, "_ref", cfg, "pluto")
@@ -233,7 +243,8 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux):
     shutil.rmtree(wd, ignore_errors=True)
     os.makedirs(wd)
     with open(os.path.join(wd, "pluto.ini"), "w") as f:
-        f.write(WIND_INI.format(nr=n[0], nt=n[1], every=every))
+        f.write(WIND_INI.format(nr=n[0], nt=n[1], every=every,
+                                solver=opts.get("solver", "hll")))
     if flux:
         write_flux_files(wd, n[0], n[1])
     subprocess.run([exe, "-maxsteps", str(steps - 1)], cwd=wd, check=True,
@@ -241,13 +252,16 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux):
     snaps = []
     for k in range(steps // every + 1):
         a = np.fromfile(os.path.join(wd, f"data.{k:04d}.dbl"), dtype="<f8")
+        # the entropy variable of ENTROPY_SWITCH is not written (set_output.c:177-179)
         snaps.append(a.reshape(6, n[1], n[0]))
     lines = [l.split() for l in open(os.path.join(wd, "dbl.out")).read().split("\n") if l]
     keep = sorted({0, 1, len(snaps) // 2, len(snaps) - 1})
     meta = dict(name=name, ref_config=cfg, kind="wind", dims=2, n=[n[0], n[1], 1],
                 steps=steps, snap_steps=[k * every for k in keep], cooling=int(flux),
-                line_force=int(flux), char_limiting=int("char" in cfg or "multid" in cfg),
-                shock_flattening=int("multid" in cfg),
+                line_force=int(flux), char_limiting=opts.get("char_limiting", 0),
+                shock_flattening=opts.get("shock_flattening", 0),
+                entropy_switch=opts.get("entropy_switch", 0),
+                solver=opts.get("solver", "hll"),
                 t=[lines[k][1] for k in keep],
                 dt=[lines[k][2] for k in keep], final_sha256=digest(snaps[-1]))
     snaps = np.stack([snaps[k] for k in keep])

@@ -69,11 +69,12 @@ def test_batch_tile_shapes_and_autotune(built):
 
 
 def test_batch_production_limiting_matches_individual_runs(built):
-    """Characteristic limiting and MULTID shock flattening (the limiting of
-    the production wind configuration) with cooling and the line force:
-    the batch's FlagShock pass and PLM give what each model gives alone."""
+    """Characteristic limiting, MULTID shock flattening and ENTROPY_SWITCH
+    ALWAYS (the numerics of the production wind configuration) with cooling
+    and the line force: the batch's FlagShock pass, PLM and entropy
+    recovery give what each model gives alone."""
     import psgb
-    kw = dict(cooling=1, line_force=1, char_limiting=1, shock_flattening=1)
+    kw = dict(cooling=1, line_force=1, char_limiting=1, shock_flattening=1, entropy_switch=2)
     solo = [psgb.wind_model_solver(s, **kw) for s in SPECS]
     inb = [psgb.wind_model_solver(s, **kw) for s in SPECS]
     batch = psgb.Batch(inb)
