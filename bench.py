@@ -62,9 +62,16 @@ METRIC = "cell-updates/s at 1 GB300 (FP64)"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
+# the numerics of the production cv_idl wind (definitions.h: CHAR_LIMITING
+# YES, SHOCK_FLATTENING MULTID, ENTROPY_SWITCH ALWAYS)
+IDL_NUMERICS = dict(char_limiting=1, shock_flattening=1, entropy_switch=2)
+
+
 class Workload:
-    def __init__(self, name):
+    def __init__(self, name, numerics="plm"):
         self.name = name
+        self.numerics = numerics
+        self.numerics_kw = IDL_NUMERICS if numerics == "idl" else {}
         if name == "wind":
             self.nx, self.ny, self.nvar = 512, 256, 6
             self.steps = 1000
@@ -109,6 +116,11 @@ class Workload:
         else:
             self.cells = self.nx * self.ny
         self.cooling = name in ("wind", "batch", "cube")
+        if numerics == "idl":
+            self.nvar = 7
+            self.desc += ("; production limiting: characteristic PLM, MULTID shock flattening,"
+                          " ENTROPY_SWITCH ALWAYS")
+            self.profile = "stage_kernel_wind_batch64_idl.md"
 
     def solver(self):
         """Device context with the initial state loaded."""
@@ -151,13 +163,13 @@ def _env_rank():
 # ----------------------------------------------------------------------
 
 def _cpu_worker(args):
-    name, steps, idx = args
-    wl = Workload(name)
+    name, steps, idx, numerics = args
+    wl = Workload(name, numerics)
     if name == "batch":
         from oracle import wind_oracle
         sp = wl.specs[idx % len(wl.specs)]
         o = wind_oracle(sp["grid"][0], sp["grid"][1], l_star=sp["l_star"], krad=sp["krad"],
-                        alpharad=sp["alpharad"])
+                        alpharad=sp["alpharad"], **wl.numerics_kw)
         cells = sp["grid"][0] * sp["grid"][1]
     elif name == "cube":
         import psgb
@@ -190,7 +202,7 @@ def cpu_throughput(wl, steps, procs=None):
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(n) as pool:
-        res = pool.map(_cpu_worker, [(wl.name, steps, i) for i in range(n)])
+        res = pool.map(_cpu_worker, [(wl.name, steps, i, wl.numerics) for i in range(n)])
     wall = time.perf_counter() - t0
     per = [r[0] for r in res]
     cells = sum(r[1] for r in res)
@@ -460,7 +472,7 @@ def batch_bench(wl, steps, warmup, rank, world):
     def make():
         out, V0s = [], []
         for sp in wl.specs:
-            s = psgb.wind_model_solver(sp)
+            s = psgb.wind_model_solver(sp, **wl.numerics_kw)
             s.set_stream(stream.cuda_stream)
             s.save()
             out.append(s)
@@ -781,8 +793,13 @@ def main():
     ap.add_argument("--workload", default="batch", choices=["wind", "blast", "batch", "cube"])
     ap.add_argument("--cube-n", type=int, default=512,
                     help="cells per direction of the cube workload (smaller cases for profiling)")
+    ap.add_argument("--numerics", default="plm", choices=["plm", "idl"],
+                    help="batch workload: primitive PLM (default) or the production cv_idl "
+                         "limiting (characteristic PLM, MULTID, entropy switch)")
     a = ap.parse_args()
-    wl = Workload(a.workload)
+    if a.numerics != "plm" and a.workload != "batch":
+        ap.error("--numerics idl is offered for the batch workload")
+    wl = Workload(a.workload, a.numerics)
     if a.workload == "cube" and a.cube_n != 512:
         wl.nx = wl.ny = wl.nz = a.cube_n
         wl.cells = a.cube_n ** 3

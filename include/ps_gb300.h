@@ -168,6 +168,10 @@ int ps_wind_synthetic_flux(const ps_config *cfg, const ps_wind *w,
  *     reference's floors xi >= 1, t_r >= 1e3 K.
  *   ps_read_sirocco_prefactors: prefactors.dat into six arrays in the
  *     file's order comp_h, comp_c, xray_h, brem_c, line_c, xi_ion.
+ *   ps_read_m_uv_fit: M_UV_data.dat, the force-multiplier table read when
+ *     KRAD = ALPHARAD = 999 (line_connect.c:182-257), into t_fit (the
+ *     table's t values) and m_fit ([point][j][i]), at most max_points
+ *     points; returns the number of points.
  * *matched (may be NULL) gets the number of records placed. */
 int ps_read_sirocco_fluxes(const ps_config *cfg, double unit_length, const double *x1,
                            const double *x2, const char *dir, int max_angles, double *fr,
@@ -177,6 +181,9 @@ int ps_read_sirocco_heatcool(const ps_config *cfg, double unit_length, const dou
                              long *matched);
 int ps_read_sirocco_prefactors(const ps_config *cfg, double unit_length, const double *x1,
                                const double *x2, const char *path, double *pre, long *matched);
+int ps_read_m_uv_fit(const ps_config *cfg, double unit_length, const double *x1,
+                     const double *x2, const char *path, int max_points, double *t_fit,
+                     double *m_fit, long *matched);
 
 /* ---------------------------------------------------------------- */
 /* device context                                                    */
@@ -281,6 +288,14 @@ int ps_set_cooling(ps_ctx *ctx, const ps_cooling *c);
  * learned cooling step leaves cells whose prefactors are not 1 to the
  * reference method. */
 int ps_set_sirocco(ps_ctx *ctx, const double *xi, const double *t_r, const double *pre);
+
+/* The tabulated force multiplier of a wind whose KRAD and ALPHARAD are both
+ * 999 (read_sirocco_fluxes, line_connect.c:182-257; LineForce with
+ * linterp, 858-887): the table's t values (npoints) and every cell's M
+ * ([point][j][i] over the total box), as M_UV_data.dat holds them
+ * (ps_read_m_uv_fit).  Such a wind does not step before this is called.
+ * Call before ps_batch_create for contexts that go into a batch. */
+int ps_set_mfit(ps_ctx *ctx, int npoints, const double *t_fit, const double *m_fit);
 
 /* No reference counterpart (the reference runs one model per process).
  * Advances n independent line-driven wind contexts (each already set up

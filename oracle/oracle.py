@@ -70,6 +70,7 @@ def lib():
         L.or_history.argtypes = [P, DP, DP, I]
         L.or_init_wind.argtypes = [P]
         L.or_set_flux.argtypes = [P, I, DP, DP, DP]
+        L.or_set_mfit.argtypes = [P, I, DP, DP]
         L.or_cooling.argtypes = [P, D, D]
         L.or_blondin_point.restype = D
         L.or_blondin_point.argtypes = [D, D, D, D, D, D]
@@ -89,6 +90,29 @@ WIND = dict(mu=0.6, rho_0=1.0e-9, cent_mass=1.4e34, t_iso=4.0e4, l_star=1.0e37, 
 WIND_GRID = dict(xbeg=(10.0, 0.0, 0.0), xend=(1000.0, 1.5707963267948966, 1.0),
                  gridtype=("log", "uniform", "uniform"))
 NANGLES = 36
+
+
+MFIT_POINTS = 21
+
+
+def synthetic_mfit(x1, x2, ntot, ngh=2, npoints=MFIT_POINTS):
+    """Synthetic force-multiplier table in the form M_UV_data.dat holds it
+    (read_sirocco_fluxes with KRAD = ALPHARAD = 999): t at npoints, log-spaced
+    1e-6..1e4, and per active cell M(t) = k t^a with k and a varying smoothly
+    over the grid; values rounded through 13 significant digits as the text
+    file carries them.  Returns t [npoints] and M [npoints][k][j][i] over the
+    total box (ghost cells 1)."""
+    import math
+    t = np.array([float("%.12e" % 10.0 ** (-6.0 + 10.0 * n / (npoints - 1)))
+                  for n in range(npoints)])
+    m = np.ones((npoints, ntot[2], ntot[1], ntot[0]))
+    for j in range(ngh, ntot[1] - ngh):
+        for i in range(ngh, ntot[0] - ngh):
+            k = 0.2 * (1.0 + 0.3 * math.sin(2.0 * x2[j]))
+            a = -0.6 + 0.05 * math.cos(x2[j]) * math.log10(x1[i] / 10.0)
+            for n in range(npoints):
+                m[n, :, j, i] = float("%.12e" % (k * t[n] ** a))
+    return t, m
 
 
 def synthetic_flux(x1, x2, ntot, l_uv=1.0e37, unit_length=1e9, na=NANGLES, ngh=2):
@@ -180,6 +204,12 @@ class Oracle:
         lib().or_set_flux(self.s, fr.shape[0], fr.ctypes.data_as(dp), ft.ctypes.data_as(dp),
                           fp.ctypes.data_as(dp))
 
+    def set_mfit(self, t, m):
+        """Tabulated force multiplier: t [npoints], M [npoints][k][j][i]."""
+        t, m = (np.ascontiguousarray(a, dtype=np.float64) for a in (t, m))
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib().or_set_mfit(self.s, len(t), t.ctypes.data_as(dp), m.ctypes.data_as(dp))
+
     def set_sirocco(self, xi=None, t_r=None, pre=None):
         """Per-cell sirocco_xi, sirocco_t_r and prefactors (6 arrays, file
         order), each over the total box."""
@@ -212,10 +242,13 @@ class Oracle:
 
 
 def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, char_limiting=0,
-                shock_flattening=0, solver="hll", entropy_switch=0, **params):
+                shock_flattening=0, solver="hll", entropy_switch=0, mfit=False, **params):
     """The 2-D spherical line-driven disk wind (PLM van Leer, HLL, RK2,
     userdef/outflow/axisymmetric/reflective boundaries, point-mass gravity,
-    floors, BLONDIN cooling and the line force), initialised."""
+    floors, BLONDIN cooling and the line force), initialised.  mfit: the
+    tabulated force multiplier (KRAD = ALPHARAD = 999, synthetic table)."""
+    if mfit:
+        params = dict(params, krad=999.0, alpharad=999.0)
     o = Oracle(dims=2, nx=(nr, nt, 1), nvar=7 if entropy_switch else 6, limiter="vl",
                solver=solver,
                bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
@@ -228,6 +261,8 @@ def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, c
         prm = dict(WIND, **params)
         o.set_flux(*synthetic_flux(o.grid(0), o.grid(1), o.ntot,
                                    l_uv=prm["l_star"] * prm["f_uv"], ngh=o.ngh[0]))
+    if mfit:   # KRAD = ALPHARAD = 999: the tabulated force multiplier
+        o.set_mfit(*synthetic_mfit(o.grid(0), o.grid(1), o.ntot, ngh=o.ngh[0]))
     o.init_wind()
     return o
 

@@ -84,6 +84,8 @@ struct or_sim {
   /* line-driven wind */
   int na;
   double *Fr, *Ft, *Fp;            /* [a][k][j][i] */
+  int nm;                          /* tabulated force multiplier: points */
+  double *t_fit, *m_fit;           /* log10 t [nm]; log10 M [nm][k][j][i] */
   double *xi_s, *tr_s;             /* sirocco_xi, sirocco_t_r */
   double *pre;                     /* 6 prefactor arrays (file order) or NULL: all 1 */
   unsigned char *flag;             /* FLAG_MINMOD bits of FlagShock, [k][j][i] */
@@ -305,6 +307,7 @@ void or_destroy(or_sim *s)
   free(s->dV); free(s->Ax1); free(s->Ax2); free(s->rvc);
   free(s->Fr); free(s->Ft); free(s->Fp); free(s->xi_s); free(s->tr_s); free(s->pre);
   free(s->flag);
+  free(s->t_fit); free(s->m_fit);
   free(s->dvds); free(s->roff); free(s->toff); free(s->moff);
   free(s->x11[0]); free(s->x11[1]); free(s->x22[0]); free(s->x22[1]);
   free(s->V); free(s->U); free(s->U0); free(s->Cdt);
@@ -530,6 +533,18 @@ void or_init_wind(or_sim *s)
   }
   s->dvds_ready = 0;
   if (s->c.entropy_switch) compute_entropy(s);   /* Startup's Boundary */
+}
+
+void or_set_mfit(or_sim *s, int npoints, const double *t_fit, const double *m_fit)
+{
+  size_t i, nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  free(s->t_fit); free(s->m_fit);
+  s->nm = npoints;
+  s->t_fit = malloc((size_t)npoints * sizeof(double));
+  s->m_fit = malloc((size_t)npoints * nc * sizeof(double));
+  /* the reader keeps log10 of what the file holds (line_connect.c:211, 228) */
+  for (i = 0; i < (size_t)npoints; i++) s->t_fit[i] = log10(t_fit[i]);
+  for (i = 0; i < (size_t)npoints * nc; i++) s->m_fit[i] = log10(m_fit[i]);
 }
 
 void or_set_flux(or_sim *s, int nangles, const double *fr, const double *ft, const double *fp)
@@ -945,7 +960,30 @@ static int vgrad_calc(or_sim *s)
   return 0;
 }
 
-/* LineForce (line_connect.c:815-903), power-law force multiplier */
+/* linterp (line_connect.c:778-808): first index whose abscissa is not
+ * below x by a linear scan, 10^ of the linear interpolant of log10 M, ends
+ * clamped */
+static double or_linterp(double x, const double *xa, const double *ya, size_t ystride, int n)
+{
+  int idx = 0;
+  double result;
+  while (idx < n && xa[idx] < x) idx++;
+  if (idx == 0) {
+    result = pow(10.0, ya[0]);
+  } else if (idx >= n) {
+    result = pow(10.0, ya[(size_t)(n - 1) * ystride]);
+  } else {
+    double x_low = xa[idx - 1], x_high = xa[idx];
+    double y_low = ya[(size_t)(idx - 1) * ystride], y_high = ya[(size_t)idx * ystride];
+    double slope = (y_high - y_low) / (x_high - x_low);
+    result = pow(10.0, y_low + slope * (x - x_low));
+  }
+  if (isnan(result)) result = 0.0;
+  return result;
+}
+
+/* LineForce (line_connect.c:815-903): power-law force multiplier, or the
+ * cell's tabulated M(t) when KRAD and ALPHARAD are both 999 */
 static void line_force(const or_sim *s, const double *v, size_t c, double *grad)
 {
   const double sigma_e = C_SIGMAT / C_AMU / 1.18;
@@ -964,7 +1002,12 @@ static void line_force(const or_sim *s, const double *v, size_t c, double *grad)
     double flux_r = s->Fr[q], flux_t = s->Ft[q], M_UV;
     if (s->dvds[q] > 0.0) {
       double t_UV = sigma_e * rho * v_th / s->dvds[q];
-      M_UV = krad * pow(t_UV, alpharad);
+      if (krad == 999 && alpharad == 999) {
+        size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+        M_UV = s->nm > 0 ? or_linterp(log10(t_UV), s->t_fit, s->m_fit + c, nc, s->nm) : 0.0;
+      } else {
+        M_UV = krad * pow(t_UV, alpharad);
+      }
       if (M_UV > M_max) M_UV = M_max;
     } else {
       M_UV = 0.0;

@@ -94,6 +94,11 @@ void    or_init_wind(or_sim *s);
 
 /* Directional UV fluxes, [angle][k][j][i] over the total box, for the
  * line force (flux_r_UV / flux_t_UV / flux_p_UV, Src/globals.h:191-210). */
+/* Tabulated force multiplier (read_sirocco_fluxes with KRAD = ALPHARAD =
+ * 999, Src/LineDriven/line_connect.c:182-257): t at npoints and the cells'
+ * M, [point][k][j][i] over the total box, as the file holds them (their
+ * log10 is kept). */
+void    or_set_mfit(or_sim *s, int npoints, const double *t_fit, const double *m_fit);
 void    or_set_flux(or_sim *s, int nangles, const double *fr, const double *ft,
                     const double *fp);
 

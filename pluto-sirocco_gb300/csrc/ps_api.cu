@@ -118,6 +118,7 @@ static int encode_map(ps_ctx *c, double *base, CUtensorMap *tm)
 void ps_wind_free(ps::WindDev *w);
 int ps_wind_step_launches(ps_ctx *c, int odd, int (*finish)(ps_ctx *, int));
 int ps_wind_hydro_launches(ps_ctx *c);
+int ps_wind_check(const ps_ctx *c, const char *who);
 int ps_wind_cool_launch(ps_ctx *c);
 int ps_wind_bnd_launch(ps_ctx *c, int stage);
 int ps_wind_stage_launch(ps_ctx *c, int stage);
@@ -509,6 +510,7 @@ extern "C" int ps_advance_step(ps_ctx *c, double dt, double *inv_dt_hyp)
     ps_set_error_msg("ps_advance_step: a spherical context needs ps_set_wind first");
     return PS_ESTATE;
   }
+  if ((r = ps_wind_check(c, "ps_advance_step"))) return r;
   ps::Scalars s;
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
@@ -629,6 +631,7 @@ extern "C" int ps_run(ps_ctx *c, int nsteps)
       ps_set_error_msg("ps_run: a spherical context needs ps_set_wind first");
       return PS_ESTATE;
     }
+    if ((r = ps_wind_check(c, "ps_run"))) return r;
     return run_wind(c, nsteps);
   }
   if (c->cool_on && c->p.cooling) return run_wind(c, nsteps);

@@ -23,6 +23,7 @@
 #include <vector>
 
 extern "C" void ps_set_error_msg(const char *msg);
+int ps_wind_check(const ps_ctx *c, const char *who);
 
 namespace ps {
 
@@ -126,15 +127,21 @@ __global__ void k_batch_finish(const BatchModel *__restrict__ models)
   finish_block(models[blockIdx.x].fin);
 }
 
-// stage kernels for the 6-variable state; the 7-variable ones (with the
-// entropy of ENTROPY_SWITCH) are instantiated in ps_batch7.cu
+// stage kernels for the 6-variable state with primitive PLM; the others
+// are instantiated in ps_batch_c.cu (characteristic limiting), ps_batch7.cu
+// and ps_batch_c7.cu (the 7-variable state of ENTROPY_SWITCH contexts)
+const void *batch_kernel_c6(int shape, int lim, int solver, int stage);
 const void *batch_kernel7(int shape, int lim, int solver, int stage);
+const void *batch_kernel_c7(int shape, int lim, int solver, int stage);
 size_t batch_smem7(int shape);
 
-static const void *batch_kernel(int nv, int shape, int lim, int solver, int stage)
+static const void *batch_kernel(int nv, bool ch, int shape, int lim, int solver, int stage)
 {
-  return nv == 7 ? batch_kernel7(shape, lim, solver, stage)
-                 : batch_kernel_nv<6>(shape, lim, solver, stage);
+  if (nv == 7)
+    return ch ? batch_kernel_c7(shape, lim, solver, stage)
+              : batch_kernel7(shape, lim, solver, stage);
+  return ch ? batch_kernel_c6(shape, lim, solver, stage)
+            : batch_kernel_nv<6, false>(shape, lim, solver, stage);
 }
 
 static size_t batch_smem(int nv, int shape)
@@ -171,6 +178,7 @@ struct ps_batch {
   int2 *sg_queue = nullptr;
   int *sg_qcount = nullptr;
   int lim = 0, solver = 0, cooling = 0, nvar = 6;
+  bool char_lim = false;  // CHAR_LIMITING YES (its own stage kernels)
   cudaStream_t stream = nullptr;      // stream the work is issued on
   cudaStream_t own_stream = nullptr;  // stream created by the batch
   cudaStream_t side[ps::kNumShapes] = {};  // tile-shape groups
@@ -327,7 +335,7 @@ static int batch_stage(ps_batch *b, int stage)
     if (!b->nitems[s]) continue;
     cudaStream_t st = s == first ? b->stream : b->side[s];
     if (s != first) BCK(cudaStreamWaitEvent(st, b->fork, 0));
-    const void *k = ps::batch_kernel(b->nvar, s, b->lim, b->solver, stage);
+    const void *k = ps::batch_kernel(b->nvar, b->char_lim, s, b->lim, b->solver, stage);
     void *args[2] = {&b->d_models, &b->d_items[s]};
     BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(ps::kShapeNT[s]), args, ps::batch_smem(b->nvar, s),
                          st));
@@ -430,11 +438,12 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
   for (int m = 0; m < n; m++) {
     ps_ctx *c = ctxs[m];
     if (!c || !c->wind) return batch_fail("ps_batch_create: every model needs ps_set_wind");
+    if (ps_wind_check(c, "ps_batch_create")) return PS_ESTATE;
     if (c->p.limiter != ctxs[0]->p.limiter || c->p.solver != ctxs[0]->p.solver ||
         c->p.cooling != ctxs[0]->p.cooling || c->host_step != ctxs[0]->host_step ||
-        c->p.nvar != ctxs[0]->p.nvar)
-      return batch_fail("ps_batch_create: models must share limiter, solver, cooling, variables "
-                        "and step");
+        c->p.nvar != ctxs[0]->p.nvar || c->p.char_lim != ctxs[0]->p.char_lim)
+      return batch_fail("ps_batch_create: models must share limiter, solver, characteristic "
+                        "limiting, cooling, variables and step");
   }
   ps_batch *b = new ps_batch();
   b->n = n;
@@ -445,6 +454,7 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
   b->solver = ctxs[0]->p.solver;
   b->cooling = ctxs[0]->p.cooling;
   b->nvar = ctxs[0]->p.nvar;
+  b->char_lim = ctxs[0]->p.char_lim != 0;
   b->host_step = ctxs[0]->host_step;
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -481,7 +491,7 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
   cudaMemcpy(b->d_pre, pre.data(), sizeof(double *) * n, cudaMemcpyHostToDevice);
   for (int s = 0; s < ps::kNumShapes; s++) {
     for (int st = 1; st <= 2; st++) {
-      e = cudaFuncSetAttribute(ps::batch_kernel(b->nvar, s, b->lim, b->solver, st),
+      e = cudaFuncSetAttribute(ps::batch_kernel(b->nvar, b->char_lim, s, b->lim, b->solver, st),
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)ps::batch_smem(b->nvar, s));
       if (e != cudaSuccess) {
@@ -565,7 +575,7 @@ extern "C" int ps_batch_autotune(ps_batch *b, int reps)
       BCK(cudaMalloc(&d_items, items.size() * sizeof(ps::TileItem)));
       BCK(cudaMemcpy(d_items, items.data(), items.size() * sizeof(ps::TileItem),
                      cudaMemcpyHostToDevice));
-      const void *k = ps::batch_kernel(b->nvar, s, b->lim, b->solver, 1);
+      const void *k = ps::batch_kernel(b->nvar, b->char_lim, s, b->lim, b->solver, 1);
       void *args[2] = {&b->d_models, &d_items};
       BCK(cudaLaunchKernel(k, dim3((unsigned)items.size()), dim3(ps::kShapeNT[s]), args,
                            ps::batch_smem(b->nvar, s), b->stream));

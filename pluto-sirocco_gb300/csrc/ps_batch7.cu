@@ -7,7 +7,7 @@ namespace ps {
 
 const void *batch_kernel7(int shape, int lim, int solver, int stage)
 {
-  return batch_kernel_nv<7>(shape, lim, solver, stage);
+  return batch_kernel_nv<7, false>(shape, lim, solver, stage);
 }
 
 size_t batch_smem7(int shape) { return batch_smem_nv<7>(shape); }

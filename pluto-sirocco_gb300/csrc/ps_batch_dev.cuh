@@ -27,7 +27,7 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap *tm)
   asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm) : "memory");
 }
 
-template <int NV, int LIM, int SOLVER, int STAGE, class TL>
+template <int NV, int LIM, int SOLVER, int STAGE, class TL, bool CHAR>
 __global__ void __launch_bounds__(TileGeom<TL>::NT)
     k_batch_stage(const BatchModel *__restrict__ models, const TileItem *__restrict__ items)
 {
@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(TileGeom<TL>::NT)
   const BatchModel &M = models[it.m];
   const CUtensorMap *tm = &M.tm[STAGE - 1];
   if (threadIdx.x == 0) tensormap_acquire(tm);
-  stage_sph_tile<NV, LIM, SOLVER, STAGE, TL>(tm, M.st[STAGE - 1], it.bx, it.by, smem_raw);
+  stage_sph_tile<NV, LIM, SOLVER, STAGE, TL, CHAR>(tm, M.st[STAGE - 1], it.bx, it.by, smem_raw);
 }
 
 // ------------------------------------------------------------------
@@ -51,34 +51,36 @@ const int kShapeY[kNumShapes] = {8, 16, 4, 16};
 const int kShapeNT[kNumShapes] = {256, 256, 256, 288};
 using Shape3 = Tile2D<16, 16, 32>;
 
-template <int NV, int LIM, int SOLVER, class TL>
+template <int NV, bool CHAR, int LIM, int SOLVER, class TL>
 const void *pick_batch(int stage)
 {
-  return stage == 1 ? reinterpret_cast<const void *>(&k_batch_stage<NV, LIM, SOLVER, 1, TL>)
-                    : reinterpret_cast<const void *>(&k_batch_stage<NV, LIM, SOLVER, 2, TL>);
+  return stage == 1
+             ? reinterpret_cast<const void *>(&k_batch_stage<NV, LIM, SOLVER, 1, TL, CHAR>)
+             : reinterpret_cast<const void *>(&k_batch_stage<NV, LIM, SOLVER, 2, TL, CHAR>);
 }
 
-template <int NV, class TL>
+template <int NV, bool CHAR, class TL>
 const void *pick_batch_shape(int lim, int solver, int stage)
 {
   if (solver == HLL) {
-    if (lim == LIM_VL) return pick_batch<NV, LIM_VL, HLL, TL>(stage);
-    if (lim == LIM_MM) return pick_batch<NV, LIM_MM, HLL, TL>(stage);
-    return pick_batch<NV, LIM_MC, HLL, TL>(stage);
+    if (lim == LIM_VL) return pick_batch<NV, CHAR, LIM_VL, HLL, TL>(stage);
+    if (lim == LIM_MM) return pick_batch<NV, CHAR, LIM_MM, HLL, TL>(stage);
+    return pick_batch<NV, CHAR, LIM_MC, HLL, TL>(stage);
   }
-  if (lim == LIM_VL) return pick_batch<NV, LIM_VL, HLLC, TL>(stage);
-  if (lim == LIM_MM) return pick_batch<NV, LIM_MM, HLLC, TL>(stage);
-  return pick_batch<NV, LIM_MC, HLLC, TL>(stage);
+  if (lim == LIM_VL) return pick_batch<NV, CHAR, LIM_VL, HLLC, TL>(stage);
+  if (lim == LIM_MM) return pick_batch<NV, CHAR, LIM_MM, HLLC, TL>(stage);
+  return pick_batch<NV, CHAR, LIM_MC, HLLC, TL>(stage);
 }
 
-template <int NV>
+// CHAR: CHAR_LIMITING YES
+template <int NV, bool CHAR>
 const void *batch_kernel_nv(int shape, int lim, int solver, int stage)
 {
   switch (shape) {
-    case 1: return pick_batch_shape<NV, Tile2D<16, 16>>(lim, solver, stage);
-    case 2: return pick_batch_shape<NV, Tile2D<64, 4>>(lim, solver, stage);
-    case 3: return pick_batch_shape<NV, Shape3>(lim, solver, stage);
-    default: return pick_batch_shape<NV, Tile2D<32, 8>>(lim, solver, stage);
+    case 1: return pick_batch_shape<NV, CHAR, Tile2D<16, 16>>(lim, solver, stage);
+    case 2: return pick_batch_shape<NV, CHAR, Tile2D<64, 4>>(lim, solver, stage);
+    case 3: return pick_batch_shape<NV, CHAR, Shape3>(lim, solver, stage);
+    default: return pick_batch_shape<NV, CHAR, Tile2D<32, 8>>(lim, solver, stage);
   }
 }
 

@@ -21,6 +21,7 @@
 #include "ps_stage.cuh"
 #include "ps_tma.cuh"
 #include "ps_wind.cuh"
+#include "ps_wind_kernels.cuh"
 
 #include <cudaTypedefs.h>
 
@@ -86,40 +87,14 @@ __global__ void k_blondin(double *V, const double *xi_s, const double *tr_s, con
     blondin_cell(V, xi_s, tr_s, p, w, x1, sc, dt, t, q, pre);
 }
 
-template <int NV, int LIM, int SOLVER, int STAGE>
-__global__ void __launch_bounds__(TileGeom<TileT<2>>::NT)
-    k_stage_sph(const __grid_constant__ CUtensorMap tm, const WindStageArgs A)
-{
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  stage_sph_tile<NV, LIM, SOLVER, STAGE, TileT<2>>(&tm, A, blockIdx.x, blockIdx.y, smem_raw);
-}
+// the single-model stage kernels (ps_wind_kernels.cuh): the primitive-PLM
+// 6-variable set here, the others in ps_wind_k.cu
+const void *stage_kernel_sph_other(int nv, bool ch, int lim, int solver, int stage);
 
-template <int NV, int LIM, int SOLVER>
-static const void *pick_sph(int stage)
+static const void *stage_kernel_sph(int nv, bool ch, int lim, int solver, int stage)
 {
-  return stage == 1 ? reinterpret_cast<const void *>(&k_stage_sph<NV, LIM, SOLVER, 1>)
-                    : reinterpret_cast<const void *>(&k_stage_sph<NV, LIM, SOLVER, 2>);
-}
-
-template <int NV>
-static const void *stage_kernel_sph_nv(int lim, int solver, int stage)
-{
-  if (solver == HLL) {
-    if (lim == LIM_VL) return pick_sph<NV, LIM_VL, HLL>(stage);
-    if (lim == LIM_MM) return pick_sph<NV, LIM_MM, HLL>(stage);
-    return pick_sph<NV, LIM_MC, HLL>(stage);
-  }
-  if (lim == LIM_VL) return pick_sph<NV, LIM_VL, HLLC>(stage);
-  if (lim == LIM_MM) return pick_sph<NV, LIM_MM, HLLC>(stage);
-  return pick_sph<NV, LIM_MC, HLLC>(stage);
-}
-
-// nv 6: rho, v1, v2, v3, p, tracer; 7: and the entropy (ENTROPY_SWITCH)
-static const void *stage_kernel_sph(int nv, int lim, int solver, int stage)
-{
-  if (nv == 6) return stage_kernel_sph_nv<6>(lim, solver, stage);
-  if (nv == 7) return stage_kernel_sph_nv<7>(lim, solver, stage);
-  return nullptr;
+  if (nv == 6 && !ch) return stage_kernel_sph_nv<6, false>(lim, solver, stage);
+  return stage_kernel_sph_other(nv, ch, lim, solver, stage);
 }
 
 }  // namespace ps
@@ -147,6 +122,8 @@ static int wind_cuda(cudaError_t e, const char *where)
 void ps_wind_free(ps::WindDev *w)
 {
   if (!w) return;
+  cudaFree(w->t_fit);
+  cudaFree(w->m_fit);
   cudaFree(w->geo);
   cudaFree(w->off);
   cudaFree(w->ent);
@@ -416,10 +393,15 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
     const double C = W.sigma_e * UD * std::sqrt(W.kelvin * W.mu * 2.0 * ps::kKB / ps::kMP);
     W.lf_a0 = std::log(W.krad) + W.alpharad * std::log(C);
     W.lf_cf = W.sigma_e / ps::kC / W.unit_acc;
+    // KRAD = ALPHARAD = 999 selects the tabulated force multiplier
+    // (line_connect.c:183, 858, 884); the table comes with ps_set_mfit
+    W.mfit = (W.krad == 999 && W.alpharad == 999) ? 1 : 0;
+    W.nm = 0;
+    W.lt0 = std::log10(C);
   }
 
-  w->k1 = ps::stage_kernel_sph(p.nvar, p.limiter, p.solver, 1);
-  w->k2 = ps::stage_kernel_sph(p.nvar, p.limiter, p.solver, 2);
+  w->k1 = ps::stage_kernel_sph(p.nvar, p.char_lim != 0, p.limiter, p.solver, 1);
+  w->k2 = ps::stage_kernel_sph(p.nvar, p.char_lim != 0, p.limiter, p.solver, 2);
   w->smem = p.nvar == 7 ? ps::stage_smem_bytes<7, ps::TileT<2>>()
                         : ps::stage_smem_bytes<6, ps::TileT<2>>();
   if (!w->k1 || !w->k2) {
@@ -568,5 +550,58 @@ extern "C" int ps_set_sirocco(ps_ctx *c, const double *xi, const double *t_r, co
         return wind_cuda(e, "ps_set_sirocco: prefactors");
   }
   ps_ctx_invalidate_graphs(c);
+  return 0;
+}
+
+// The tabulated force multiplier of KRAD = ALPHARAD = 999 runs
+// (read_sirocco_fluxes, line_connect.c:182-257): t at npoints and every
+// cell's M, [point][j][i] over the total box, as M_UV_data.dat holds them;
+// the log10 of each is kept, as the reader does.
+extern "C" int ps_set_mfit(ps_ctx *c, int npoints, const double *t_fit, const double *m_fit)
+{
+  if (!c || !c->wind) return wind_fail("ps_set_mfit: needs ps_set_wind first");
+  WindDev *w = c->wind;
+  if (!w->a.w.mfit) return wind_fail("ps_set_mfit: the wind's KRAD and ALPHARAD are not 999");
+  if (npoints < 1 || npoints > 4096 || !t_fit || !m_fit)
+    return wind_fail("ps_set_mfit: bad arguments");
+  const ps::Params &p = c->p;
+  const int n0 = p.ntot[0], n1 = p.ntot[1];
+  const size_t plane = (size_t)n0 * n1;
+  std::vector<double> lt(npoints), lm((size_t)npoints * plane);
+  for (int k = 0; k < npoints; k++) lt[k] = std::log10(t_fit[k]);
+  for (size_t q = 0; q < lm.size(); q++) lm[q] = std::log10(m_fit[q]);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return wind_cuda(e, "ps_set_mfit");
+  cudaFree(w->t_fit);
+  cudaFree(w->m_fit);
+  w->t_fit = w->m_fit = nullptr;
+  if ((e = cudaMalloc(&w->t_fit, npoints * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&w->m_fit, (size_t)npoints * p.vstride * sizeof(double))) != cudaSuccess)
+    return wind_cuda(e, "ps_set_mfit: allocation");
+  if ((e = cudaMemcpy(w->t_fit, lt.data(), npoints * sizeof(double), cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return wind_cuda(e, "ps_set_mfit: t");
+  for (int k = 0; k < npoints; k++)
+    if ((e = cudaMemcpy2D(w->m_fit + (size_t)k * p.vstride + p.xoff, (size_t)p.px * sizeof(double),
+                          lm.data() + (size_t)k * plane, (size_t)n0 * sizeof(double),
+                          (size_t)n0 * sizeof(double), (size_t)n1, cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+      return wind_cuda(e, "ps_set_mfit: M");
+  w->a.L.t_fit = w->t_fit;
+  w->a.L.m_fit = w->m_fit;
+  w->a.w.nm = npoints;
+  ps_ctx_invalidate_graphs(c);
+  return 0;
+}
+
+// A wind whose KRAD and ALPHARAD ask for the table cannot step without it.
+int ps_wind_check(const ps_ctx *c, const char *who)
+{
+  if (c->wind && c->wind->a.w.mfit && c->wind->a.w.nm == 0) {
+    char buf[160];
+    std::snprintf(buf, sizeof(buf), "%s: KRAD = ALPHARAD = 999 needs ps_set_mfit", who);
+    ps_set_error_msg(buf);
+    return PS_ESTATE;
+  }
   return 0;
 }

@@ -46,7 +46,11 @@ struct LineList {
   // point (c2a, c2b)
   const double *c1a, *c1b, *c2a, *c2b;
   const double *inv_ds;  // 1 / ds; 0 for a bin without direction (dv/ds = -999)
-  double *lq;            // per entry and stage: -alpharad * log(dv/ds), -inf if dv/ds <= 0
+  double *lq;            // per entry and stage: -alpharad * log(dv/ds) (power law) or
+                         // -log10(dv/ds) (table), -inf if dv/ds <= 0
+  // tabulated force multiplier (KRAD = ALPHARAD = 999): log10 t at the
+  // table's points and each cell's log10 M, [point][pitched cell]
+  const double *t_fit, *m_fit;
 };
 
 struct WindParams {
@@ -61,6 +65,10 @@ struct WindParams {
   // (code-unit rho and p): lf_a0 = log(krad) + alpharad log(C); the
   // acceleration per bin is (1 + M) F lf_cf
   double lf_a0, lf_cf;
+  // KRAD = ALPHARAD = 999: M from each cell's table, log10 t = lt0 +
+  // log10(rho p)/2 - log10(dv/ds) (lt0 = log10 C), nm points
+  int mfit, nm;
+  double lt0;
   // > 0: BLONDIN at this constant ionisation parameter with T_x (the
   // Cartesian cooling configuration); 0: xi from the state / sirocco_xi
   double xi_const;

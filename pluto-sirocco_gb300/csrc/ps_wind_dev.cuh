@@ -33,6 +33,7 @@ struct WindDev {
   double *xi = nullptr, *tr = nullptr;
   double *pre = nullptr;  // 5 prefactor arrays (ch, cc, xh, lc, bc), NULL: all 1
   unsigned char *shock = nullptr;  // SHOCK_FLATTENING MULTID: shocked zones, total box
+  double *t_fit = nullptr, *m_fit = nullptr;  // tabulated force multiplier (log10)
   long nent = 0;
   const void *k1 = nullptr, *k2 = nullptr;
   size_t smem = 0;
@@ -91,10 +92,13 @@ __device__ __forceinline__ void char_slopes(const double (&v)[NV], const double 
   wp[2] = dvp[RHO] + l2p * dvp[PRS];
   wp[3] = dvp[vt];
   wp[4] = dvp[vb];
+  if (minmod) {   // FLAG_MINMOD
 #pragma unroll
-  for (int k = 0; k < 5; k++)
-    wl[k] = minmod ? (wp[k] * wm[k] > 0.0 ? abs_min(wp[k], wm[k]) : 0.0)   // FLAG_MINMOD
-                   : limited_slope_general<LIM>(wp[k], wm[k], cp, cm);
+    for (int k = 0; k < 5; k++) wl[k] = wp[k] * wm[k] > 0.0 ? abs_min(wp[k], wm[k]) : 0.0;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 5; k++) wl[k] = limited_slope_general<LIM>(wp[k], wm[k], cp, cm);
+  }
   // dc = sum_k wl[k] R[nv][k] with the nonzero entries of the right
   // eigenvectors, in the order of k
   double dc[5];
@@ -389,13 +393,46 @@ __device__ __forceinline__ void bilinear_w(double fx, double fy, const double (&
 // (1 + M) sigma_e F / c, M = min(krad t^alpharad, 4400), t = sigma_e rho
 // v_th / (dv/ds), M = 0 where dv/ds <= 0.  Evaluated as
 // M = exp(lf_a0 + alpharad/2 log(rho p) + lq) with lq = -alpharad log(dv/ds)
-// from VGradCalc (one log per call, one exp per bin).
+// from VGradCalc (one log per call, one exp per bin).  With KRAD = ALPHARAD
+// = 999, M is interpolated in the cell's table at log10 t = lt0 +
+// log10(rho p)/2 + lq, lq = -log10(dv/ds).
 template <int NV>
 __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineList &L,
-                                             const WindParams &w, int e0, int e1, int comp)
+                                             const WindParams &w, int e0, int e1, int comp,
+                                             long long cell, long long vstride)
 {
-  const double base = w.lf_a0 + 0.5 * w.alpharad * log(vg[RHO] * vg[PRS]);
   double g = 0.0;
+  if (w.mfit) {
+    // linterp (line_connect.c:778-808) of the cell's log10 M over log10 t:
+    // the first point not below x by a linear scan, ends clamped
+    const double base = w.lt0 + 0.5 * log10(vg[RHO] * vg[PRS]);
+    const double *m = L.m_fit + cell;
+    for (int e = e0; e < e1; e++) {
+      double M = 0.0;
+      if (L.lq[e] != -INFINITY) {
+        const double x = base + L.lq[e];
+        int idx = 0;
+        while (idx < w.nm && L.t_fit[idx] < x) idx++;
+        double y;
+        if (idx == 0) {
+          y = m[0];
+        } else if (idx >= w.nm) {
+          y = m[(w.nm - 1) * vstride];
+        } else {
+          const double x_low = L.t_fit[idx - 1], y_low = m[(idx - 1) * vstride];
+          const double slope = (m[idx * vstride] - y_low) / (L.t_fit[idx] - x_low);
+          y = y_low + slope * (x - x_low);
+        }
+        M = exp10(y);
+        if (is_nan_bits(M)) M = 0.0;
+        if (M > 4400.) M = 4400.;
+      }
+      const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
+      g += (1.0 + M) * F;
+    }
+    return g * w.lf_cf;
+  }
+  const double base = w.lf_a0 + 0.5 * w.alpharad * log(vg[RHO] * vg[PRS]);
   for (int e = e0; e < e1; e++) {
     double M = exp(base + L.lq[e]);
     if (M > 4400.) M = 4400.;
@@ -405,7 +442,9 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
   return g * w.lf_cf;
 }
 
-template <int D, int NV, int LIM, int SOLVER, class TL>
+// CHAR: CHAR_LIMITING YES (a kernel of its own, so that the primitive
+// path keeps its register budget)
+template <int D, int NV, int LIM, int SOLVER, class TL, bool CHAR>
 __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double *__restrict__ svp,
                                           double *__restrict__ svm, double *__restrict__ sf,
                                           double *__restrict__ spr, double *__restrict__ scm,
@@ -444,7 +483,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
         minmod = ((S[c] | S[c - 1] | S[c + 1] | S[c - p.px] | S[c + p.px]) & 1) != 0;
       }
     }
-    if (p.char_lim) {
+    if constexpr (CHAR) {
       double v0[NV], dvp[NV], dvm[NV], dv[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) {
@@ -460,13 +499,24 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
       }
       continue;
     }
+    if (minmod) {   // FLAG_MINMOD
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        const double vm1 = sv[nv * G::VS + s0 - SST], v0 = sv[nv * G::VS + s0],
+                     vp1 = sv[nv * G::VS + s0 + SST];
+        const double dvp = (vp1 - v0) * wp, dvm = (v0 - vm1) * wm;
+        const double dv = dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0;
+        svp[nv * G::NPMAX + q] = v0 + dv * dp;
+        svm[nv * G::NPMAX + q] = v0 - dv * dm;
+      }
+      continue;
+    }
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       const double vm1 = sv[nv * G::VS + s0 - SST], v0 = sv[nv * G::VS + s0],
                    vp1 = sv[nv * G::VS + s0 + SST];
       const double dvp = (vp1 - v0) * wp, dvm = (v0 - vm1) * wm;
-      const double dv = minmod ? (dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0)   // FLAG_MINMOD
-                               : limited_slope_general<LIM>(dvp, dvm, cp, cm);
+      const double dv = limited_slope_general<LIM>(dvp, dvm, cp, cm);
       svp[nv * G::NPMAX + q] = v0 + dv * dp;
       svm[nv * G::NPMAX + q] = v0 - dv * dm;
     }
@@ -553,7 +603,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
         rhs[PRS] += dt * 0.5 * mflux * g0;
       }
       if (A.w.line_force) {
-        const double gr = line_force<NV>(vc, A.L, A.w, e0, e1, 0);
+        const double gr = line_force<NV>(vc, A.L, A.w, e0, e1, 0, vcell(p, gj, gi), p.vstride);
         rhs[VX1] += dt * vc[RHO] * gr;
         rhs[PRS] += dt * 0.5 * mflux * gr;
       }
@@ -574,7 +624,8 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
         rhs[PRS] += dt * vc[RHO] * vc[VX3] * g2;
       }
       if (A.w.line_force) {
-        const double gt = line_force<NV>(vc, A.L, A.w, e0, e1, 1), gz = 0.0;
+        const double gt = line_force<NV>(vc, A.L, A.w, e0, e1, 1, vcell(p, gj, gi), p.vstride);
+        const double gz = 0.0;
         rhs[VX2] += dt * vc[RHO] * gt;
         rhs[PRS] += dt * 0.5 * mflux * gt;
         rhs[VX3] += dt * vc[RHO] * gz;
@@ -592,7 +643,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
 }
 
 // One tile (bx, by) of one stage of one wind grid.
-template <int NV, int LIM, int SOLVER, int STAGE, class TL>
+template <int NV, int LIM, int SOLVER, int STAGE, class TL, bool CHAR>
 __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const WindStageArgs &A,
                                                int bx, int by, unsigned char *smem_raw)
 {
@@ -691,16 +742,16 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
           const double v2 = ans2[0] * A.L.c2a[e] + ans2[1] * A.L.c2b[e];
           const double dvds = fabs(v2 - v1) * ids;
           if (is_nan_bits(dvds)) flags |= F_NAN;
-          if (dvds > 0.0) lq = -alpha * log(dvds);
+          if (dvds > 0.0) lq = A.w.mfit ? -log10(dvds) : -alpha * log(dvds);
         }
         A.L.lq[e] = lq;
       }
     }
   }
 
-  sweep_sph<0, NV, LIM, SOLVER, TL>(sv, svp, svm, sf, spr, scm, U, cdt, own, cx, cy, gi, gj, dt,
+  sweep_sph<0, NV, LIM, SOLVER, TL, CHAR>(sv, svp, svm, sf, spr, scm, U, cdt, own, cx, cy, gi, gj, dt,
                                     dtdV, e0, e1, A, STAGE == 1, ox, oy);
-  sweep_sph<1, NV, LIM, SOLVER, TL>(sv, svp, svm, sf, spr, scm, U, cdt, own, cx, cy, gi, gj, dt,
+  sweep_sph<1, NV, LIM, SOLVER, TL, CHAR>(sv, svp, svm, sf, spr, scm, U, cdt, own, cx, cy, gi, gj, dt,
                                     dtdV, e0, e1, A, STAGE == 1, ox, oy);
 
   if (own) {

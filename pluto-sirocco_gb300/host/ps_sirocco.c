@@ -9,6 +9,9 @@
  *       cool_ff dens n_h"  (read_sirocco_heatcool, flag 1)
  *   prefactors.dat   a header line, then "i rcen[cm] j thetacen dens
  *       comp_h comp_c xray_h brem_c line_c xi_ion"  (same function)
+ *   M_UV_data.dat   a header line whose second word is the number of
+ *       points, a word and the t values, then per cell "i j x1[cm] x2[rad]
+ *       M_0 ... M_{n-1}"  (read_sirocco_fluxes with KRAD = ALPHARAD = 999)
  *
  * Records are placed on the grid by their coordinates, with the reference's
  * tolerances: |1 - x1_file / UNIT_LENGTH / x1[i]| < 1e-6 and
@@ -213,4 +216,55 @@ int ps_read_sirocco_prefactors(const ps_config *cfg, double unit_length, const d
   if (rc) return rc;
   if (matched) *matched = count;
   return 0;
+}
+
+int ps_read_m_uv_fit(const ps_config *cfg, double unit_length, const double *x1,
+                     const double *x2, const char *path, int max_points, double *t_fit,
+                     double *m_fit, long *matched)
+{
+  if (!cfg || !x1 || !x2 || !path || !t_fit || !m_fit || max_points <= 0 || !(unit_length > 0))
+    return fail("ps_read_m_uv_fit: bad arguments");
+  FILE *f = fopen(path, "r");
+  if (!f) return fail("ps_read_m_uv_fit: cannot open the file");
+  const int ng = PS_NGHOST(cfg), n0 = cfg->nx[0] + 2 * ng, n1 = cfg->nx[1] + 2 * ng;
+  const size_t plane = (size_t)n0 * n1;
+  char *line = (char *)malloc(PS_LINE);
+  double *vals = (double *)malloc(sizeof(double) * (size_t)max_points);
+  if (!line || !vals) {
+    free(line);
+    free(vals);
+    fclose(f);
+    return fail("ps_read_m_uv_fit: out of memory");
+  }
+  long np = -1, count = 0;
+  int rc = 0;
+  if (!fgets(line, PS_LINE, f) || sscanf(line, "%*s %ld", &np) != 1 || np <= 0)
+    rc = fail("ps_read_m_uv_fit: header improperly formatted");
+  else if (np > max_points)
+    rc = fail("ps_read_m_uv_fit: more points than max_points");
+  if (!rc && fscanf(f, "%*s ") != 0) rc = fail("ps_read_m_uv_fit: no t header");
+  for (long k = 0; !rc && k < np; k++)
+    if (fscanf(f, "%le", &t_fit[k]) != 1) rc = fail("ps_read_m_uv_fit: error in reading t");
+  long ii, jj;
+  double x1in, x2in;
+  while (!rc && fscanf(f, "%ld ", &ii) == 1) {
+    if (fscanf(f, "%ld %le %le", &jj, &x1in, &x2in) != 3) {
+      rc = fail("ps_read_m_uv_fit: error in reading a record");
+      break;
+    }
+    for (long k = 0; k < np && !rc; k++)
+      if (fscanf(f, "%le", &vals[k]) != 1) rc = fail("ps_read_m_uv_fit: error in reading a record");
+    if (rc) break;
+    const int i = find_cell(x1, ng, cfg->nx[0], x1in / unit_length, match_ratio, 1e-6);
+    const int j = find_cell(x2, ng, cfg->nx[1], x2in, match_ratio, 1e-6);
+    if (i < 0 || j < 0) continue;
+    for (long k = 0; k < np; k++) m_fit[(size_t)k * plane + (size_t)j * n0 + i] = vals[k];
+    count++;
+  }
+  free(line);
+  free(vals);
+  fclose(f);
+  if (rc) return rc;
+  if (matched) *matched = count;
+  return (int)np;
 }

@@ -34,7 +34,8 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_sg_label", "ps_sg_set_data", "ps_sg_train", "ps_sg_grad", "ps_sg_predict",
            "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect",
            "ps_set_cooling", "ps_write_dbl", "ps_read_dbl", "ps_read_sirocco_fluxes",
-           "ps_read_sirocco_heatcool", "ps_read_sirocco_prefactors", "ps_set_sirocco"]
+           "ps_read_sirocco_heatcool", "ps_read_sirocco_prefactors", "ps_set_sirocco",
+           "ps_read_m_uv_fit", "ps_set_mfit"]
 
 
 class Config(ctypes.Structure):
@@ -163,6 +164,8 @@ def lib():
         L.ps_read_sirocco_heatcool.argtypes = [CP, D, DP, DP, ctypes.c_char_p, DP, DP, LP]
         L.ps_read_sirocco_prefactors.argtypes = [CP, D, DP, DP, ctypes.c_char_p, DP, LP]
         L.ps_set_sirocco.argtypes = [P, DP, DP, DP]
+        L.ps_read_m_uv_fit.argtypes = [CP, D, DP, DP, ctypes.c_char_p, ctypes.c_int, DP, DP, LP]
+        L.ps_set_mfit.argtypes = [P, ctypes.c_int, DP, DP]
         _lib = L
     return _lib
 
@@ -401,6 +404,13 @@ class Solver:
         self._sirocco = arrs
         check(lib().ps_set_sirocco(self.ctx, *[None if a is None else _dp(a) for a in arrs]),
               "ps_set_sirocco")
+
+    def set_mfit(self, t_fit, m_fit):
+        """The tabulated force multiplier (KRAD = ALPHARAD = 999): t values
+        and M [point][j][i] (or [point][k][j][i]) over the total box."""
+        t, m = (np.ascontiguousarray(a, dtype=np.float64) for a in (t_fit, m_fit))
+        self._mfit = (t, m)
+        check(lib().ps_set_mfit(self.ctx, len(t), _dp(t), _dp(m)), "ps_set_mfit")
 
     def set_cooling(self, cooling):
         check(lib().ps_set_cooling(self.ctx, ctypes.byref(cooling)), "ps_set_cooling")
@@ -745,6 +755,18 @@ def read_sirocco_heatcool(cfg, grid, path, xi, t_r, unit_length=1e9):
                                          _dp(grid.x(1)), os.fsencode(path), _dp(xi), _dp(t_r),
                                          ctypes.byref(m)), "ps_read_sirocco_heatcool")
     return m.value
+
+
+def read_m_uv_fit(cfg, grid, path, max_points=256, unit_length=1e9):
+    """M_UV_data.dat -> (t [n], M [n][j][i] over the total box, cells matched);
+    cells without a record keep M = 1."""
+    t = np.zeros(max_points)
+    m = np.ones((max_points, grid.ntot[1], grid.ntot[0]))
+    mc = ctypes.c_long()
+    n = lib().ps_read_m_uv_fit(ctypes.byref(cfg), unit_length, _dp(grid.x(0)), _dp(grid.x(1)),
+                               os.fsencode(path), max_points, _dp(t), _dp(m), ctypes.byref(mc))
+    check(n, "ps_read_m_uv_fit")
+    return t[:n].copy(), m[:n].copy(), mc.value
 
 
 def read_sirocco_prefactors(cfg, grid, path, pre, unit_length=1e9):

@@ -82,8 +82,8 @@ L_star                      1.0e37
 f_x                         1.0
 f_uv                        1.0
 T_x                         5.6e7
-KRAD                        0.2
-ALPHARAD                    -0.6
+KRAD                        {krad}
+ALPHARAD                    {alpharad}
 DFLOOR                      1.0e-20
 GAMMA                       1.6666666666666667
 """
@@ -216,6 +216,25 @@ def write_flux_files(wd, nr, nt):
                             f"{x2[j]:.12e} {vals}\n")
 
 
+def write_mfit_file(wd, nr, nt):
+    """M_UV_data.dat in the layout read_sirocco_fluxes reads with KRAD =
+    ALPHARAD = 999 (Src/LineDriven/line_connect.c:182-257): a header line
+    whose second token is the number of points, a word followed by the t
+    values, then one row per active cell: i j r[cm] theta[rad] M_0 .. M_n."""
+    import psgb
+    from oracle import synthetic_mfit, WIND
+    x1 = psgb.build_grid(nr, 2, 10.0, 1000.0, "log")[0]
+    x2 = psgb.build_grid(nt, 2, 0.0, 1.5707963267948966, "uniform")[0]
+    t, m = synthetic_mfit(x1, x2, (nr + 4, nt + 4, 1))
+    with open(os.path.join(wd, "M_UV_data.dat"), "w") as f:
+        f.write(f"npoints {len(t)}\n")
+        f.write("t " + " ".join("%.12e" % v for v in t) + "\n")
+        for j in range(2, nt + 2):
+            for i in range(2, nr + 2):
+                vals = " ".join("%.12e" % v for v in m[:, 0, j, i])
+                f.write(f"{i - 2} {j - 2} {x1[i] * WIND['unit_length']:.12e} {x2[j]:.12e} {vals}\n")
+
+
 # name, ref config, (nr, nt), steps, snapshot every, with flux files, and
 # the numerics switches of the ref config's definitions.h / pluto.ini
 WIND_CASES = [
@@ -232,6 +251,7 @@ WIND_CASES = [
      dict(char_limiting=1, shock_flattening=1, entropy_switch=2)),
     ("wind2d_idl_64x32", "wind2d_idl", (64, 32), 200, 20, True,
      dict(char_limiting=1, shock_flattening=1, entropy_switch=2)),
+    ("wind2d_mfit_64x32", "wind2d", (64, 32), 100, 20, True, dict(mfit=True)),
 ]
 
 
@@ -243,10 +263,14 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux, opts):
     shutil.rmtree(wd, ignore_errors=True)
     os.makedirs(wd)
     with open(os.path.join(wd, "pluto.ini"), "w") as f:
+        mfit = opts.get("mfit", False)
         f.write(WIND_INI.format(nr=n[0], nt=n[1], every=every,
-                                solver=opts.get("solver", "hll")))
+                                solver=opts.get("solver", "hll"),
+                                krad=999 if mfit else 0.2, alpharad=999 if mfit else -0.6))
     if flux:
         write_flux_files(wd, n[0], n[1])
+    if opts.get("mfit"):
+        write_mfit_file(wd, n[0], n[1])
     subprocess.run([exe, "-maxsteps", str(steps - 1)], cwd=wd, check=True,
                    stdout=subprocess.DEVNULL)
     snaps = []
@@ -260,7 +284,7 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux, opts):
                 steps=steps, snap_steps=[k * every for k in keep], cooling=int(flux),
                 line_force=int(flux), char_limiting=opts.get("char_limiting", 0),
                 shock_flattening=opts.get("shock_flattening", 0),
-                entropy_switch=opts.get("entropy_switch", 0),
+                entropy_switch=opts.get("entropy_switch", 0), mfit=int(opts.get("mfit", 0)),
                 solver=opts.get("solver", "hll"),
                 t=[lines[k][1] for k in keep],
                 dt=[lines[k][2] for k in keep], final_sha256=digest(snaps[-1]))

@@ -146,6 +146,41 @@ def test_wind_entropy_switch_matches_reference(built, name):
     assert np.max(np.abs(ent / ref - 1.0)) < 1e-9
 
 
+def test_wind_tabulated_force_multiplier_matches_reference(built, tmp_path):
+    """KRAD = ALPHARAD = 999: the line force interpolates each cell's
+    tabulated M(t) (M_UV_data.dat, read here by the C reader from the file
+    the reference read) instead of k t^alpha; full physics, 100 steps."""
+    import psgb
+    from make_golden import write_mfit_file
+    meta = _case("wind2d_mfit")
+    snaps = np.load(meta["npz"])["snaps"]
+    nr, nt = meta["n"][0], meta["n"][1]
+    cfg = psgb.make_wind_config(nr, nt, cooling=1)
+    w = psgb.make_wind(line_force=1, krad=999.0, alpharad=999.0)
+    g = psgb.WindGrid(cfg)
+    s = psgb.Solver(cfg, g)
+    s.set_state(psgb.wind_state(cfg, w, g))
+    s.set_time(0.0, 1e-4, 0)
+    s.set_wind(w, psgb.wind_flux(cfg, w, g))
+    with pytest.raises(RuntimeError):        # the table is required
+        s.run(1)
+    write_mfit_file(str(tmp_path), nr, nt)
+    t, m, matched = psgb.read_m_uv_fit(cfg, g, str(tmp_path / "M_UV_data.dat"))
+    assert matched == nr * nt
+    s.set_mfit(t, m)
+    done = 0
+    for k, step in enumerate(meta["snap_steps"]):
+        if step > done:
+            s.run(step - done)
+            done = step
+        r = assert_hydro_close(_active(s.get_state()), snaps[k], f"step {step}")
+        print("tabulated M, step", step, "relative L1 per variable", r)
+    # and it is not the power law
+    h = _wind_solver(nr, nt, cooling=1, line_force=1)
+    h.run(meta["snap_steps"][-1])
+    assert not np.allclose(_active(h.get_state()), snaps[-1], rtol=1e-6)
+
+
 def _rel_l1(a, b):
     return np.abs(a - b).sum(axis=(1, 2)) / np.maximum(np.abs(b).sum(axis=(1, 2)), 1e-300)
 

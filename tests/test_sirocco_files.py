@@ -86,3 +86,22 @@ def test_bad_files_are_rejected(built, tmp_path):
     with pytest.raises(RuntimeError):
         psgb.read_sirocco_heatcool(cfg, g, str(tmp_path / "py_heatcool.dat"),
                                    np.zeros((20, 28)), np.zeros((20, 28)))
+
+
+def test_force_multiplier_table_file(built, tmp_path):
+    """M_UV_data.dat (read with KRAD = ALPHARAD = 999) in the layout the
+    golden generator writes for the reference: the reader places every row
+    and returns the table's t values and each cell's M as written."""
+    import psgb
+    from make_golden import write_mfit_file
+    from oracle import synthetic_mfit
+    cfg, g = _grid()
+    write_mfit_file(str(tmp_path), cfg.nx[0], cfg.nx[1])
+    t, m, matched = psgb.read_m_uv_fit(cfg, g, str(tmp_path / "M_UV_data.dat"))
+    et, em = synthetic_mfit(g.x(0), g.x(1), (cfg.nx[0] + 4, cfg.nx[1] + 4, 1))
+    assert matched == cfg.nx[0] * cfg.nx[1]
+    assert np.array_equal(t, et)
+    assert np.array_equal(m[:, 2:-2, 2:-2], em[:, 0, 2:-2, 2:-2])
+    assert np.all(m[:, :2] == 1.0)          # ghost rows keep the caller's values
+    with pytest.raises(RuntimeError):       # more points than room for them
+        psgb.read_m_uv_fit(cfg, g, str(tmp_path / "M_UV_data.dat"), max_points=4)
