@@ -77,10 +77,14 @@ __device__ __forceinline__ void char_slopes(const double (&v)[NV], const double 
                                             double gam, bool minmod, double (&dv)[NV])
 {
   constexpr int vn = VX1 + D, vt = D == 0 ? VX2 : VX3, vb = D == 0 ? VX3 : VX1;
-  const double cs2 = gam * v[PRS] / v[RHO];
+  // PrimEigenvectors' sound speed and the entries 1/(rho c), -1/c^2 and
+  // rho/c of L and R from one division: with a = gamma p and
+  // ir = 1/(rho a), c^2 = a^2 ir, 1/c^2 = rho^2 ir, 1/(rho c) = c rho ir
+  const double a = gam * v[PRS], ir = 1.0 / (v[RHO] * a);
+  const double cs2 = a * a * ir, icss = v[RHO] * v[RHO] * ir;
   const double cs = sqrt(cs2);
-  const double rhocs = v[RHO] * cs, rho_cs = v[RHO] / cs;
-  const double l0p = 1.0 / rhocs, l2p = -1.0 / cs2;
+  const double rhocs = v[RHO] * cs, rho_cs = v[RHO] * cs * icss;
+  const double l0p = cs * v[RHO] * ir, l2p = -icss;
   double wp[5], wm[5], wl[5];
   wm[0] = -1.0 * dvm[vn] + l0p * dvm[PRS];
   wm[1] = 1.0 * dvm[vn] + l0p * dvm[PRS];
@@ -686,7 +690,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
     // as ComputeEntropy leaves it after Boundary (Src/entropy_switch.c:14-37);
     // the stored entropy plane is not read
     for (int k = tid; k < G::VS; k += G::NT)
-      sv[(NV - 1) * G::VS + k] = sv[PRS * G::VS + k] / pow(sv[RHO * G::VS + k], p.gamma);
+      sv[(NV - 1) * G::VS + k] = sv[PRS * G::VS + k] * rho_pow(sv[RHO * G::VS + k], -p.gamma);
     __syncthreads();
   }
 
@@ -760,7 +764,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       double v0[NV], U0[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
-      if constexpr (NV == NFLX + 2) v0[NV - 1] = v0[PRS] / pow(v0[RHO], p.gamma);
+      if constexpr (NV == NFLX + 2) v0[NV - 1] = v0[PRS] * rho_pow(v0[RHO], -p.gamma);
       prim_to_cons<NV>(v0, U0, p.gmm1);
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = 0.5 * U0[nv] + 0.5 * U[nv];
