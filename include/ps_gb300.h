@@ -54,6 +54,9 @@ extern "C" {
 #define PS_F_NEG_DENSITY  0x04  /* FLAG_NEGATIVE_DENSITY                          */
 #define PS_F_DT_SMALL     0x08  /* dt too small (Src/main.c:672-683)              */
 #define PS_F_TMA_TIMEOUT  0x10  /* a bounded wait on a tile copy ran out          */
+#define PS_F_COOLING      0x20  /* the ODE cooling path failed in a cell: NaN
+                                   temperature or more than 1000 substeps
+                                   (QUIT_PLUTO in Src/Cooling/cooling_ode_solver.c) */
 
 typedef struct ps_config {
   int    dims;         /* DIMENSIONS: 2 or 3                                  */
@@ -68,7 +71,12 @@ typedef struct ps_config {
   double cfl_max_var;  /* [Time] CFL_max_var                                  */
   double tstop;        /* [Time] tstop                                        */
   double first_dt;     /* [Time] first_dt                                     */
-  int    cooling;      /* COOLING != NO: dt is recomputed after odd steps only */
+  int    cooling;      /* COOLING: 0 NO; 1 BLONDIN (split implicit solve);
+                           2 the ODE path of the production wind (COOLING
+                           TABULATED with its CoolingSource and Radiat:
+                           BLONDIN rates integrated by RKF12 / Cash-Karp,
+                           sets dt_cool; spherical contexts).  With cooling,
+                           dt is recomputed after odd steps only          */
   int    char_limiting; /* CHAR_LIMITING YES: PLM on characteristic variables
                            (Src/States/plm_states.c:481-746; spherical
                            contexts)                                      */

@@ -242,7 +242,8 @@ class Oracle:
 
 
 def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, char_limiting=0,
-                shock_flattening=0, solver="hll", entropy_switch=0, mfit=False, **params):
+                shock_flattening=0, solver="hll", entropy_switch=0, mfit=False, ode_cooling=0,
+                **params):
     """The 2-D spherical line-driven disk wind (PLM van Leer, HLL, RK2,
     userdef/outflow/axisymmetric/reflective boundaries, point-mass gravity,
     floors, BLONDIN cooling and the line force), initialised.  mfit: the
@@ -252,8 +253,8 @@ def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, c
     o = Oracle(dims=2, nx=(nr, nt, 1), nvar=7 if entropy_switch else 6, limiter="vl",
                solver=solver,
                bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
-               cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling,
-               geometry=3, gridtype=WIND_GRID["gridtype"], xbeg=WIND_GRID["xbeg"],
+               cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt,
+               cooling=2 if (cooling and ode_cooling) else cooling, geometry=3, gridtype=WIND_GRID["gridtype"], xbeg=WIND_GRID["xbeg"],
                xend=WIND_GRID["xend"], body_force=1, line_force=line_force, floors=1,
                params=dict(WIND, **params), char_limiting=char_limiting,
                shock_flattening=shock_flattening, entropy_switch=entropy_switch)

@@ -1444,6 +1444,237 @@ static double bl_zbrent(const bl_ctx *bc, int which, double x1, double x2, doubl
   return b;
 }
 
+/* ------------------------------------------------------------------ */
+/* ODE cooling path: CoolingSource with the production problem's Radiat */
+/* (Test_Problems/LineDrivenWind/cv_idl/cooling_source.c:50-246,       */
+/* radiat.c:21-142) and the integrators of Src/Cooling/                */
+/* cooling_ode_solver.c (SolveODE_RKF12 265-324, SolveODE_CK45 26-218) */
+/* ------------------------------------------------------------------ */
+
+#define OR_MAX_COOLING_RATE 0.1   /* g_maxCoolingRate (Src/globals.h:104) */
+#define OR_MIN_COOLING_TEMP 1.e4  /* g_minCoolingTemp as Radiat sets it */
+
+/* MeanMolecularWeight with COOLING == TABULATED (Src/mean_mol_weight.c:
+ * 138-141) and the default mass fractions (Src/pluto.h:692-720) */
+static double mu_tabulated(void)
+{
+  const double AH = 1.008, AHe = 4.004, AZ = 30.0;
+  const double xH = 0.7110, xHe = 0.2741;
+  const double xZ = (1.0 - xH - xHe);
+  const double fHe = (xHe / AHe * AH / xH), fZ = (xZ / AZ * AH / xH);
+  return (AH + fHe * AHe + fZ * AZ) / (2.0 + 3.0 * fHe + fZ * (1.0 + AZ * 0.5));
+}
+
+typedef struct {
+  double x1, time, xi_s, tr_s;
+  double ch, cc, xh, lc, bc;
+} ode_cell;
+
+/* Radiat: d(rho e)/dt in code units for the state v (v[re] = rho e); may
+ * floor v[re] (radiat.c:58-62).  Returns 0, or 1 on a NaN temperature. */
+static int ode_radiat(const or_sim *s, const ode_cell *oc, double *v, int re, double *rhs)
+{
+  double mu = s->c.mu, lx = s->c.l_star * s->c.f_x;
+  double r = oc->x1 * s->c.unit_length;
+  double rho = v[RHO] * s->c.unit_density;
+  double nH = rho / (1.43 * C_MP), ne, T, prs, xi, tx, sqT, sqxi, sqsqxi;
+  double E_cost = s->c.unit_length / s->c.unit_density / pow(s->c.unit_velocity, 3.0);
+  double comp_heat, comp_cool, xray_heat, line_cool, brem_cool, lambda;
+  prs = v[re] * (s->c.gamma - 1.0);
+  if (prs < 0.0) {
+    prs = small_pressure;
+    v[re] = prs / (s->c.gamma - 1.0);
+  }
+  T = prs / v[RHO] * KELVIN_OF(s) * mu;
+  if (T != T) {
+    *rhs = 0.0;
+    return 1;
+  }
+  if (T < OR_MIN_COOLING_TEMP) {
+    *rhs = 0.0;
+    return 0;
+  }
+  if (oc->time < 3.0) {
+    xi = lx / nH / r / r;
+    tx = s->c.t_x;
+  } else {
+    xi = oc->xi_s;
+    tx = oc->tr_s;
+  }
+  sqT = sqrt(T);
+  sqxi = sqrt(xi);
+  sqsqxi = pow(xi, 0.25);
+  ne = 1.21 * nH;   /* PY_CONNECT is not defined */
+  comp_heat = oc->ch * (8.9e-36 * xi * tx);
+  comp_cool = oc->cc * (8.9e-36 * xi * (4.0 * T));
+  xray_heat = oc->xh * (1.5e-21 * (sqsqxi / sqT));
+  line_cool = oc->lc * ((1e-16 * exp(-1.3e5 / T) / sqxi / T) +
+                        fmin(fmin(1e-24, 5e-27 * sqT), 1.5e-17 / T));
+  brem_cool = oc->bc * (3.3e-27 * sqT);
+  lambda = nH * (ne * comp_heat + nH * xray_heat - ne * comp_cool - ne * line_cool -
+                 ne * brem_cool);
+  *rhs = v[NFLX] > 0.01 ? lambda * E_cost : 0.0;   /* v[TRC] */
+  *rhs *= 1.0 - 1.0 / cosh(pow(T / OR_MIN_COOLING_TEMP, 12));
+  return 0;
+}
+
+/* SolveODE_RKF12 for the one variable rho e: 2nd-order solution into
+ * v2[re], returns the scaled difference to the 1st-order one */
+static double ode_rkf12(const or_sim *s, const ode_cell *oc, const double *v0, double k1,
+                        double *v2, int re, double dt, int *bad)
+{
+  double v1[NVMAX + 1], k2, v1st, vscal;
+  int nv;
+  for (nv = 0; nv <= re; nv++) v1[nv] = v0[nv];
+  v1[re] = v0[re] + 0.5 * dt * k1;
+  *bad |= ode_radiat(s, oc, v1, re, &k2);
+  v2[re] = v0[re] + dt * k2;
+  v1st = v0[re] + dt * k1;
+  vscal = fabs(v0[re]) + dt * fabs(k1);
+  return fabs(v2[re] - v1st) / fabs(vscal);
+}
+
+/* SolveODE_CK45 for rho e: Cash-Karp 4(5) with adaptive substeps until dt
+ * is covered; v5[re] gets the result, the return value is the suggested
+ * next step.  As in the reference, an accepted substep grows the step by
+ * the cap 5 (the error used for the growth is reset to 1e-18 first). */
+static double ode_ck45(const or_sim *s, const ode_cell *oc, const double *v0_in, double k1_in,
+                       double *v5, int re, double dt, double tol, int *bad)
+{
+  const double c1 = 37.0 / 378.0, c3 = 250.0 / 621.0, c4 = 125.0 / 594.0,
+               c6 = 512.0 / 1771.0;
+  const double c2 = 0.0, c5 = 0.0;
+  const double cs1 = 2825.0 / 27648.0, cs2 = 0.0, cs3 = 18575.0 / 48384.0,
+               cs4 = 13525.0 / 55296.0, cs5 = 277.0 / 14336.0, cs6 = 0.25;
+  const double b21 = 0.2;
+  const double b31 = 3.0 / 40.0, b32 = 9.0 / 40.0;
+  const double b41 = 0.3, b42 = -0.9, b43 = 1.2;
+  const double b51 = -11.0 / 54.0, b52 = 2.5, b53 = -70.0 / 27.0, b54 = 35.0 / 27.0;
+  const double b61 = 1631.0 / 55296.0, b62 = 175.0 / 512.0, b63 = 575.0 / 13824.0,
+               b64 = 44275.0 / 110592.0, b65 = 253.0 / 4096.0;
+  double v0[NVMAX + 1], v1[NVMAX + 1], k1 = k1_in, k2, k3, k4, k5, k6, v4, err, scrh;
+  double t = 0.0, tend = dt;
+  int nv, ksub = 0;
+  for (nv = 0; nv <= re; nv++) v0[nv] = v1[nv] = v0_in[nv];
+  for (;;) {
+    v1[re] = v0[re] + dt * b21 * k1;
+    *bad |= ode_radiat(s, oc, v1, re, &k2);
+    v1[re] = v0[re] + dt * (b31 * k1 + b32 * k2);
+    *bad |= ode_radiat(s, oc, v1, re, &k3);
+    v1[re] = v0[re] + dt * (b41 * k1 + b42 * k2 + b43 * k3);
+    *bad |= ode_radiat(s, oc, v1, re, &k4);
+    v1[re] = v0[re] + dt * (b51 * k1 + b52 * k2 + b53 * k3 + b54 * k4);
+    *bad |= ode_radiat(s, oc, v1, re, &k5);
+    v1[re] = v0[re] + dt * (b61 * k1 + b62 * k2 + b63 * k3 + b64 * k4 + b65 * k5);
+    *bad |= ode_radiat(s, oc, v1, re, &k6);
+    v5[re] = v0[re] + dt * (c1 * k1 + c2 * k2 + c3 * k3 + c4 * k4 + c5 * k5 + c6 * k6);
+    v4 = v0[re] + dt * (cs1 * k1 + cs2 * k2 + cs3 * k3 + cs4 * k4 + cs5 * k5 + cs6 * k6);
+    scrh = fabs(v0[re]) + dt * fabs(k1);
+    err = 0.0;
+    {
+      double e1 = fabs(v5[re] - v4) / fabs(scrh);
+      err = MAXD(err, e1);
+    }
+    err /= tol;
+    if (err < 1.0) {
+      double dt_grow;
+      ksub++;
+      err = MAXD(0.0, 1.e-18);
+      t += dt;
+      dt_grow = 0.9 * dt * pow(err, -0.2);
+      dt_grow = MIND(dt_grow, 5.0 * dt);
+      dt = dt_grow;
+      if (fabs(t / tend - 1.0) < 1.e-9) break;
+      if (dt > (tend - t)) dt = tend - t;
+      v0[re] = v5[re];
+      *bad |= ode_radiat(s, oc, v0, re, &k1);
+      if (ksub > 1000) {
+        *bad |= 2;
+        break;
+      }
+    } else {
+      double dt_shrink = 0.9 * dt * pow(err, -0.25);
+      dt = MAXD(dt_shrink, 0.05 * dt);
+    }
+  }
+  return dt;
+}
+
+/* CoolingSource over the active cells: integrate d(rho e)/dt = Radiat from
+ * 0 to dt (RKF12 when not stiff and accurate, else adaptive CK45 from a
+ * rough first step), floor at g_minCoolingTemp for gas that crossed it,
+ * and lower dt_cool to dt * g_maxCoolingRate / |p1/p0 - 1|. */
+static void ode_cooling(or_sim *s, double dt, double t)
+{
+  int i, j, k, nv, nvar = s->c.nvar, re = nvar;
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
+  const double min_tol = 2.e-5, gm1 = s->c.gamma - 1.0, mu0 = mu_tabulated();
+  ode_cell oc;
+  oc.time = t;
+  oc.ch = oc.cc = oc.xh = oc.lc = oc.bc = 1.0;
+  for (k = s->beg[2]; k <= s->end[2]; k++)
+  for (j = s->beg[1]; j <= s->end[1]; j++)
+  for (i = s->beg[0]; i <= s->end[0]; i++) {
+    size_t c = cidx(s, k, j, i);
+    double v0[NVMAX + 1], v1[NVMAX + 1], k1, err = 0.0, prs, T0, T1, scrh;
+    int stiff, bad = 0;
+    oc.x1 = s->x[0][i];
+    oc.xi_s = s->xi_s[c];
+    oc.tr_s = s->tr_s[c];
+    if (s->pre) {
+      oc.ch = s->pre[0 * nc + c];
+      oc.cc = s->pre[1 * nc + c];
+      oc.xh = s->pre[2 * nc + c];
+      oc.bc = s->pre[3 * nc + c];
+      oc.lc = s->pre[4 * nc + c];
+    }
+    for (nv = 0; nv < nvar; nv++) v0[nv] = v1[nv] = s->V[nv * nc + c];
+    prs = v0[PRS];
+    T0 = v0[PRS] / v0[RHO] * KELVIN_OF(s) * mu0;
+    v0[re] = v1[re] = prs / gm1;
+    if (T0 <= 0.0) {
+      s->fail |= 1024;
+      return;
+    }
+    bad |= ode_radiat(s, &oc, v0, re, &k1);
+    stiff = (fabs(k1) > 0.5 / dt ? 1 : 0);
+    if (!stiff) {
+      err = ode_rkf12(s, &oc, v0, k1, v1, re, dt, &bad);
+      err /= min_tol;
+    }
+    if (stiff || err > 1.0) {
+      double dt1, dts, t1 = 0.0;
+      int done = 0;
+      dt1 = 0.5 / (fabs(k1) + 1.0 / dt);
+      do {
+        if ((t1 + dt1) >= dt) {
+          dt1 = dt - t1;
+          done = 1;
+        }
+        dts = ode_ck45(s, &oc, v0, k1, v1, re, dt1, min_tol, &bad);
+        t1 += dt1;
+        dt1 = dts;
+        if (done) break;
+        for (nv = 0; nv <= re; nv++) v0[nv] = v1[nv];
+        bad |= ode_radiat(s, &oc, v0, re, &k1);
+      } while (!done);
+    }
+    if (bad) {
+      s->fail |= 1024;
+      return;
+    }
+    prs = v1[re] * gm1;
+    T1 = prs / v1[RHO] * KELVIN_OF(s) * mu0;
+    if (prs < 0.0) prs = small_pressure;
+    if (T1 < OR_MIN_COOLING_TEMP && T0 > OR_MIN_COOLING_TEMP)
+      prs = OR_MIN_COOLING_TEMP * v1[RHO] / (KELVIN_OF(s) * mu0);
+    err = fabs(prs / s->V[PRS * nc + c] - 1.0);
+    scrh = dt * OR_MAX_COOLING_RATE / err;
+    s->dt_cool = MIND(s->dt_cool, scrh);
+    s->V[PRS * nc + c] = prs;
+  }
+}
+
 void or_cooling(or_sim *s, double dt, double t)
 {
   int i, j, k;
@@ -1451,6 +1682,10 @@ void or_cooling(or_sim *s, double dt, double t)
   double lx = s->c.l_star * s->c.f_x, mu = s->c.mu;
   double g_minCoolingTemp = 1.e4;
   bl_ctx b;
+  if (s->c.cooling == 2) {
+    ode_cooling(s, dt, t);
+    return;
+  }
   memset(&b, 0, sizeof(b));
   b.dt_share = dt * UNIT_T(s);
   b.comp_c_pre = b.comp_h_pre = b.line_c_pre = b.brem_c_pre = b.xray_h_pre = 1.0;

@@ -42,7 +42,9 @@ typedef struct {
   double xbeg[3], xend[3], ratio[3];
   double gamma;
   double cfl, cfl_max_var, tstop, first_dt;
-  int    cooling;       /* 0: none; 1: BLONDIN split source (Strang rules)  */
+  int    cooling;       /* 0: none; 1: BLONDIN split source (Strang rules);
+                           2: the ODE path (COOLING TABULATED with the
+                           production problem's CoolingSource/Radiat)     */
   /* line-driven disk wind (all zero for the plain hydro configurations) */
   int    body_force;    /* point-mass gravity (BodyForceVector)            */
   int    line_force;    /* VGradCalc + LineForce                           */

@@ -52,6 +52,17 @@ INCS    += -I$(SRC)/Cooling/BLONDIN -I$(SRC)/LineDriven
 OBJ     += cooling.o line_connect.o
 endif
 
+# The wind with the ODE cooling path (COOLING TABULATED): the generic
+# integrators (Src/Cooling/cooling_ode_solver.c, Tabulated/) with the
+# production problem's own CoolingSource and Radiat (BLONDIN rates as the
+# right-hand side), compiled where they lie in Test_Problems.
+ifneq ($(wildcard $(CFGDIR)/WIND_ODE),)
+CVIDL   := $(REF)/Test_Problems/LineDrivenWind/cv_idl
+SRCDIRS += $(SRC)/LineDriven $(SRC)/Cooling $(SRC)/Cooling/Tabulated
+INCS    += -I$(SRC)/LineDriven -I$(SRC)/Cooling
+OBJ     += line_connect.o cooling_ode_solver.o jacobian.o maxrate.o cv_radiat.o cv_cooling_source.o
+endif
+
 # The configuration directory comes first so that its init.c (and any
 # file it overrides) wins, as with PLUTO's own VPATH.
 VPATH := $(CFGDIR) $(SRCDIRS)
@@ -67,6 +78,12 @@ $(OUT)/pluto.ini: $(CFGDIR)/pluto.ini
 	cp $< $@
 
 $(OUT)/%.o: %.c $(CFGDIR)/definitions.h | $(OUT)
+	$(CC) $(CFLAGS) $(INCS) -c $< -o $@
+
+$(OUT)/cv_radiat.o: $(CVIDL)/radiat.c $(CFGDIR)/definitions.h | $(OUT)
+	$(CC) $(CFLAGS) $(INCS) -c $< -o $@
+
+$(OUT)/cv_cooling_source.o: $(CVIDL)/cooling_source.c $(CFGDIR)/definitions.h | $(OUT)
 	$(CC) $(CFLAGS) $(INCS) -c $< -o $@
 
 $(OUT):

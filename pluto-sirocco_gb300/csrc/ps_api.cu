@@ -186,7 +186,8 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   if ((cfg->dims != 2 && cfg->dims != 3) || (cfg->nvar < 5 || cfg->nvar > 7) ||
       (!sph && cfg->nvar == 7) || (cfg->geometry != PS_CARTESIAN && !sph) ||
       (sph && (cfg->dims != 2 || cfg->nvar != sph_nvar)) ||
-      cfg->entropy_switch < 0 || cfg->entropy_switch > 2 ||
+      cfg->entropy_switch < 0 || cfg->entropy_switch > 2 || cfg->cooling < 0 ||
+      cfg->cooling > 2 || (cfg->cooling == 2 && !sph) ||
       cfg->limiter < 0 || cfg->limiter > 2 ||
       (cfg->solver != PS_HLLC && cfg->solver != PS_HLL) || cfg->gamma <= 1.0) {
     ps_set_error_msg("ps_create: unsupported configuration (Cartesian: dims 2/3, nvar 5/6; "

@@ -67,6 +67,20 @@ __global__ void k_batch_shock(const BatchModel *__restrict__ models,
   }
 }
 
+__global__ void k_batch_ode(const BatchModel *__restrict__ models,
+                            const BlockItem *__restrict__ blocks, const double *const *xi,
+                            const double *const *tr, const double *const *pre)
+{
+  const BlockItem bi = blocks[blockIdx.x];
+  const WindStageArgs &A = models[bi.m].st[0];
+  Scalars *sc = A.s.sc;
+  if (sc->done) return;
+  const int q = bi.b * blockDim.x + threadIdx.x;
+  if (q < A.s.p.nx[0] * A.s.p.nx[1])
+    ode_wind_cell(const_cast<double *>(A.s.Vn), xi[bi.m], tr[bi.m], A.s.p, A.w, A.g.x1, sc,
+                  sc->dt, sc->t, q, pre[bi.m]);
+}
+
 __global__ void k_batch_blondin(const BatchModel *__restrict__ models,
                                 const BlockItem *__restrict__ blocks, const double *const *xi,
                                 const double *const *tr, const double *const *pre)
@@ -384,6 +398,12 @@ static int batch_cool(ps_batch *b)
     b->launches += 2;
     return 0;
   }
+  if (b->cooling == 2) {   // the ODE path
+    ps::k_batch_ode<<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, b->d_xi,
+                                                             b->d_tr, b->d_pre);
+    b->launches++;
+    return 0;
+  }
   ps::k_batch_blondin<<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, b->d_xi,
                                                                b->d_tr, b->d_pre);
   b->launches++;
@@ -680,6 +700,9 @@ extern "C" long ps_batch_launch_count(const ps_batch *b) { return b ? b->launche
 extern "C" int ps_batch_set_surrogate(ps_batch *b, ps_surrogate *s, int use_net)
 {
   if (!b) return batch_fail("ps_batch_set_surrogate: null batch");
+  if (s && b->cooling == 2)
+    return batch_fail("ps_batch_set_surrogate: the learned step replaces BLONDIN's implicit "
+                      "solve, not the ODE cooling path");
   BCK(cudaStreamSynchronize(b->stream));
   if (s && !b->sg_queue) {
     BCK(cudaMalloc(&b->sg_queue, sizeof(int2) * (size_t)b->total_cells));

@@ -28,7 +28,7 @@ constexpr double kSmallPressure = 1.e-12;  // g_smallPressure (Src/globals.h:116
 
 // device flag bits (mirrors PS_F_* of the C ABI)
 constexpr unsigned F_NAN = 0x01, F_CONS2PRIM = 0x02, F_NEG_DENSITY = 0x04,
-                   F_DT_SMALL = 0x08, F_TMA_TIMEOUT = 0x10;
+                   F_DT_SMALL = 0x08, F_TMA_TIMEOUT = 0x10, F_COOLING = 0x20;
 
 __device__ __forceinline__ double abs_min(double a, double b)
 {

@@ -921,6 +921,9 @@ extern "C" int ps_set_surrogate(ps_ctx *c, ps_surrogate *s, int use_net)
   if (!c) return sg_fail("ps_set_surrogate: null context");
   if (s && !c->wind && !c->cool_on)
     return sg_fail("ps_set_surrogate: needs ps_set_wind or ps_set_cooling first");
+  if (s && c->p.cooling == 2)
+    return sg_fail("ps_set_surrogate: the learned step replaces BLONDIN's implicit solve, not "
+                   "the ODE cooling path");
   SCK(cudaStreamSynchronize(c->stream));
   if (s) SCK(cudaStreamSynchronize(s->stream));
   if (s && !c->sg_queue) {

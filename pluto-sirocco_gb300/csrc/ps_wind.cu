@@ -77,6 +77,17 @@ __global__ void k_wind_init_xi(const double *V, double *xi, double *tr, const Pa
     init_xi_cell(V, xi, tr, p, w, x1, q);
 }
 
+// CoolingSource (ODE path) over the active cells
+__global__ void k_ode_cool(double *V, const double *xi_s, const double *tr_s, const Params p,
+                           const WindParams w, const double *x1, Scalars *sc, const double *pre)
+{
+  if (sc->done) return;
+  const double dt = sc->dt, t = sc->t;
+  const int n = p.nx[0] * p.nx[1];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    ode_wind_cell(V, xi_s, tr_s, p, w, x1, sc, dt, t, q, pre);
+}
+
 __global__ void k_blondin(double *V, const double *xi_s, const double *tr_s, const Params p,
                           const WindParams w, const double *x1, Scalars *sc, const double *pre)
 {
@@ -399,6 +410,17 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
     W.nm = 0;
     W.lt0 = std::log10(C);
   }
+  {
+    // the ODE cooling path: E_cost of Radiat and KELVIN times
+    // MeanMolecularWeight with COOLING TABULATED and the default mass
+    // fractions (Src/mean_mol_weight.c:138-141, Src/pluto.h:692-720)
+    W.ode_e_cost = UL / UD / std::pow(UV, 3.0);
+    const double AH = 1.008, AHe = 4.004, AZ = 30.0, xH = 0.7110, xHe = 0.2741;
+    const double xZ = (1.0 - xH - xHe);
+    const double fHe = (xHe / AHe * AH / xH), fZ = (xZ / AZ * AH / xH);
+    const double mu0 = (AH + fHe * AHe + fZ * AZ) / (2.0 + 3.0 * fHe + fZ * (1.0 + AZ * 0.5));
+    W.ode_mu0_kelvin = W.kelvin * mu0;
+  }
 
   w->k1 = ps::stage_kernel_sph(p.nvar, p.char_lim != 0, p.limiter, p.solver, 1);
   w->k2 = ps::stage_kernel_sph(p.nvar, p.char_lim != 0, p.limiter, p.solver, 2);
@@ -491,6 +513,13 @@ int ps_wind_cool_launch(ps_ctx *c)
   WindDev *w = c->wind;
   const ps::Params &p = c->p;
   if (!p.cooling) return 0;
+  if (p.cooling == 2) {   // the ODE path
+    const int nb = (p.nx[0] * p.nx[1] + 127) / 128;
+    ps::k_ode_cool<<<nb, 128, 0, c->stream>>>(c->V, w->xi, w->tr, p, w->a.w, w->a.g.x1, c->sc,
+                                              w->pre);
+    c->launches++;
+    return 0;
+  }
   if (c->sg) return ps_sg_cool_launch(c);
   const int nb = (p.nx[0] * p.nx[1] + 127) / 128;
   ps::k_blondin<<<nb, 128, 0, c->stream>>>(c->V, w->xi, w->tr, p, w->a.w, w->a.g.x1, c->sc,

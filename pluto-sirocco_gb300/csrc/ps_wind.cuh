@@ -69,6 +69,10 @@ struct WindParams {
   // log10(rho p)/2 - log10(dv/ds) (lt0 = log10 C), nm points
   int mfit, nm;
   double lt0;
+  // the ODE cooling path (cooling = 2): UNIT_LENGTH / UNIT_DENSITY /
+  // UNIT_VELOCITY^3 and KELVIN times the tabulated-cooling mean molecular
+  // weight (Src/mean_mol_weight.c:138-141)
+  double ode_e_cost, ode_mu0_kelvin;
   // > 0: BLONDIN at this constant ionisation parameter with T_x (the
   // Cartesian cooling configuration); 0: xi from the state / sirocco_xi
   double xi_const;

@@ -15,6 +15,7 @@
 #pragma once
 
 #include "ps_blondin.cuh"
+#include "ps_ode_cool.cuh"
 #include "ps_ctx.cuh"
 #include "ps_physics.cuh"
 #include "ps_stage.cuh"
@@ -372,6 +373,55 @@ __device__ __forceinline__ void blondin_cell(double *V, const double *xi_s, cons
   const double T_f = bl_solve(b, T, overflow);
   if (overflow) atomicOr(&sc->flags, F_NAN);
   blondin_store(V, p, w, b, c, T_f);
+}
+
+// CoolingSource with the production Radiat on one cell (the ODE path,
+// cooling = 2): the new pressure and this cell's bound on dt_cool, kept as
+// the minimum over cells (positive doubles order as their bit patterns).
+__device__ __forceinline__ void ode_wind_cell(double *V, const double *xi_s, const double *tr_s,
+                                              const Params &p, const WindParams &w,
+                                              const double *x1, Scalars *sc, double dt, double t,
+                                              long long q, const double *pre)
+{
+  int gi, gj, gk;
+  cell_of(p, q, gi, gj, gk);
+  const long long c = vcell3(p, gk, gj, gi);
+  OdeCell o;
+  o.ch = o.cc = o.xh = o.lc = o.bc = 1.0;
+  if (pre) {
+    o.ch = pre[c];
+    o.cc = pre[p.vstride + c];
+    o.xh = pre[2 * p.vstride + c];
+    o.lc = pre[3 * p.vstride + c];
+    o.bc = pre[4 * p.vstride + c];
+  }
+  o.rho = V[RHO * p.vstride + c];
+  o.trc = V[NFLX * p.vstride + c];
+  o.rho_cgs_nH = o.rho * w.unit_density / (1.43 * kMP);
+  if (t < 3.0) {
+    const double r = x1[gi] * w.unit_length;
+    o.xi = w.lx / o.rho_cgs_nH / r / r;
+    o.tx = w.t_x;
+  } else {
+    o.xi = xi_s[c];
+    o.tx = tr_s[c];
+  }
+  o.sqxi = sqrt(o.xi);
+  o.sqsqxi = pow(o.xi, 0.25);
+  o.gm1 = p.gmm1;
+  o.kmu = w.kelvin * w.mu;
+  o.e_cost = w.ode_e_cost;
+  bool bad = false;
+  double dtc = 1.e38;
+  const double prs = ode_cool_cell(o, V[PRS * p.vstride + c], dt, w.ode_mu0_kelvin, dtc, bad);
+  if (bad) {
+    atomicOr(&sc->flags, F_COOLING);
+    return;
+  }
+  V[PRS * p.vstride + c] = prs;
+  if (dtc >= 0.0 && dtc < 1.e38)
+    atomicMin(reinterpret_cast<unsigned long long *>(&sc->dt_cool),
+              static_cast<unsigned long long>(__double_as_longlong(dtc)));
 }
 
 // ---------------------------------------------------------------

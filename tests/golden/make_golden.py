@@ -252,6 +252,7 @@ WIND_CASES = [
     ("wind2d_idl_64x32", "wind2d_idl", (64, 32), 200, 20, True,
      dict(char_limiting=1, shock_flattening=1, entropy_switch=2)),
     ("wind2d_mfit_64x32", "wind2d", (64, 32), 100, 20, True, dict(mfit=True)),
+    ("wind2d_ode_64x32", "wind2d_ode", (64, 32), 100, 20, True, dict(ode_cooling=1)),
 ]
 
 
@@ -285,6 +286,7 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux, opts):
                 line_force=int(flux), char_limiting=opts.get("char_limiting", 0),
                 shock_flattening=opts.get("shock_flattening", 0),
                 entropy_switch=opts.get("entropy_switch", 0), mfit=int(opts.get("mfit", 0)),
+                ode_cooling=opts.get("ode_cooling", 0),
                 solver=opts.get("solver", "hll"),
                 t=[lines[k][1] for k in keep],
                 dt=[lines[k][2] for k in keep], final_sha256=digest(snaps[-1]))

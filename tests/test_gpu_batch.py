@@ -87,6 +87,23 @@ def test_batch_production_limiting_matches_individual_runs(built):
     batch.close()
 
 
+def test_batch_ode_cooling_matches_individual_runs(built):
+    """The ODE cooling path in a batch (one launch for every model's
+    CoolingSource, each model's own dt_cool) gives what each model gives
+    alone."""
+    import psgb
+    solo = [psgb.wind_model_solver(s, cooling=2, line_force=1) for s in SPECS]
+    inb = [psgb.wind_model_solver(s, cooling=2, line_force=1) for s in SPECS]
+    batch = psgb.Batch(inb)
+    for chunk in (5, 8):
+        flags = 0
+        for s in solo:
+            flags |= s.run(chunk)
+        assert batch.run(chunk) == flags
+        _check_equal(solo, inb)
+    batch.close()
+
+
 def test_batch_rejects_mixed_models(built):
     import psgb
     a = psgb.wind_model_solver(SPECS[0], cooling=1)

@@ -181,6 +181,36 @@ def test_wind_tabulated_force_multiplier_matches_reference(built, tmp_path):
     assert not np.allclose(_active(h.get_state()), snaps[-1], rtol=1e-6)
 
 
+def test_wind_ode_cooling_matches_reference(built):
+    """The ODE cooling path (cooling = 2: COOLING TABULATED with the
+    production problem's CoolingSource and Radiat, RKF12 or adaptive
+    Cash-Karp per cell, dt_cool limiting the step), with the line force,
+    against the reference run: state and the time step at every snapshot."""
+    import psgb
+    meta = _case("wind2d_ode")
+    snaps = np.load(meta["npz"])["snaps"]
+    s = _wind_solver(meta["n"][0], meta["n"][1], cooling=2, line_force=1)
+    done = 0
+    for k, step in enumerate(meta["snap_steps"]):
+        if step > done:
+            assert s.run(step - done) & 0x20 == 0   # PS_F_COOLING
+            done = step
+        r = assert_hydro_close(_active(s.get_state()), snaps[k], f"step {step}")
+        print("ODE cooling, step", step, "relative L1 per variable", r)
+        t, dt, _, _ = s.time()
+        assert abs(t - float(meta["t"][k])) <= 6e-7 * abs(t)
+        assert abs(dt - float(meta["dt"][k])) <= 6e-7 * abs(dt)
+    # dt_cool is what limits the step here: the BLONDIN run's dt differs
+    h = _wind_solver(meta["n"][0], meta["n"][1], cooling=1, line_force=1)
+    h.run(20)
+    assert abs(h.time()[1] - float(meta["dt"][1])) > 1e-3 * h.time()[1]
+    # the learned step is for BLONDIN's implicit solve only
+    sg = psgb.Surrogate(psgb.SG_DRAW_BOX and [b[0] for b in psgb.SG_DRAW_BOX],
+                        [b[1] for b in psgb.SG_DRAW_BOX])
+    assert psgb.lib().ps_set_surrogate(s.ctx, sg.h, 1) < 0
+    sg.close()
+
+
 def _rel_l1(a, b):
     return np.abs(a - b).sum(axis=(1, 2)) / np.maximum(np.abs(b).sum(axis=(1, 2)), 1e-300)
 
