@@ -582,6 +582,7 @@ def batch_bench(wl, steps, warmup, rank, world):
                    "hydro": "bit-exact against the oracle (tests/test_gpu_wind.py, "
                             "tests/test_gpu_batch.py); the learned step only changes pressure",
                    "tile_shapes": shapes, "autotune_s": t_tune,
+                   "line_force": _line_force_figures(wl),
                    "l2": "256 MiB buffer written before every timed step (L2 flushed)",
                    "parallelism": "replicas only" if world > 1 else "single GPU"},
         "e2e": {"value": wl.cells * e2e_steps / e2e_wall, "unit": "cell-updates/s",
@@ -731,6 +732,33 @@ def cube_bench(wl, steps, warmup, rank, world):
         print(json.dumps(out_json), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def _line_force_figures(wl):
+    """The line force is fused into the stage kernel; its own memory work per
+    cell-update from the flux-bin lists the batch's models carry: per bin
+    with a nonzero (F_r, F_theta) and stage, VGradCalc reads 7 static doubles
+    (bilinear weights of the offset point, four velocity projections, 1/ds)
+    and writes one, and each of the two sweeps reads it back with one flux
+    (12 doubles), against the 5 doubles per bin of all 36 bins of a dense
+    per-angle design (2880 B per cell-update)."""
+    import numpy as np
+    import psgb
+    bins = cells = 0
+    for sp in wl.specs:
+        nr, nt = sp["grid"]
+        cfg = psgb.make_wind_config(nr, nt)
+        w = psgb.make_wind(l_star=sp["l_star"], krad=sp["krad"], alpharad=sp["alpharad"])
+        g = psgb.WindGrid(cfg)
+        fr, ft, _ = psgb.wind_flux(cfg, w, g)
+        act = (slice(None), 0, slice(2, -2), slice(2, -2))
+        bins += int(np.count_nonzero((fr[act] != 0.0) | (ft[act] != 0.0)))
+        cells += nr * nt
+    per_cell = bins / cells
+    return {"bins_per_cell": per_cell, "angles": 36,
+            "bytes_per_cell_update": 2 * 12 * 8 * per_cell,
+            "dense_design_bytes_per_cell_update": 2 * 5 * 36 * 8,
+            "flux": "synthetic: the radial bin of each cell (real SIROCCO fluxes fill more bins)"}
 
 
 def _rooflines(out, wl, stage_ms, per_kernel):
