@@ -101,7 +101,7 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
   v[VX1] = u[VX1] * tau;
   v[VX2] = u[VX2] * tau;
   v[VX3] = u[VX3] * tau;
-  const double kin = 0.5 * m2 / u[RHO];
+  const double kin = 0.5 * m2 * tau;
   if (u[PRS] < 0.0) {
     u[PRS] = kSmallPressure / gmm1 + kin;
     flag |= F_CONS2PRIM;
@@ -147,9 +147,10 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
   double uL[NV], uR[NV];
   prim_to_cons<NV>(vL, uL, gmm1);
   prim_to_cons<NV>(vR, uR, gmm1);
-  const double a2L = gam * vL[PRS] / vL[RHO];
-  const double a2R = gam * vR[PRS] / vR[RHO];
-  const double aL = sqrt(a2L), aR = sqrt(a2R);
+  // sound speeds sqrt(gamma p / rho) as (gamma p) rsqrt(gamma p rho): one
+  // reciprocal square root in place of a division and a square root
+  const double gpL = gam * vL[PRS], gpR = gam * vR[PRS];
+  const double aL = gpL * rsqrt(gpL * vL[RHO]), aR = gpR * rsqrt(gpR * vR[RHO]);
   const double SL = dmin(vL[VN] - aL, vR[VN] - aR);
   const double SR = dmax(vL[VN] + aL, vR[VN] + aR);
   cmax = dmax(fabs(SL), fabs(SR));

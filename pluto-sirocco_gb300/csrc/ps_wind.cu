@@ -167,10 +167,10 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   // geometry (Src/set_geometry.c:62-240) and PLM weights (plm_coeffs.c:30-74)
   enum {
     G_X1, G_DX1, G_INVDX1, G_RINV, G_ABSX1, G_ABSX1P, G_A1F, G_DVR, G_RDR, G_RTINV, G_G0, G_X11A,
-    G_X22A, G_LOCR, G_XGC1, G_FX, N1ARR
+    G_X22A, G_LOCR, G_XGC1, G_FX, G_INVDVR, N1ARR
   };
   enum { H_X2, H_DX2, H_INVDX2, H_DMU, H_SXP, H_SPABS, H_SN, H_CT, H_SIN2, H_COS2, H_X11B, H_X22B,
-         H_XGC2, H_FY, N2ARR };
+         H_XGC2, H_FY, H_INVDMU, N2ARR };
   std::vector<double> a1((size_t)N1ARR * n0, 0.0), a2((size_t)N2ARR * n1, 0.0);
   std::vector<double> plm((size_t)12 * (n0 > n1 ? n0 : n1), 0.0);
   const int nmax = n0 > n1 ? n0 : n1;
@@ -184,10 +184,11 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
     A1(G_DX1, i) = dx1[i];
     A1(G_INVDX1, i) = 1.0 / (dx1[i]);
     A1(G_RINV, i) = 1.0 / x1[i];
-    A1(G_ABSX1, i) = std::fabs(x1[i]);
+    A1(G_ABSX1, i) = 1.0 / std::fabs(x1[i]);
     A1(G_ABSX1P, i) = std::fabs(x1p[i]);
     A1(G_A1F, i) = x1p[i] * x1p[i];
     A1(G_DVR, i) = std::fabs(x1p[i] * x1p[i] * x1p[i] - x1m[i] * x1m[i] * x1m[i]) / 3.0;
+    A1(G_INVDVR, i) = 1.0 / A1(G_DVR, i);
     A1(G_RDR, i) = std::fabs(x1[i]) * dx1[i];
     const double rt = (xR * xR * xR - xL * xL * xL) / (xR * xR - xL * xL) / 1.5;
     A1(G_RTINV, i) = 1.0 / rt;
@@ -206,9 +207,10 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
     A2(H_DX2, j) = dx2[j];
     A2(H_INVDX2, j) = 1.0 / (dx2[j]);
     A2(H_DMU, j) = std::fabs(std::cos(xL) - std::cos(xR));
+    A2(H_INVDMU, j) = 1.0 / A2(H_DMU, j);
     A2(H_SXP, j) = std::fabs(std::sin(xR));
     A2(H_SPABS, j) = std::fabs(std::fabs(std::sin(xR)));
-    A2(H_SN, j) = std::fabs(std::fabs(std::sin(x2[j])));
+    A2(H_SN, j) = 1.0 / std::fabs(std::fabs(std::sin(x2[j])));
     A2(H_CT, j) = 1.0 / std::tan(x2[j]);
     A2(H_SIN2, j) = std::sin(x2[j]);
     A2(H_COS2, j) = std::cos(x2[j]);
@@ -335,7 +337,8 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   G.dx1 = g1 + (size_t)G_DX1 * n0;
   G.inv_dx1 = g1 + (size_t)G_INVDX1 * n0;
   G.rinv = g1 + (size_t)G_RINV * n0;
-  G.absx1 = g1 + (size_t)G_ABSX1 * n0;
+  G.inv_absx1 = g1 + (size_t)G_ABSX1 * n0;
+  G.inv_dVr = g1 + (size_t)G_INVDVR * n0;
   G.absx1p = g1 + (size_t)G_ABSX1P * n0;
   G.A1f = g1 + (size_t)G_A1F * n0;
   G.dVr = g1 + (size_t)G_DVR * n0;
@@ -349,7 +352,8 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   G.dmu = g2 + (size_t)H_DMU * n1;
   G.sxp = g2 + (size_t)H_SXP * n1;
   G.spabs = g2 + (size_t)H_SPABS * n1;
-  G.sn = g2 + (size_t)H_SN * n1;
+  G.inv_sn = g2 + (size_t)H_SN * n1;
+  G.inv_dmu = g2 + (size_t)H_INVDMU * n1;
   G.ct = g2 + (size_t)H_CT * n1;
   G.sin2 = g2 + (size_t)H_SIN2 * n1;
   G.cos2 = g2 + (size_t)H_COS2 * n1;

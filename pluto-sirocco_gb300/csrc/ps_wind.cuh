@@ -14,7 +14,8 @@ struct SphGeom {
   // x1 direction (ntot[0] entries)
   const double *x1, *dx1, *inv_dx1;
   const double *rinv;    // 1/x1                    (r_1 of the x1 sources)
-  const double *absx1;   // |x1|                    (phi-momentum divisor)
+  const double *inv_absx1;  // 1/|x1|               (phi-momentum divisor, as a factor)
+  const double *inv_dVr;    // 1/dVr                 (volume divisor, with inv_dmu)
   const double *absx1p;  // |x1p|                   (phi-momentum flux factor)
   const double *A1f;     // x1p*x1p
   const double *dVr;     // |x1p^3 - x1m^3| / 3
@@ -27,7 +28,8 @@ struct SphGeom {
   const double *dmu;     // |cos(x2m) - cos(x2p)|
   const double *sxp;     // |sin(x2p)|
   const double *spabs;   // |sp|
-  const double *sn;      // |sin(x2)|
+  const double *inv_sn;  // 1/|sin(x2)|               (phi-momentum divisor, as a factor)
+  const double *inv_dmu; // 1/dmu
   const double *ct;      // 1/tan(x2)
   const double *sin2, *cos2;
   const double *fy;      // VGradCalc: bilinear weight of the cell centre in x2

@@ -637,7 +637,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
       rhs[nv] = -dtdV * (fAr - fAl);
     }
     rhs[VN] -= dtdl * (spr[qr] - spr[ql]);
-    rhs[VX3] /= D == 0 ? g.absx1[gi] : g.sn[gj];
+    rhs[VX3] *= D == 0 ? g.inv_absx1[gi] : g.inv_sn[gj];
     const double mflux = sf[RHO * G::NFMAX + qr] + sf[RHO * G::NFMAX + ql];
     double vc[NV];
     if (D == 0) {
@@ -766,7 +766,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = a.Us[nv * p.vstride + cell];
     }
-    dtdV = dt / (g.dVr[gi] * g.dmu[gj]);
+    dtdV = dt * g.inv_dVr[gi] * g.inv_dmu[gj];
     if (A.w.line_force) {
       // VGradCalc for the bins of this cell (line_connect.c:628-738)
       const int dc = (oy + cy) * p.nx[0] + (ox + cx);
