@@ -249,6 +249,7 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   p.vstride = (long long)p.px * p.ntot[1] * p.ntot[2];
   p.gamma = cfg->gamma;
   p.gmm1 = cfg->gamma - 1.0;
+  p.igmm1 = 1.0 / p.gmm1;
   p.cfl = cfg->cfl;
   p.cfl_max_var = cfg->cfl_max_var;
   p.tstop = cfg->tstop;

@@ -39,6 +39,7 @@ struct Params {
   long long vstride;      // elements between variables
   int bc[6];
   double gamma, gmm1;
+  double igmm1;           // 1 / (gamma - 1): p / (gamma - 1) as a product
   double cfl, cfl_max_var, tstop, first_dt;
 };
 

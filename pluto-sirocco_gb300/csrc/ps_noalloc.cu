@@ -202,6 +202,7 @@ extern "C" int ps_advance_step_noalloc(const ps_config *cfg, const double *dx1, 
   p.vstride = cells;
   p.gamma = cfg->gamma;
   p.gmm1 = cfg->gamma - 1.0;
+  p.igmm1 = 1.0 / p.gmm1;
   p.cfl = cfg->cfl;
   p.cfl_max_var = cfg->cfl_max_var;
   p.tstop = cfg->tstop;

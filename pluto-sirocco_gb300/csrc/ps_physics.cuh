@@ -63,15 +63,17 @@ __device__ __forceinline__ double limited_slope(double dvp, double dvm)
 
 template <int NV>
 __device__ __forceinline__ void prim_to_cons(const double (&v)[NV], double (&u)[NV],
-                                             double gmm1)
+                                             double igmm1)
 {
+  // E = rho v^2 / 2 + p / (gamma - 1), the division as a product with
+  // igmm1 = 1 / (gamma - 1)
   const double rho = v[RHO];
   u[RHO] = rho;
   u[VX1] = rho * v[VX1];
   u[VX2] = rho * v[VX2];
   u[VX3] = rho * v[VX3];
   double e = v[VX1] * v[VX1] + v[VX2] * v[VX2] + v[VX3] * v[VX3];
-  u[PRS] = 0.5 * rho * e + v[PRS] / gmm1;
+  u[PRS] = 0.5 * rho * e + v[PRS] * igmm1;
 #pragma unroll
   for (int nv = NFLX; nv < NV; nv++) u[nv] = rho * v[nv];
 }
@@ -141,12 +143,12 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
 // side with SHOCK_FLATTENING MULTID, Src/HD/hllc.c:93-104).
 template <int NV, int SOLVER, int VN>
 __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&vR)[NV],
-                                        double gam, double gmm1, double (&f)[NV],
+                                        double gam, double igmm1, double (&f)[NV],
                                         double &pr, double &cmax, bool hll = false)
 {
   double uL[NV], uR[NV];
-  prim_to_cons<NV>(vL, uL, gmm1);
-  prim_to_cons<NV>(vR, uR, gmm1);
+  prim_to_cons<NV>(vL, uL, igmm1);
+  prim_to_cons<NV>(vR, uR, igmm1);
   // sound speeds sqrt(gamma p / rho) as (gamma p) rsqrt(gamma p rho): one
   // reciprocal square root in place of a division and a square root
   const double gpL = gam * vL[PRS], gpR = gam * vR[PRS];

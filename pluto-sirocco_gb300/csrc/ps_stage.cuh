@@ -163,7 +163,7 @@ __device__ __forceinline__ void sweep(const double *__restrict__ sv, double *__r
   constexpr int NP = PX * PY * PZ, NF = FX * FY * FZ;
   constexpr int SST = D == 0 ? 1 : (D == 1 ? G::SX : G::SX * G::SY);  // smem stride along D
   constexpr int VN = VX1 + D;
-  const double gam = a.p.gamma, gmm1 = a.p.gmm1;
+  const double gam = a.p.gamma;
 
   // (1) PLM: + and - states of cells -1 .. T_D along D
   for (int q = threadIdx.x; q < NP; q += G::NT) {
@@ -197,7 +197,7 @@ __device__ __forceinline__ void sweep(const double *__restrict__ sv, double *__r
       vL[nv] = svp[nv * G::NPMAX + pl];
       vR[nv] = svm[nv * G::NPMAX + pr_];
     }
-    riemann<NV, SOLVER, VN>(vL, vR, gam, gmm1, f, pr, cm);
+    riemann<NV, SOLVER, VN>(vL, vR, gam, a.p.igmm1, f, pr, cm);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) sf[nv * G::NFMAX + q] = f[nv];
     spr[q] = pr;
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(TileGeom<TileT<DIMS>>::NT)
       const int s0 = ((cz + TL::HZ) * G::SY + cy + TL::HY) * G::SX + cx + TL::HX;
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v[nv] = sv[nv * G::VS + s0];
-      prim_to_cons<NV>(v, U, p.gmm1);
+      prim_to_cons<NV>(v, U, p.igmm1);
     } else {
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = a.Us[nv * p.vstride + cell];
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(TileGeom<TileT<DIMS>>::NT)
       double v0[NV], U0[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
-      prim_to_cons<NV>(v0, U0, p.gmm1);
+      prim_to_cons<NV>(v0, U0, p.igmm1);
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = 0.5 * U0[nv] + 0.5 * U[nv];
     }

@@ -216,7 +216,7 @@ __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params 
       for (int nv = 0; nv < NV; nv++) V[nv * p.vstride + c] = v[nv];
       if (stage == 2) {
         double u[NV];
-        prim_to_cons<NV>(v, u, p.gmm1);
+        prim_to_cons<NV>(v, u, p.igmm1);
 #pragma unroll
         for (int nv = 0; nv < NV; nv++) Us[nv * p.vstride + c] = u[nv];
       }
@@ -514,7 +514,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
   constexpr int VN = VX1 + D;
   const Params &p = A.s.p;
   const SphGeom &g = A.g;
-  const double gam = p.gamma, gmm1 = p.gmm1;
+  const double gam = p.gamma;
 
   // (1) PLM with the general-grid weights of the cell, on the primitive or
   // (CHAR_LIMITING) the characteristic variables
@@ -599,7 +599,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
         }
       }
     }
-    riemann<NV, SOLVER, VN>(vL, vR, gam, gmm1, f, pr, cmx, hll);
+    riemann<NV, SOLVER, VN>(vL, vR, gam, p.igmm1, f, pr, cmx, hll);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) sf[nv * G::NFMAX + q] = f[nv];
     spr[q] = pr;
@@ -761,7 +761,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       const int s0 = (cy + TL::HY) * G::SX + cx + TL::HX;
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v[nv] = sv[nv * G::VS + s0];
-      prim_to_cons<NV>(v, U, p.gmm1);
+      prim_to_cons<NV>(v, U, p.igmm1);
     } else {
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = a.Us[nv * p.vstride + cell];
@@ -815,7 +815,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
       if constexpr (NV == NFLX + 2) v0[NV - 1] = v0[PRS] * rho_pow(v0[RHO], -p.gamma);
-      prim_to_cons<NV>(v0, U0, p.gmm1);
+      prim_to_cons<NV>(v0, U0, p.igmm1);
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = 0.5 * U0[nv] + 0.5 * U[nv];
     }
