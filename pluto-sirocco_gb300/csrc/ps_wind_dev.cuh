@@ -667,23 +667,15 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
       for (int nv = 0; nv < NV; nv++) vc[nv] = sv[nv * G::VS + s0];
       const double r_1 = g.rtinv[gi], ct = g.ct[gj];
       const double vphi = vc[VX3];
-      double Sm = vc[RHO] * (-vc[VX2] * vc[VX1] + ct * vphi * vphi);
-      Sm += 0.0 - ct * 0.0;
+      // the reference also adds the x2 and x3 components of the point-mass
+      // gravity and the x3 component of the line force, all exact zeros
+      // (rhs_source.c:339-396); they are left out
+      const double Sm = vc[RHO] * (-vc[VX2] * vc[VX1] + ct * vphi * vphi);
       rhs[VX2] += dt * Sm * r_1;
-      if (A.w.body_force) {
-        const double g1 = 0.0, g2 = 0.0;
-        rhs[VX2] += dt * vc[RHO] * g1;
-        rhs[PRS] += dt * 0.5 * mflux * g1;
-        rhs[VX3] += dt * vc[RHO] * g2;
-        rhs[PRS] += dt * vc[RHO] * vc[VX3] * g2;
-      }
       if (A.w.line_force) {
         const double gt = line_force<NV>(vc, A.L, A.w, e0, e1, 1, vcell(p, gj, gi), p.vstride);
-        const double gz = 0.0;
         rhs[VX2] += dt * vc[RHO] * gt;
         rhs[PRS] += dt * 0.5 * mflux * gt;
-        rhs[VX3] += dt * vc[RHO] * gz;
-        rhs[PRS] += dt * vc[RHO] * vc[VX3] * gz;
       }
     }
 #pragma unroll
