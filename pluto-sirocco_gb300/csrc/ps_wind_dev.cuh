@@ -64,6 +64,42 @@ __device__ __forceinline__ double limited_slope_general(double dvp, double dvm, 
   }
 }
 
+// The van Leer slopes of n variables of one cell with one division: the
+// denominators' reciprocals by Montgomery's simultaneous inversion (prefix
+// products, one reciprocal of the total, a backward pass).  Variables whose
+// one-sided differences have opposite signs get slope 0 and denominator 1.
+// When the product of the denominators leaves the normal range, each slope
+// takes its own division.  The slopes stay within a few ulps of the direct
+// quotients.
+template <int N>
+__device__ __forceinline__ void vl_slopes(const double (&dvp)[N], const double (&dvm)[N],
+                                          double cp, double cm, double (&dv)[N])
+{
+  const double c2 = cp + cm - 2.0;
+  double num[N], den[N], pre[N];
+  double prod = 1.0;
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    const double pm = dvp[k] * dvm[k];
+    const bool on = pm > 0.0;
+    num[k] = on ? pm * (cp * dvm[k] + cm * dvp[k]) : 0.0;
+    den[k] = on ? dvp[k] * dvp[k] + dvm[k] * dvm[k] + c2 * pm : 1.0;
+    pre[k] = prod;
+    prod *= den[k];
+  }
+  if (prod >= 2.2250738585072014e-308 && prod <= 1.7976931348623157e308) {
+    double r = 1.0 / prod;
+#pragma unroll
+    for (int k = N - 1; k >= 0; k--) {
+      dv[k] = num[k] * (r * pre[k]);
+      r *= den[k];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; k++) dv[k] = num[k] / den[k];
+  }
+}
+
 // Limited slopes on characteristic variables (CHAR_LIMITING YES,
 // Src/States/plm_states.c:481-746, HD with energy, general grid): the
 // one-sided differences projected on the left primitive eigenvectors
@@ -562,6 +598,22 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
         const double dv = dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0;
         svp[nv * G::NPMAX + q] = v0 + dv * dp;
         svm[nv * G::NPMAX + q] = v0 - dv * dm;
+      }
+      continue;
+    }
+    if constexpr (LIM == LIM_VL) {
+      double v0[NV], dvp[NV], dvm[NV], dv[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        v0[nv] = sv[nv * G::VS + s0];
+        dvp[nv] = (sv[nv * G::VS + s0 + SST] - v0[nv]) * wp;
+        dvm[nv] = (v0[nv] - sv[nv * G::VS + s0 - SST]) * wm;
+      }
+      vl_slopes<NV>(dvp, dvm, cp, cm, dv);
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        svp[nv * G::NPMAX + q] = v0[nv] + dv[nv] * dp;
+        svm[nv * G::NPMAX + q] = v0[nv] - dv[nv] * dm;
       }
       continue;
     }
