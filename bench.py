@@ -68,10 +68,13 @@ IDL_NUMERICS = dict(char_limiting=1, shock_flattening=1, entropy_switch=2)
 
 
 class Workload:
-    def __init__(self, name, numerics="plm"):
+    def __init__(self, name, numerics="plm", flux="radial"):
         self.name = name
         self.numerics = numerics
-        self.numerics_kw = IDL_NUMERICS if numerics == "idl" else {}
+        self.flux = flux
+        self.numerics_kw = dict(IDL_NUMERICS if numerics == "idl" else {})
+        if flux == "dense":
+            self.numerics_kw["dense_flux"] = True
         if name == "wind":
             self.nx, self.ny, self.nvar = 512, 256, 6
             self.steps = 1000
@@ -121,6 +124,10 @@ class Workload:
             self.desc += ("; production limiting: characteristic PLM, MULTID shock flattening,"
                           " ENTROPY_SWITCH ALWAYS")
             self.profile = "stage_kernel_wind_batch64_idl.md"
+        if flux == "dense":
+            self.desc += ("; UV flux in all 36 bins (the library's dense synthetic flux, the "
+                          "shape of SIROCCO's fluxes)")
+            self.profile = "stage_kernel_wind_batch64_dense.md"
 
     def solver(self):
         """Device context with the initial state loaded."""
@@ -163,8 +170,8 @@ def _env_rank():
 # ----------------------------------------------------------------------
 
 def _cpu_worker(args):
-    name, steps, idx, numerics = args
-    wl = Workload(name, numerics)
+    name, steps, idx, numerics, flux = args
+    wl = Workload(name, numerics, flux)
     if name == "batch":
         from oracle import wind_oracle
         sp = wl.specs[idx % len(wl.specs)]
@@ -202,7 +209,8 @@ def cpu_throughput(wl, steps, procs=None):
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(n) as pool:
-        res = pool.map(_cpu_worker, [(wl.name, steps, i, wl.numerics) for i in range(n)])
+        res = pool.map(_cpu_worker, [(wl.name, steps, i, wl.numerics, wl.flux)
+                                     for i in range(n)])
     wall = time.perf_counter() - t0
     per = [r[0] for r in res]
     cells = sum(r[1] for r in res)
@@ -750,7 +758,7 @@ def _line_force_figures(wl):
         cfg = psgb.make_wind_config(nr, nt)
         w = psgb.make_wind(l_star=sp["l_star"], krad=sp["krad"], alpharad=sp["alpharad"])
         g = psgb.WindGrid(cfg)
-        fr, ft, _ = psgb.wind_flux(cfg, w, g)
+        fr, ft, _ = psgb.wind_flux(cfg, w, g, dense=wl.flux == "dense")
         act = (slice(None), 0, slice(2, -2), slice(2, -2))
         bins += int(np.count_nonzero((fr[act] != 0.0) | (ft[act] != 0.0)))
         cells += nr * nt
@@ -758,7 +766,9 @@ def _line_force_figures(wl):
     return {"bins_per_cell": per_cell, "angles": 36,
             "bytes_per_cell_update": 2 * 12 * 8 * per_cell,
             "dense_design_bytes_per_cell_update": 2 * 5 * 36 * 8,
-            "flux": "synthetic: the radial bin of each cell (real SIROCCO fluxes fill more bins)"}
+            "flux": ("synthetic, all 36 bins" if wl.flux == "dense" else
+                     "synthetic: the radial bin of each cell (real SIROCCO fluxes fill more "
+                     "bins)")}
 
 
 def _rooflines(out, wl, stage_ms, per_kernel):
@@ -824,10 +834,13 @@ def main():
     ap.add_argument("--numerics", default="plm", choices=["plm", "idl"],
                     help="batch workload: primitive PLM (default) or the production cv_idl "
                          "limiting (characteristic PLM, MULTID, entropy switch)")
+    ap.add_argument("--flux", default="radial", choices=["radial", "dense"],
+                    help="batch workload: UV flux in each cell's radial bin (default) or in "
+                         "all 36 bins")
     a = ap.parse_args()
-    if a.numerics != "plm" and a.workload != "batch":
-        ap.error("--numerics idl is offered for the batch workload")
-    wl = Workload(a.workload, a.numerics)
+    if (a.numerics != "plm" or a.flux != "radial") and a.workload != "batch":
+        ap.error("--numerics and --flux are offered for the batch workload")
+    wl = Workload(a.workload, a.numerics, a.flux)
     if a.workload == "cube" and a.cube_n != 512:
         wl.nx = wl.ny = wl.nz = a.cube_n
         wl.cells = a.cube_n ** 3

@@ -163,6 +163,14 @@ int ps_wind_synthetic_flux(const ps_config *cfg, const ps_wind *w,
                            const double *x1, const double *x2,
                            double *fr, double *ft, double *fp);
 
+/* The same with flux in every bin, a stand-in for SIROCCO's fluxes (which
+ * fill most bins): weight 1 in the radial bin, 0.05/(1 + |d|) d bins away,
+ * split into (F_r, F_theta) by the cosine and sine of the bin's angle from
+ * the radial one, rounded the same way. */
+int ps_wind_synthetic_flux_dense(const ps_config *cfg, const ps_wind *w,
+                                 const double *x1, const double *x2,
+                                 double *fr, double *ft, double *fp);
+
 /* Readers of the files a SIROCCO run hands to the wind problem
  * (Src/LineDriven/line_connect.c:43-497), host only.  Records are placed on
  * the 2-D spherical grid (x1, x2: cell-centre arrays of the total box, x1 in

@@ -115,20 +115,45 @@ def synthetic_mfit(x1, x2, ntot, ngh=2, npoints=MFIT_POINTS):
     return t, m
 
 
-def synthetic_flux(x1, x2, ntot, l_uv=1.0e37, unit_length=1e9, na=NANGLES, ngh=2):
+def dense_flux_bins(theta, f0, na=NANGLES):
+    """The dense synthetic flux of one cell at polar angle theta with
+    L_UV/(4 pi r^2) = f0: every bin a carries f0 w(d) at the angle
+    d 2pi/na from the radial bin a0 (d = a - a0), w = 1 at d = 0 and
+    0.05/(1 + |d|) elsewhere, split into (F_r, F_theta) = (cos, sin) of that
+    angle; values rounded through 13 significant digits."""
+    import math
+    a0 = int(math.floor(theta / (2 * 3.14159265358979 / 36)))
+    fr, ft = [], []
+    for a in range(na):
+        d = a - a0
+        w = 1.0 if d == 0 else 0.05 / (1.0 + abs(d))
+        ang = d * (2.0 * math.pi / na)
+        fr.append(float("%.12e" % (f0 * w * math.cos(ang))))
+        ft.append(float("%.12e" % (f0 * w * math.sin(ang))))
+    return fr, ft
+
+
+def synthetic_flux(x1, x2, ntot, l_uv=1.0e37, unit_length=1e9, na=NANGLES, ngh=2, dense=False):
     """Synthetic directional UV flux: L_UV/(4 pi r^2) in the angle bin that
     contains the radial direction of each active cell, zero elsewhere; the
     values are rounded through the 13-significant-digit text of the
-    directional_flux_*.dat files the reference reads.  Arrays are
-    [angle][k][j][i] over the total box (ghost cells zero)."""
+    directional_flux_*.dat files the reference reads.  dense: every bin
+    carries flux instead (dense_flux_bins).  Arrays are [angle][k][j][i]
+    over the total box (ghost cells zero)."""
     import math
     fr = np.zeros((na, ntot[2], ntot[1], ntot[0]))
+    ft = np.zeros_like(fr)
     for j in range(ngh, ntot[1] - ngh):
         a = int(math.floor(x2[j] / (2 * 3.14159265358979 / 36)))
         for i in range(ngh, ntot[0] - ngh):
             r = x1[i] * unit_length
-            fr[a, :, j, i] = float("%.12e" % (l_uv / (4 * math.pi * r * r)))
-    return fr, np.zeros_like(fr), np.zeros_like(fr)
+            if dense:
+                bfr, bft = dense_flux_bins(x2[j], l_uv / (4 * math.pi * r * r), na)
+                fr[:, :, j, i] = np.array(bfr)[:, None]
+                ft[:, :, j, i] = np.array(bft)[:, None]
+            else:
+                fr[a, :, j, i] = float("%.12e" % (l_uv / (4 * math.pi * r * r)))
+    return fr, ft, np.zeros_like(fr)
 
 
 class Oracle:
@@ -243,7 +268,7 @@ class Oracle:
 
 def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, char_limiting=0,
                 shock_flattening=0, solver="hll", entropy_switch=0, mfit=False, ode_cooling=0,
-                **params):
+                dense_flux=False, **params):
     """The 2-D spherical line-driven disk wind (PLM van Leer, HLL, RK2,
     userdef/outflow/axisymmetric/reflective boundaries, point-mass gravity,
     floors, BLONDIN cooling and the line force), initialised.  mfit: the
@@ -261,7 +286,8 @@ def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, c
     if line_force:
         prm = dict(WIND, **params)
         o.set_flux(*synthetic_flux(o.grid(0), o.grid(1), o.ntot,
-                                   l_uv=prm["l_star"] * prm["f_uv"], ngh=o.ngh[0]))
+                                   l_uv=prm["l_star"] * prm["f_uv"], ngh=o.ngh[0],
+                                   dense=dense_flux))
     if mfit:   # KRAD = ALPHARAD = 999: the tabulated force multiplier
         o.set_mfit(*synthetic_mfit(o.grid(0), o.grid(1), o.ntot, ngh=o.ngh[0]))
     o.init_wind()

@@ -483,7 +483,9 @@ __device__ __forceinline__ void bilinear_w(double fx, double fy, const double (&
 // (1 + M) sigma_e F / c, M = min(krad t^alpharad, 4400), t = sigma_e rho
 // v_th / (dv/ds), M = 0 where dv/ds <= 0.  Evaluated as
 // M = exp(lf_a0 + alpharad/2 log(rho p) + lq) with lq = -alpharad log(dv/ds)
-// from VGradCalc (one log per call, one exp per bin).  With KRAD = ALPHARAD
+// from VGradCalc (one log per call, one exp per bin); for cells with two or
+// more bins as M = (rho p)^(alpharad/2) B, B = exp(lf_a0 + lq) formed once per
+// stage in VGradCalc (one log and one exp per call).  With KRAD = ALPHARAD
 // = 999, M is interpolated in the cell's table at log10 t = lt0 +
 // log10(rho p)/2 + lq, lq = -log10(dv/ds).
 template <int NV>
@@ -515,6 +517,22 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
         }
         M = exp10(y);
         if (is_nan_bits(M)) M = 0.0;
+        if (M > 4400.) M = 4400.;
+      }
+      const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
+      g += (1.0 + M) * F;
+    }
+    return g * w.lf_cf;
+  }
+  if (e1 - e0 >= 2) {
+    // M = (rho p)^(alpharad/2) times the bin's factor from VGradCalc (0 where
+    // dv/ds <= 0)
+    const double Q = exp(0.5 * w.alpharad * log(vg[RHO] * vg[PRS]));
+    for (int e = e0; e < e1; e++) {
+      const double B = L.lq[e];
+      double M = 0.0;
+      if (B > 0.0) {
+        M = Q * B;
         if (M > 4400.) M = 4400.;
       }
       const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
@@ -830,9 +848,13 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       v21[1] = (V2[sc0 + 1] + V2[jm + 1] + V2[jm] + V2[sc0]) / 4.0;
       bilinear_w(g.fx[gi], g.fy[gj], v11, v12, v21, v22, ans1);
       const double alpha = A.w.alpharad;
+      // two or more bins: the bin's factor k C^alpha (dv/ds)^-alpha is kept
+      // instead of its log, so that each sweep needs one power of rho p and
+      // a product per bin (line_force)
+      const bool fact = e1 - e0 >= 2;
       for (int e = e0; e < e1; e++) {
         const double ids = A.L.inv_ds[e];
-        double lq = -INFINITY;
+        double lq = (fact && !A.w.mfit) ? 0.0 : -INFINITY;
         if (ids != 0.0) {
           double ans2[2];
           bilinear_w(A.L.fr1[e], A.L.fr2[e], v11, v12, v21, v22, ans2);
@@ -840,7 +862,10 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
           const double v2 = ans2[0] * A.L.c2a[e] + ans2[1] * A.L.c2b[e];
           const double dvds = fabs(v2 - v1) * ids;
           if (is_nan_bits(dvds)) flags |= F_NAN;
-          if (dvds > 0.0) lq = A.w.mfit ? -log10(dvds) : -alpha * log(dvds);
+          if (dvds > 0.0)
+            lq = A.w.mfit ? -log10(dvds)
+                 : fact   ? exp(A.w.lf_a0 - alpha * log(dvds))
+                          : -alpha * log(dvds);
         }
         A.L.lq[e] = lq;
       }

@@ -258,3 +258,58 @@ int ps_wind_synthetic_flux(const ps_config *cfg, const ps_wind *w,
   }
   return 0;
 }
+
+int ps_wind_synthetic_flux_dense(const ps_config *cfg, const ps_wind *w, const double *x1,
+                                 const double *x2, double *fr, double *ft, double *fp)
+{
+  int n0, n1, na, i, j, a;
+  size_t nc;
+  char buf[64];
+  double l_uv;
+  if (!cfg || !w || !x1 || !x2 || !fr || !ft || !fp || cfg->dims != 2 || w->nangles < 1 ||
+      w->nangles > 64) {
+    ps_set_error_msg("ps_wind_synthetic_flux_dense: bad arguments");
+    return PS_EINVAL;
+  }
+  const int ng = PS_NGHOST(cfg);
+  n0 = cfg->nx[0] + 2 * ng;
+  n1 = cfg->nx[1] + 2 * ng;
+  nc = (size_t)n0 * n1;
+  na = w->nangles;
+  memset(fr, 0, (size_t)na * nc * sizeof(double));
+  memset(ft, 0, (size_t)na * nc * sizeof(double));
+  memset(fp, 0, (size_t)na * nc * sizeof(double));
+  l_uv = w->l_star * w->f_uv;
+  /* the rounded values depend on the column i and the bin offset d only:
+   * tabulate them once per column (d in [-(na-1), na-1]) */
+  const int nd = 2 * na - 1;
+  double *tr = (double *)malloc(sizeof(double) * (size_t)nd * 2);
+  if (!tr) {
+    ps_set_error_msg("ps_wind_synthetic_flux_dense: out of memory");
+    return PS_EINVAL;
+  }
+  for (i = ng; i < n0 - ng; i++) {
+    const double r = x1[i] * w->unit_length;
+    const double f0 = l_uv / (4 * 3.141592653589793 * r * r);
+    int d;
+    for (d = -(na - 1); d <= na - 1; d++) {
+      const double wt = d == 0 ? 1.0 : 0.05 / (1.0 + (double)abs(d));
+      const double ang = d * (2.0 * 3.141592653589793 / na);
+      snprintf(buf, sizeof(buf), "%.12e", f0 * wt * cos(ang));
+      tr[2 * (d + na - 1)] = strtod(buf, NULL);
+      snprintf(buf, sizeof(buf), "%.12e", f0 * wt * sin(ang));
+      tr[2 * (d + na - 1) + 1] = strtod(buf, NULL);
+    }
+    for (j = ng; j < n1 - ng; j++) {
+      const int a0 = (int)floor(x2[j] / (2 * W_PI / 36));
+      for (a = 0; a < na; a++) {
+        const int k = a - a0 + na - 1;
+        if (k < 0 || k >= nd) continue;
+        fr[(size_t)a * nc + (size_t)j * n0 + i] = tr[2 * k];
+        ft[(size_t)a * nc + (size_t)j * n0 + i] = tr[2 * k + 1];
+      }
+    }
+  }
+  free(tr);
+  return 0;
+}

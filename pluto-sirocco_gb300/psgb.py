@@ -26,7 +26,8 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_advance_step", "ps_run", "ps_sync", "ps_device_state", "ps_launch_count",
            "ps_get_dt_history", "ps_set_stream", "ps_probe_fp64_flops", "ps_save_state",
            "ps_restore_state", "ps_time_step_kernels", "ps_advance_step_noalloc",
-           "ps_init_wind", "ps_wind_synthetic_flux", "ps_set_wind", "ps_split_source",
+           "ps_init_wind", "ps_wind_synthetic_flux", "ps_wind_synthetic_flux_dense",
+           "ps_set_wind", "ps_split_source",
            "ps_batch_create", "ps_batch_destroy", "ps_batch_run", "ps_batch_sync",
            "ps_batch_set_stream", "ps_batch_launch_count", "ps_batch_set_shape",
            "ps_batch_get_shape", "ps_batch_autotune", "ps_batch_time_step_kernels",
@@ -125,6 +126,8 @@ def lib():
                                    DP, DP, DP, DP]
         L.ps_wind_synthetic_flux.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Wind), DP,
                                              DP, DP, DP, DP]
+        L.ps_wind_synthetic_flux_dense.argtypes = [ctypes.POINTER(Config),
+                                                   ctypes.POINTER(Wind), DP, DP, DP, DP, DP]
         L.ps_set_wind.argtypes = [P, ctypes.POINTER(Wind), DP, DP, DP]
         L.ps_split_source.argtypes = [P, D, D]
         L.ps_batch_create.argtypes = [ctypes.POINTER(P), I, ctypes.POINTER(P)]
@@ -247,12 +250,19 @@ def wind_state(cfg, wind, grid):
     return V
 
 
-def wind_flux(cfg, wind, grid):
+def wind_flux(cfg, wind, grid, dense=False):
+    """Synthetic directional UV flux, [angle][k][j][i] over the total box:
+    L_UV/(4 pi r^2) in the bin of each cell's radial direction
+    (ps_wind_synthetic_flux), or with dense=True in every bin: weight 1 in
+    the radial bin and 0.05/(1 + |d|) d bins away, split into (F_r, F_theta)
+    by the cosine and sine of the bin's angle from the radial one -- a stand-in
+    for SIROCCO's fluxes, which fill most bins.  Values are rounded through
+    13 significant digits as the flux files carry them."""
     shape = (wind.nangles, 1, grid.ntot[1], grid.ntot[0])
     fr, ft, fp = np.zeros(shape), np.zeros(shape), np.zeros(shape)
-    check(lib().ps_wind_synthetic_flux(ctypes.byref(cfg), ctypes.byref(wind), _dp(grid.x(0)),
-                                       _dp(grid.x(1)), _dp(fr), _dp(ft), _dp(fp)),
-          "ps_wind_synthetic_flux")
+    fn = lib().ps_wind_synthetic_flux_dense if dense else lib().ps_wind_synthetic_flux
+    check(fn(ctypes.byref(cfg), ctypes.byref(wind), _dp(grid.x(0)), _dp(grid.x(1)), _dp(fr),
+             _dp(ft), _dp(fp)), "ps_wind_synthetic_flux")
     return fr, ft, fp
 
 
@@ -547,7 +557,7 @@ def batch_models(n=64, seed=4):
 
 
 def wind_model_solver(spec, cooling=1, line_force=1, char_limiting=0, shock_flattening=0,
-                      entropy_switch=0):
+                      entropy_switch=0, dense_flux=False):
     """One wind context for a batch spec (see batch_models)."""
     nr, nt = spec["grid"]
     cfg = make_wind_config(nr, nt, cooling=cooling, char_limiting=char_limiting,
@@ -558,7 +568,7 @@ def wind_model_solver(spec, cooling=1, line_force=1, char_limiting=0, shock_flat
     s = Solver(cfg, g)
     s.set_state(wind_state(cfg, w, g))
     s.set_time(0.0, 1e-4, 0)
-    s.set_wind(w, wind_flux(cfg, w, g) if line_force else None)
+    s.set_wind(w, wind_flux(cfg, w, g, dense=dense_flux) if line_force else None)
     return s
 
 

@@ -195,16 +195,17 @@ def run_case(ref, name, cfg, dims, n, solver, bc, steps, full):
     print(name, "t =", t_s, "dt =", dt_s)
 
 
-def write_flux_files(wd, nr, nt):
+def write_flux_files(wd, nr, nt, dense=False):
     """directional_flux_{r,theta,phi}.dat in the format read by
     read_sirocco_fluxes (Src/LineDriven/line_connect.c:84-165): two header
     lines (the second holds the angle count as its third token), then one
-    row per active cell: i j k r[cm] theta[rad] F_0 .. F_35."""
+    row per active cell: i j k r[cm] theta[rad] F_0 .. F_35.  dense: flux in
+    every bin (oracle.dense_flux_bins)."""
     import psgb
     from oracle import synthetic_flux, NANGLES, WIND
     x1 = psgb.build_grid(nr, 2, 10.0, 1000.0, "log")[0]
     x2 = psgb.build_grid(nt, 2, 0.0, 1.5707963267948966, "uniform")[0]
-    fl = synthetic_flux(x1, x2, (nr + 4, nt + 4, 1))
+    fl = synthetic_flux(x1, x2, (nr + 4, nt + 4, 1), dense=dense)
     for ax, name in enumerate(("r", "theta", "phi")):
         with open(os.path.join(wd, f"directional_flux_{name}.dat"), "w") as f:
             f.write("# synthetic directional UV flux\n")
@@ -253,6 +254,7 @@ WIND_CASES = [
      dict(char_limiting=1, shock_flattening=1, entropy_switch=2)),
     ("wind2d_mfit_64x32", "wind2d", (64, 32), 100, 20, True, dict(mfit=True)),
     ("wind2d_ode_64x32", "wind2d_ode", (64, 32), 100, 20, True, dict(ode_cooling=1)),
+    ("wind2d_dense_64x32", "wind2d", (64, 32), 100, 20, True, dict(dense_flux=1)),
 ]
 
 
@@ -269,7 +271,7 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux, opts):
                                 solver=opts.get("solver", "hll"),
                                 krad=999 if mfit else 0.2, alpharad=999 if mfit else -0.6))
     if flux:
-        write_flux_files(wd, n[0], n[1])
+        write_flux_files(wd, n[0], n[1], dense=bool(opts.get("dense_flux", 0)))
     if opts.get("mfit"):
         write_mfit_file(wd, n[0], n[1])
     subprocess.run([exe, "-maxsteps", str(steps - 1)], cwd=wd, check=True,
@@ -286,7 +288,7 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux, opts):
                 line_force=int(flux), char_limiting=opts.get("char_limiting", 0),
                 shock_flattening=opts.get("shock_flattening", 0),
                 entropy_switch=opts.get("entropy_switch", 0), mfit=int(opts.get("mfit", 0)),
-                ode_cooling=opts.get("ode_cooling", 0),
+                ode_cooling=opts.get("ode_cooling", 0), dense_flux=opts.get("dense_flux", 0),
                 solver=opts.get("solver", "hll"),
                 t=[lines[k][1] for k in keep],
                 dt=[lines[k][2] for k in keep], final_sha256=digest(snaps[-1]))

@@ -181,6 +181,30 @@ def test_wind_tabulated_force_multiplier_matches_reference(built, tmp_path):
     assert not np.allclose(_active(h.get_state()), snaps[-1], rtol=1e-6)
 
 
+def test_wind_dense_flux_matches_reference(built):
+    """Flux in every one of the 36 bins (the shape of SIROCCO's fluxes): the
+    line force takes its factored form (one power of rho p per sweep and a
+    product per bin) and matches the reference run on the same flux files."""
+    import psgb
+    meta = _case("wind2d_dense")
+    snaps = np.load(meta["npz"])["snaps"]
+    nr, nt = meta["n"][0], meta["n"][1]
+    cfg = psgb.make_wind_config(nr, nt, cooling=1)
+    w = psgb.make_wind(line_force=1)
+    g = psgb.WindGrid(cfg)
+    s = psgb.Solver(cfg, g)
+    s.set_state(psgb.wind_state(cfg, w, g))
+    s.set_time(0.0, 1e-4, 0)
+    s.set_wind(w, psgb.wind_flux(cfg, w, g, dense=True))
+    done = 0
+    for k, step in enumerate(meta["snap_steps"]):
+        if step > done:
+            s.run(step - done)
+            done = step
+        r = assert_hydro_close(_active(s.get_state()), snaps[k], f"step {step}")
+        print("dense flux, step", step, "relative L1 per variable", r)
+
+
 def test_wind_ode_cooling_matches_reference(built):
     """The ODE cooling path (cooling = 2: COOLING TABULATED with the
     production problem's CoolingSource and Radiat, RKF12 or adaptive

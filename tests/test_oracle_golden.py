@@ -66,7 +66,8 @@ def test_wind_oracle_matches_reference(built, meta):
                     shock_flattening=meta.get("shock_flattening", 0),
                     solver=meta.get("solver", "hll"),
                     entropy_switch=meta.get("entropy_switch", 0), mfit=bool(meta.get("mfit", 0)),
-                    ode_cooling=meta.get("ode_cooling", 0))
+                    ode_cooling=meta.get("ode_cooling", 0),
+                    dense_flux=bool(meta.get("dense_flux", 0)))
     done = 0
     for k, step in enumerate(meta["snap_steps"]):
         if step > done:

@@ -105,3 +105,16 @@ def test_force_multiplier_table_file(built, tmp_path):
     assert np.all(m[:, :2] == 1.0)          # ghost rows keep the caller's values
     with pytest.raises(RuntimeError):       # more points than room for them
         psgb.read_m_uv_fit(cfg, g, str(tmp_path / "M_UV_data.dat"), max_points=4)
+
+
+def test_dense_flux_matches_the_golden_generator(built):
+    """The dense synthetic flux of the library (every bin filled) is the one
+    the golden reference run read from its flux files."""
+    import psgb
+    from oracle import synthetic_flux
+    cfg, g = _grid()
+    w = psgb.make_wind()
+    fr, ft, fp = psgb.wind_flux(cfg, w, g, dense=True)
+    er, et, ep = synthetic_flux(g.x(0), g.x(1), g.ntot, l_uv=w.l_star * w.f_uv, dense=True)
+    assert np.array_equal(fr, er) and np.array_equal(ft, et) and np.array_equal(fp, ep)
+    assert np.count_nonzero(fr[:, 0, 2:-2, 2:-2]) > 30 * cfg.nx[0] * cfg.nx[1]
