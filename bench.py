@@ -165,6 +165,26 @@ def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
 
 
+def max_over_ranks(ms, dist):
+    """Replicas only: every rank runs the whole workload on its own GPU; the
+    job's time is the slowest rank's (all-reduce MAX, then a barrier).  dist
+    is torch.distributed or None for one rank."""
+    if not dist:
+        return ms
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    tt = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(tt.item())
+
+
+def replica_rate(cells, steps, world, ms):
+    """Whole-job cell-updates/s of `world` replicas of `cells` cells each
+    over `steps` steps in `ms` milliseconds (the slowest rank's)."""
+    return cells * steps * world / (ms * 1e-3)
+
+
 # ----------------------------------------------------------------------
 # CPU side (oracle restatement of the reference)
 # ----------------------------------------------------------------------
@@ -362,12 +382,8 @@ def gpu_bench(wl, steps, warmup, rank, world):
     launches = s.launches() - launches0
     flags = s.sync()
     ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
-    if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-        dist.barrier()
-    value = wl.cells * steps * world / (ms * 1e-3)
+    ms = max_over_ranks(ms, dist)
+    value = replica_rate(wl.cells, steps, world, ms)
     t_end, _, step_end, _ = s.time()
 
     # per-kernel durations (extra steps outside the timed region)
@@ -507,14 +523,10 @@ def batch_bench(wl, steps, warmup, rank, world):
                 b.record(stream)
             torch.cuda.synchronize()
         ms = sum(a.elapsed_time(b) for a, b in ev)
-        if dist:
-            tt = torch.tensor([ms], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            ms = float(tt.item())
-            dist.barrier()
+        ms = max_over_ranks(ms, dist)
         return ms, clk.summary()
 
-    rate = lambda ms: wl.cells * steps * world / (ms * 1e-3)
+    rate = lambda ms: replica_rate(wl.cells, steps, world, ms)
 
     # plain GPU form
     plain, _ = make()
@@ -653,14 +665,10 @@ def cube_bench(wl, steps, warmup, rank, world):
                 b.record(stream)
             torch.cuda.synchronize()
         ms = sum(a.elapsed_time(b) for a, b in ev)
-        if dist:
-            tt = torch.tensor([ms], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            ms = float(tt.item())
-            dist.barrier()
+        ms = max_over_ranks(ms, dist)
         return ms, clk.summary()
 
-    rate = lambda ms: wl.cells * steps * world / (ms * 1e-3)
+    rate = lambda ms: replica_rate(wl.cells, steps, world, ms)
     ms_plain, _ = timed()
     flags_plain = s.sync()
     # training tuples: cells of the plain run after 10 steps, plus draws
