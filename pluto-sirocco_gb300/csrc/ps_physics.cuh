@@ -183,13 +183,13 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
     fR[VX2] = uR[VX2] * vR[VN];
     fR[VX3] = uR[VX3] * vR[VN];
     fR[PRS] = (uR[PRS] + vR[PRS]) * vR[VN];
+    // (SL SR (uR - uL) + SR fL - SL fR) / (SR - SL) with the three weights
+    // divided once
     const double scrh = 1.0 / (SR - SL);
+    const double a = SL * SR * scrh, bR = SR * scrh, bL = SL * scrh;
 #pragma unroll
-    for (int nv = 0; nv < NFLX; nv++) {
-      double t = SL * SR * (uR[nv] - uL[nv]) + SR * fL[nv] - SL * fR[nv];
-      f[nv] = t * scrh;
-    }
-    pr = (SR * vL[PRS] - SL * vR[PRS]) * scrh;
+    for (int nv = 0; nv < NFLX; nv++) f[nv] = a * (uR[nv] - uL[nv]) + bR * fL[nv] - bL * fR[nv];
+    pr = bR * vL[PRS] - bL * vR[PRS];
   } else {
     // HLLC: only the star state on the side selected by the contact speed
     // is formed; the reference forms both and discards one.

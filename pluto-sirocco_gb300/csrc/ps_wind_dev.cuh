@@ -696,15 +696,14 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
       fr_phi = g.spabs[gj];
       dtdl = A.s.dtdx[1][gj] * g.rtinv[gi];
     }
+    // -dt/dV (F_r A_r - F_l A_l) with the area and dt/dV folded into one
+    // weight per face (the phi momentum's face factors as well)
     double rhs[NV];
+    const double cl = dtdV * Al, cr = -dtdV * Ar;
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
-      double fAl = sf[nv * G::NFMAX + ql] * Al, fAr = sf[nv * G::NFMAX + qr] * Ar;
-      if (nv == VX3) {
-        fAl *= fl_phi;
-        fAr *= fr_phi;
-      }
-      rhs[nv] = -dtdV * (fAr - fAl);
+      const double wl = nv == VX3 ? cl * fl_phi : cl, wr = nv == VX3 ? cr * fr_phi : cr;
+      rhs[nv] = sf[nv * G::NFMAX + qr] * wr + sf[nv * G::NFMAX + ql] * wl;
     }
     rhs[VN] -= dtdl * (spr[qr] - spr[ql]);
     rhs[VX3] *= D == 0 ? g.inv_absx1[gi] : g.inv_sn[gj];
