@@ -117,3 +117,59 @@ def test_wind_requires_spherical_nvar6(built):
     cfg.geometry = psgb.SPHERICAL
     ctx = ctypes.c_void_p()
     assert psgb.lib().ps_create(ctypes.byref(cfg), ctypes.byref(ctx)) == -1
+
+
+@pytest.mark.parametrize("case", ["entropy_cartesian", "nvar7_without_entropy", "nvar6_with_entropy",
+                                  "char_cartesian", "multid_cartesian", "ode_cartesian",
+                                  "entropy_out_of_range", "cooling_out_of_range"])
+def test_numerics_switches_rejected_without_gpu(built, case):
+    """The production numerics and the ODE cooling path are built for the
+    spherical wind: other combinations are refused before any device work."""
+    import psgb
+    if case in ("entropy_cartesian", "char_cartesian", "multid_cartesian", "ode_cartesian"):
+        cfg = psgb.make_config(dims=2, nx=(32, 32, 1), nvar=7 if case == "entropy_cartesian" else 5)
+    else:
+        cfg = psgb.make_wind_config(32, 16)
+    if case == "entropy_cartesian":
+        cfg.entropy_switch = 2
+    elif case == "nvar7_without_entropy":
+        cfg.nvar = 7
+    elif case == "nvar6_with_entropy":
+        cfg.entropy_switch = 2
+        cfg.nvar = 6
+    elif case == "char_cartesian":
+        cfg.char_limiting = 1
+    elif case == "multid_cartesian":
+        cfg.shock_flattening = 1
+    elif case == "ode_cartesian":
+        cfg.cooling = 2
+    elif case == "entropy_out_of_range":
+        cfg.entropy_switch = 3
+    else:
+        cfg.cooling = 3
+    ctx = ctypes.c_void_p()
+    assert psgb.lib().ps_create(ctypes.byref(cfg), ctypes.byref(ctx)) == -1
+    assert psgb.lib().ps_last_error()
+    assert not ctx.value
+
+
+def test_wind_host_helpers_with_three_ghost_zones_and_entropy(built):
+    """MULTID contexts carry 3 ghost zones per side (GetNghost): the host
+    grid, initial state (with the entropy s = p / rho^gamma of the entropy
+    switch) and flux arrays follow, matching the oracle's."""
+    import psgb
+    from oracle import wind_oracle, synthetic_flux
+    cfg = psgb.make_wind_config(40, 20, char_limiting=1, shock_flattening=1, entropy_switch=2)
+    assert psgb.nghost(cfg) == 3 and cfg.nvar == 7
+    w = psgb.make_wind()
+    g = psgb.WindGrid(cfg)
+    assert g.ntot[:2] == [46, 26]
+    V = psgb.wind_state(cfg, w, g)
+    o = wind_oracle(40, 20, char_limiting=1, shock_flattening=1, entropy_switch=2)
+    assert o.ngh[:2] == [3, 3]
+    assert np.array_equal(V[:6], o.V[:6])
+    act = (slice(3, -3), slice(3, -3))
+    assert np.allclose(V[6, 0][act], o.V[6, 0][act], rtol=1e-15, atol=0)
+    fr, ft, fp = psgb.wind_flux(cfg, w, g)
+    ofr, oft, ofp = synthetic_flux(o.grid(0), o.grid(1), o.ntot, ngh=3)
+    assert np.array_equal(fr, ofr) and np.array_equal(ft, oft)

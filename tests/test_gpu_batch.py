@@ -105,8 +105,16 @@ def test_batch_ode_cooling_matches_individual_runs(built):
 
 
 def test_batch_rejects_mixed_models(built):
+    """Models of one batch share the kernels: cooling kind, limiting form
+    and variable count must agree."""
     import psgb
-    a = psgb.wind_model_solver(SPECS[0], cooling=1)
-    b = psgb.wind_model_solver(SPECS[1], cooling=0)
-    with pytest.raises(RuntimeError):
-        psgb.Batch([a, b])
+    for kw_a, kw_b in [(dict(cooling=1), dict(cooling=0)),
+                       (dict(cooling=1), dict(cooling=2)),
+                       (dict(char_limiting=1), dict()),
+                       (dict(entropy_switch=2), dict())]:
+        a = psgb.wind_model_solver(SPECS[0], **kw_a)
+        b = psgb.wind_model_solver(SPECS[1], **kw_b)
+        with pytest.raises(RuntimeError):
+            psgb.Batch([a, b])
+        a.close()
+        b.close()
