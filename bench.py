@@ -428,19 +428,19 @@ def gpu_bench(wl, steps, warmup, rank, world):
 
 def _batch_e2e(solvers, batch, V0s, steps):
     """Batch through the C ABI with host arrays: per step every model's
-    Data.Vc copied in from pinned host memory, one ps_batch_run step, every
-    model's Data.Vc copied back."""
+    Data.Vc copied in from pinned host memory (ps_batch_set_states), one
+    ps_batch_run step, every model's Data.Vc copied back
+    (ps_batch_get_states); wall time."""
     import torch
     host = [torch.from_numpy(v.copy()).pin_memory().numpy() for v in V0s]
     for s in solvers:
         s.restore()
+    batch.sync()
     t0 = time.perf_counter()
     for _ in range(steps):
-        for s, v in zip(solvers, host):
-            s.set_state(v)
+        batch.set_states(host)      # every model's Data.Vc in (ps_batch_set_states)
         batch.run(1)
-        for s, v in zip(solvers, host):
-            s.get_state(out=v)
+        batch.get_states(host)      # and out (ps_batch_get_states, synchronises)
     return time.perf_counter() - t0, int(sum(v.nbytes for v in V0s))
 
 

@@ -327,6 +327,12 @@ int  ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out);
 int  ps_batch_destroy(ps_batch *b);
 int  ps_batch_run(ps_batch *b, int nsteps);
 int  ps_batch_sync(ps_batch *b);      /* OR of every model's PS_F_* flags */
+/* Every model's Data.Vc to / from host arrays (Vc[m]: model m's
+ * [nv][k][j][i] array over its total box), the copies queued together on
+ * the batch's stream (get: then one synchronisation); the models' time
+ * state is kept.  For hosts that hand the states in and out between steps. */
+int  ps_batch_set_states(ps_batch *b, const double *const *Vc);
+int  ps_batch_get_states(ps_batch *b, double *const *Vc);
 int  ps_batch_set_stream(ps_batch *b, void *stream);
 long ps_batch_launch_count(const ps_batch *b);
 /* Tile shape of the stage kernels per model: 0 = 32x8, 1 = 16x16,

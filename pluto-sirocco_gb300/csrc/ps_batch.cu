@@ -674,6 +674,40 @@ extern "C" int ps_batch_run(ps_batch *b, int nsteps)
   return 0;
 }
 
+// Every model's Data.Vc from host arrays (Vc[m], [nv][k][j][i] over its
+// total box, pinned for the copies to overlap nothing but each other), all
+// copies queued on the batch's stream; the models' time state is kept.
+extern "C" int ps_batch_set_states(ps_batch *b, const double *const *Vc)
+{
+  if (!b || !Vc) return batch_fail("ps_batch_set_states: bad arguments");
+  for (int m = 0; m < b->n; m++) {
+    ps_ctx *c = b->ctx[m];
+    const ps::Params &p = c->p;
+    if (!Vc[m]) return batch_fail("ps_batch_set_states: null array");
+    BCK(cudaMemcpy2DAsync(c->V + p.xoff, (size_t)p.px * 8, Vc[m], (size_t)p.ntot[0] * 8,
+                          (size_t)p.ntot[0] * 8, (size_t)p.ntot[1] * p.ntot[2] * p.nvar,
+                          cudaMemcpyHostToDevice, b->stream));
+  }
+  return 0;
+}
+
+// Every model's Data.Vc into host arrays, queued on the batch's stream after
+// the work issued so far, then one synchronisation.
+extern "C" int ps_batch_get_states(ps_batch *b, double *const *Vc)
+{
+  if (!b || !Vc) return batch_fail("ps_batch_get_states: bad arguments");
+  for (int m = 0; m < b->n; m++) {
+    ps_ctx *c = b->ctx[m];
+    const ps::Params &p = c->p;
+    if (!Vc[m]) return batch_fail("ps_batch_get_states: null array");
+    BCK(cudaMemcpy2DAsync(Vc[m], (size_t)p.ntot[0] * 8, c->V + p.xoff, (size_t)p.px * 8,
+                          (size_t)p.ntot[0] * 8, (size_t)p.ntot[1] * p.ntot[2] * p.nvar,
+                          cudaMemcpyDeviceToHost, b->stream));
+  }
+  BCK(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
 extern "C" int ps_batch_sync(ps_batch *b)
 {
   if (!b) return PS_EINVAL;

@@ -36,7 +36,7 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect",
            "ps_set_cooling", "ps_write_dbl", "ps_read_dbl", "ps_read_sirocco_fluxes",
            "ps_read_sirocco_heatcool", "ps_read_sirocco_prefactors", "ps_set_sirocco",
-           "ps_read_m_uv_fit", "ps_set_mfit"]
+           "ps_read_m_uv_fit", "ps_set_mfit", "ps_batch_set_states", "ps_batch_get_states"]
 
 
 class Config(ctypes.Structure):
@@ -134,6 +134,8 @@ def lib():
         L.ps_batch_destroy.argtypes = [P]
         L.ps_batch_run.argtypes = [P, I]
         L.ps_batch_sync.argtypes = [P]
+        L.ps_batch_set_states.argtypes = [P, ctypes.POINTER(DP)]
+        L.ps_batch_get_states.argtypes = [P, ctypes.POINTER(DP)]
         L.ps_batch_set_stream.argtypes = [P, P]
         L.ps_batch_launch_count.argtypes = [P]
         L.ps_batch_launch_count.restype = ctypes.c_long
@@ -510,6 +512,19 @@ class Batch:
     def run(self, nsteps):
         check(lib().ps_batch_run(self.h, nsteps), "ps_batch_run")
         return self.sync()
+
+    def set_states(self, arrays):
+        """Every model's state from host arrays (one per model, each the
+        shape get_state() returns; pinned memory for full copy speed)."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in arrays]
+        self._state_refs = arrs
+        ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrs))(*[_dp(a) for a in arrs])
+        check(lib().ps_batch_set_states(self.h, ptrs), "ps_batch_set_states")
+
+    def get_states(self, arrays):
+        """Every model's state into the given host arrays (written in place)."""
+        ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrays))(*[_dp(a) for a in arrays])
+        check(lib().ps_batch_get_states(self.h, ptrs), "ps_batch_get_states")
 
     def sync(self):
         return check(lib().ps_batch_sync(self.h), "ps_batch_sync")

@@ -104,6 +104,35 @@ def test_batch_ode_cooling_matches_individual_runs(built):
     batch.close()
 
 
+def test_batch_state_transfer(built):
+    """ps_batch_set_states / ps_batch_get_states move every model's Data.Vc
+    in one queue: what they read equals each model's ps_get_state, and a
+    batch stepped from states handed in equals the models stepped alone
+    from the same states."""
+    import psgb
+    solo, inb = _pairs(1)
+    batch = psgb.Batch(inb)
+    batch.run(3)
+    host = [np.zeros_like(m.get_state()) for m in inb]
+    batch.get_states(host)
+    for m, h in zip(inb, host):
+        assert np.array_equal(h, m.get_state())
+    for s in solo:
+        s.run(3)
+    # hand in states changed on the host, then step both forms
+    for h in host:
+        h[4] *= 1.01                 # pressure
+    batch.set_states(host)
+    for s, h in zip(solo, host):
+        s.set_state(h)
+    flags = 0
+    for s in solo:
+        flags |= s.run(4)
+    assert batch.run(4) == flags
+    _check_equal(solo, inb)
+    batch.close()
+
+
 def test_batch_rejects_mixed_models(built):
     """Models of one batch share the kernels: cooling kind, limiting form
     and variable count must agree."""
