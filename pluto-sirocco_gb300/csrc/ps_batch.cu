@@ -684,9 +684,12 @@ extern "C" int ps_batch_set_states(ps_batch *b, const double *const *Vc)
     ps_ctx *c = b->ctx[m];
     const ps::Params &p = c->p;
     if (!Vc[m]) return batch_fail("ps_batch_set_states: null array");
-    BCK(cudaMemcpy2DAsync(c->V + p.xoff, (size_t)p.px * 8, Vc[m], (size_t)p.ntot[0] * 8,
-                          (size_t)p.ntot[0] * 8, (size_t)p.ntot[1] * p.ntot[2] * p.nvar,
-                          cudaMemcpyHostToDevice, b->stream));
+    const size_t rows = (size_t)p.ntot[1] * p.ntot[2] * p.nvar;
+    if (p.px == p.ntot[0] && p.xoff == 0)   // rows back to back: one linear copy
+      BCK(cudaMemcpyAsync(c->V, Vc[m], rows * p.ntot[0] * 8, cudaMemcpyHostToDevice, b->stream));
+    else
+      BCK(cudaMemcpy2DAsync(c->V + p.xoff, (size_t)p.px * 8, Vc[m], (size_t)p.ntot[0] * 8,
+                            (size_t)p.ntot[0] * 8, rows, cudaMemcpyHostToDevice, b->stream));
   }
   return 0;
 }
@@ -700,9 +703,12 @@ extern "C" int ps_batch_get_states(ps_batch *b, double *const *Vc)
     ps_ctx *c = b->ctx[m];
     const ps::Params &p = c->p;
     if (!Vc[m]) return batch_fail("ps_batch_get_states: null array");
-    BCK(cudaMemcpy2DAsync(Vc[m], (size_t)p.ntot[0] * 8, c->V + p.xoff, (size_t)p.px * 8,
-                          (size_t)p.ntot[0] * 8, (size_t)p.ntot[1] * p.ntot[2] * p.nvar,
-                          cudaMemcpyDeviceToHost, b->stream));
+    const size_t rows = (size_t)p.ntot[1] * p.ntot[2] * p.nvar;
+    if (p.px == p.ntot[0] && p.xoff == 0)
+      BCK(cudaMemcpyAsync(Vc[m], c->V, rows * p.ntot[0] * 8, cudaMemcpyDeviceToHost, b->stream));
+    else
+      BCK(cudaMemcpy2DAsync(Vc[m], (size_t)p.ntot[0] * 8, c->V + p.xoff, (size_t)p.px * 8,
+                            (size_t)p.ntot[0] * 8, rows, cudaMemcpyDeviceToHost, b->stream));
   }
   BCK(cudaStreamSynchronize(b->stream));
   return 0;
