@@ -674,12 +674,82 @@ extern "C" int ps_batch_run(ps_batch *b, int nsteps)
   return 0;
 }
 
+namespace ps {
+
+// Up to kCopyList arrays copied by one launch, blockIdx.y = array: the
+// state transfer between pinned host memory and the device when every host
+// array is device-accessible (GPU loads or stores over the host link, which
+// on this part run faster than the copy engines).
+constexpr int kCopyList = 128;
+struct CopyList {
+  const double *src[kCopyList];
+  double *dst[kCopyList];
+  long long count[kCopyList];
+};
+
+__global__ void __launch_bounds__(256) k_copy_list(const __grid_constant__ CopyList L)
+{
+  const int m = blockIdx.y;
+  const long long n = L.count[m], n2 = n / 2;
+  const double2 *s2 = reinterpret_cast<const double2 *>(L.src[m]);
+  double2 *d2 = reinterpret_cast<double2 *>(L.dst[m]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2;
+       i += (long long)gridDim.x * blockDim.x)
+    d2[i] = s2[i];
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) L.dst[m][n - 1] = L.src[m][n - 1];
+}
+
+}  // namespace ps
+
+// The device address of a pinned (page-locked or registered) host array, or
+// NULL when the array is not pinned or not 16-byte aligned.
+static const void *pinned_device_ptr(const void *h)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  if (reinterpret_cast<uintptr_t>(a.devicePointer) % 16 != 0) return nullptr;
+  return a.devicePointer;
+}
+
+// All models' arrays by the copy kernel when every host array is pinned and
+// every device state is one linear block; returns 1 when it did the copies.
+static int batch_copy_kernel(ps_batch *b, const double *const *host, bool to_device)
+{
+  for (int m = 0; m < b->n; m++) {
+    const ps::Params &p = b->ctx[m]->p;
+    if (p.px != p.ntot[0] || p.xoff != 0 || !pinned_device_ptr(host[m])) return 0;
+  }
+  for (int m0 = 0; m0 < b->n; m0 += ps::kCopyList) {
+    ps::CopyList L;
+    const int cnt = std::min(ps::kCopyList, b->n - m0);
+    for (int k = 0; k < cnt; k++) {
+      ps_ctx *c = b->ctx[m0 + k];
+      const double *h = static_cast<const double *>(pinned_device_ptr(host[m0 + k]));
+      L.count[k] = (long long)c->p.ntot[0] * c->p.ntot[1] * c->p.ntot[2] * c->p.nvar;
+      L.src[k] = to_device ? h : c->V;
+      L.dst[k] = to_device ? c->V : const_cast<double *>(h);
+    }
+    ps::k_copy_list<<<dim3(2 * (unsigned)b->num_sms, (unsigned)cnt), 256, 0, b->stream>>>(L);
+    b->launches++;
+  }
+  return cudaGetLastError() == cudaSuccess ? 1 : -1;
+}
+
 // Every model's Data.Vc from host arrays (Vc[m], [nv][k][j][i] over its
-// total box, pinned for the copies to overlap nothing but each other), all
-// copies queued on the batch's stream; the models' time state is kept.
+// total box, pinned for the full transfer speed), all copies queued on the
+// batch's stream; the models' time state is kept.
 extern "C" int ps_batch_set_states(ps_batch *b, const double *const *Vc)
 {
   if (!b || !Vc) return batch_fail("ps_batch_set_states: bad arguments");
+  for (int m = 0; m < b->n; m++)
+    if (!Vc[m]) return batch_fail("ps_batch_set_states: null array");
+  const int k = batch_copy_kernel(b, Vc, true);
+  if (k < 0) return batch_fail("ps_batch_set_states: copy kernel launch failed");
+  if (k) return 0;
   for (int m = 0; m < b->n; m++) {
     ps_ctx *c = b->ctx[m];
     const ps::Params &p = c->p;
@@ -699,6 +769,14 @@ extern "C" int ps_batch_set_states(ps_batch *b, const double *const *Vc)
 extern "C" int ps_batch_get_states(ps_batch *b, double *const *Vc)
 {
   if (!b || !Vc) return batch_fail("ps_batch_get_states: bad arguments");
+  for (int m = 0; m < b->n; m++)
+    if (!Vc[m]) return batch_fail("ps_batch_get_states: null array");
+  const int k = batch_copy_kernel(b, Vc, false);
+  if (k < 0) return batch_fail("ps_batch_get_states: copy kernel launch failed");
+  if (k) {
+    BCK(cudaStreamSynchronize(b->stream));
+    return 0;
+  }
   for (int m = 0; m < b->n; m++) {
     ps_ctx *c = b->ctx[m];
     const ps::Params &p = c->p;

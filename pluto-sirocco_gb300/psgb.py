@@ -517,12 +517,23 @@ class Batch:
         """Every model's state from host arrays (one per model, each the
         shape get_state() returns; pinned memory for full copy speed)."""
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in arrays]
+        self._check_states(arrs)
         self._state_refs = arrs
         ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrs))(*[_dp(a) for a in arrs])
         check(lib().ps_batch_set_states(self.h, ptrs), "ps_batch_set_states")
 
+    def _check_states(self, arrays):
+        if len(arrays) != len(self.solvers):
+            raise ValueError("one array per model")
+        for a, sv in zip(arrays, self.solvers):
+            g = sv.grid
+            want = sv.cfg.nvar * g.ntot[0] * g.ntot[1] * g.ntot[2]
+            if a.size != want or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("a state array does not match its model's [nv][k][j][i] box")
+
     def get_states(self, arrays):
         """Every model's state into the given host arrays (written in place)."""
+        self._check_states(arrays)
         ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrays))(*[_dp(a) for a in arrays])
         check(lib().ps_batch_get_states(self.h, ptrs), "ps_batch_get_states")
 

@@ -110,19 +110,23 @@ def test_batch_state_transfer(built):
     batch stepped from states handed in equals the models stepped alone
     from the same states."""
     import psgb
+    import torch
     solo, inb = _pairs(1)
     batch = psgb.Batch(inb)
     batch.run(3)
-    host = [np.zeros_like(m.get_state()) for m in inb]
+    host = [np.zeros_like(m.get_state()) for m in inb]   # pageable: the copy engines
     batch.get_states(host)
-    for m, h in zip(inb, host):
-        assert np.array_equal(h, m.get_state())
+    pinned = [torch.zeros(h.shape, dtype=torch.float64).pin_memory().numpy() for h in host]
+    batch.get_states(pinned)                             # pinned: the copy kernel
+    for m, h, q in zip(inb, host, pinned):
+        assert np.array_equal(h, m.get_state()) and np.array_equal(q, h)
     for s in solo:
         s.run(3)
     # hand in states changed on the host, then step both forms
-    for h in host:
+    for h, q in zip(host, pinned):
         h[4] *= 1.01                 # pressure
-    batch.set_states(host)
+        q[...] = h
+    batch.set_states(pinned)
     for s, h in zip(solo, host):
         s.set_state(h)
     flags = 0
