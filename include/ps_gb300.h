@@ -333,6 +333,12 @@ int  ps_batch_sync(ps_batch *b);      /* OR of every model's PS_F_* flags */
  * state is kept.  For hosts that hand the states in and out between steps. */
 int  ps_batch_set_states(ps_batch *b, const double *const *Vc);
 int  ps_batch_get_states(ps_batch *b, double *const *Vc);
+/* The same transfers by the copy engines only, queued without waiting:
+ * two batches on their own streams then overlap one batch's transfers with
+ * the other's steps.  The host arrays (pinned) are in use until
+ * ps_batch_sync returns. */
+int  ps_batch_set_states_async(ps_batch *b, const double *const *Vc);
+int  ps_batch_get_states_async(ps_batch *b, double *const *Vc);
 int  ps_batch_set_stream(ps_batch *b, void *stream);
 long ps_batch_launch_count(const ps_batch *b);
 /* Tile shape of the stage kernels per model: 0 = 32x8, 1 = 16x16,

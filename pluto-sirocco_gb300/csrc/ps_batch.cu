@@ -739,57 +739,80 @@ static int batch_copy_kernel(ps_batch *b, const double *const *host, bool to_dev
   return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 
+// Every model's Data.Vc between the host arrays and the device by the copy
+// engines, queued on the batch's stream: one linear copy per model when its
+// rows lie back to back, else a 2-D copy.
+static int batch_copy_engines(ps_batch *b, const double *const *host, bool to_device)
+{
+  for (int m = 0; m < b->n; m++) {
+    ps_ctx *c = b->ctx[m];
+    const ps::Params &p = c->p;
+    const size_t rows = (size_t)p.ntot[1] * p.ntot[2] * p.nvar;
+    double *h = const_cast<double *>(host[m]);
+    cudaError_t e;
+    if (p.px == p.ntot[0] && p.xoff == 0)
+      e = to_device ? cudaMemcpyAsync(c->V, h, rows * p.ntot[0] * 8, cudaMemcpyHostToDevice,
+                                      b->stream)
+                    : cudaMemcpyAsync(h, c->V, rows * p.ntot[0] * 8, cudaMemcpyDeviceToHost,
+                                      b->stream);
+    else
+      e = to_device
+              ? cudaMemcpy2DAsync(c->V + p.xoff, (size_t)p.px * 8, h, (size_t)p.ntot[0] * 8,
+                                  (size_t)p.ntot[0] * 8, rows, cudaMemcpyHostToDevice, b->stream)
+              : cudaMemcpy2DAsync(h, (size_t)p.ntot[0] * 8, c->V + p.xoff, (size_t)p.px * 8,
+                                  (size_t)p.ntot[0] * 8, rows, cudaMemcpyDeviceToHost, b->stream);
+    if (e != cudaSuccess) return batch_cuda(e, to_device ? "ps_batch: state in" : "ps_batch: state out");
+  }
+  return 0;
+}
+
+static int batch_check_host(const ps_batch *b, const void *arr, const char *what)
+{
+  if (!b || !arr) return batch_fail(what);
+  const double *const *h = static_cast<const double *const *>(arr);
+  for (int m = 0; m < b->n; m++)
+    if (!h[m]) return batch_fail(what);
+  return 0;
+}
+
 // Every model's Data.Vc from host arrays (Vc[m], [nv][k][j][i] over its
 // total box, pinned for the full transfer speed), all copies queued on the
 // batch's stream; the models' time state is kept.
 extern "C" int ps_batch_set_states(ps_batch *b, const double *const *Vc)
 {
-  if (!b || !Vc) return batch_fail("ps_batch_set_states: bad arguments");
-  for (int m = 0; m < b->n; m++)
-    if (!Vc[m]) return batch_fail("ps_batch_set_states: null array");
+  if (int r = batch_check_host(b, Vc, "ps_batch_set_states: bad arguments")) return r;
   const int k = batch_copy_kernel(b, Vc, true);
   if (k < 0) return batch_fail("ps_batch_set_states: copy kernel launch failed");
-  if (k) return 0;
-  for (int m = 0; m < b->n; m++) {
-    ps_ctx *c = b->ctx[m];
-    const ps::Params &p = c->p;
-    if (!Vc[m]) return batch_fail("ps_batch_set_states: null array");
-    const size_t rows = (size_t)p.ntot[1] * p.ntot[2] * p.nvar;
-    if (p.px == p.ntot[0] && p.xoff == 0)   // rows back to back: one linear copy
-      BCK(cudaMemcpyAsync(c->V, Vc[m], rows * p.ntot[0] * 8, cudaMemcpyHostToDevice, b->stream));
-    else
-      BCK(cudaMemcpy2DAsync(c->V + p.xoff, (size_t)p.px * 8, Vc[m], (size_t)p.ntot[0] * 8,
-                            (size_t)p.ntot[0] * 8, rows, cudaMemcpyHostToDevice, b->stream));
-  }
-  return 0;
+  return k ? 0 : batch_copy_engines(b, Vc, true);
 }
 
 // Every model's Data.Vc into host arrays, queued on the batch's stream after
 // the work issued so far, then one synchronisation.
 extern "C" int ps_batch_get_states(ps_batch *b, double *const *Vc)
 {
-  if (!b || !Vc) return batch_fail("ps_batch_get_states: bad arguments");
-  for (int m = 0; m < b->n; m++)
-    if (!Vc[m]) return batch_fail("ps_batch_get_states: null array");
+  if (int r = batch_check_host(b, Vc, "ps_batch_get_states: bad arguments")) return r;
   const int k = batch_copy_kernel(b, Vc, false);
   if (k < 0) return batch_fail("ps_batch_get_states: copy kernel launch failed");
-  if (k) {
-    BCK(cudaStreamSynchronize(b->stream));
-    return 0;
-  }
-  for (int m = 0; m < b->n; m++) {
-    ps_ctx *c = b->ctx[m];
-    const ps::Params &p = c->p;
-    if (!Vc[m]) return batch_fail("ps_batch_get_states: null array");
-    const size_t rows = (size_t)p.ntot[1] * p.ntot[2] * p.nvar;
-    if (p.px == p.ntot[0] && p.xoff == 0)
-      BCK(cudaMemcpyAsync(Vc[m], c->V, rows * p.ntot[0] * 8, cudaMemcpyDeviceToHost, b->stream));
-    else
-      BCK(cudaMemcpy2DAsync(Vc[m], (size_t)p.ntot[0] * 8, c->V + p.xoff, (size_t)p.px * 8,
-                            (size_t)p.ntot[0] * 8, rows, cudaMemcpyDeviceToHost, b->stream));
-  }
+  if (!k)
+    if (int r = batch_copy_engines(b, Vc, false)) return r;
   BCK(cudaStreamSynchronize(b->stream));
   return 0;
+}
+
+// The same transfers by the copy engines only, queued without waiting, so
+// that the copies of one batch overlap the steps of another batch on the
+// GPU's multiprocessors; the host arrays (pinned) stay untouched until
+// ps_batch_sync returns.
+extern "C" int ps_batch_set_states_async(ps_batch *b, const double *const *Vc)
+{
+  if (int r = batch_check_host(b, Vc, "ps_batch_set_states_async: bad arguments")) return r;
+  return batch_copy_engines(b, Vc, true);
+}
+
+extern "C" int ps_batch_get_states_async(ps_batch *b, double *const *Vc)
+{
+  if (int r = batch_check_host(b, Vc, "ps_batch_get_states_async: bad arguments")) return r;
+  return batch_copy_engines(b, Vc, false);
 }
 
 extern "C" int ps_batch_sync(ps_batch *b)

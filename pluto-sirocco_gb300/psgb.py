@@ -36,7 +36,8 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect",
            "ps_set_cooling", "ps_write_dbl", "ps_read_dbl", "ps_read_sirocco_fluxes",
            "ps_read_sirocco_heatcool", "ps_read_sirocco_prefactors", "ps_set_sirocco",
-           "ps_read_m_uv_fit", "ps_set_mfit", "ps_batch_set_states", "ps_batch_get_states"]
+           "ps_read_m_uv_fit", "ps_set_mfit", "ps_batch_set_states", "ps_batch_get_states",
+           "ps_batch_set_states_async", "ps_batch_get_states_async"]
 
 
 class Config(ctypes.Structure):
@@ -136,6 +137,8 @@ def lib():
         L.ps_batch_sync.argtypes = [P]
         L.ps_batch_set_states.argtypes = [P, ctypes.POINTER(DP)]
         L.ps_batch_get_states.argtypes = [P, ctypes.POINTER(DP)]
+        L.ps_batch_set_states_async.argtypes = [P, ctypes.POINTER(DP)]
+        L.ps_batch_get_states_async.argtypes = [P, ctypes.POINTER(DP)]
         L.ps_batch_set_stream.argtypes = [P, P]
         L.ps_batch_launch_count.argtypes = [P]
         L.ps_batch_launch_count.restype = ctypes.c_long
@@ -509,9 +512,26 @@ class Batch:
         except Exception:
             pass
 
-    def run(self, nsteps):
+    def run(self, nsteps, wait=True):
+        """nsteps steps of every model; wait=False only queues them (sync()
+        then returns the flags)."""
         check(lib().ps_batch_run(self.h, nsteps), "ps_batch_run")
-        return self.sync()
+        return self.sync() if wait else 0
+
+    def set_states_async(self, arrays):
+        """set_states by the copy engines, queued without waiting (the
+        arrays, pinned, are in use until sync())."""
+        self._check_states(arrays)
+        self._state_refs = list(arrays)
+        ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrays))(*[_dp(a) for a in arrays])
+        check(lib().ps_batch_set_states_async(self.h, ptrs), "ps_batch_set_states_async")
+
+    def get_states_async(self, arrays):
+        """get_states by the copy engines, queued without waiting."""
+        self._check_states(arrays)
+        self._out_refs = list(arrays)
+        ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrays))(*[_dp(a) for a in arrays])
+        check(lib().ps_batch_get_states_async(self.h, ptrs), "ps_batch_get_states_async")
 
     def set_states(self, arrays):
         """Every model's state from host arrays (one per model, each the

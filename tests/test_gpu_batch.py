@@ -137,6 +137,37 @@ def test_batch_state_transfer(built):
     batch.close()
 
 
+def test_batch_overlapped_halves(built):
+    """Two batches on their own streams, each step handed in and out through
+    pinned host arrays by the queued copy-engine transfers
+    (ps_batch_set_states_async / ps_batch_get_states_async) while the other
+    batch steps: the same states as the models stepped alone."""
+    import psgb
+    import torch
+    solo, inb = _pairs(1)
+    parts = [psgb.Batch(inb[:1]), psgb.Batch(inb[1:])]
+    hosts = [[torch.from_numpy(m.get_state()).pin_memory().numpy() for m in p.solvers]
+             for p in parts]
+    for step in range(6):
+        for p, h in zip(parts, hosts):
+            p.sync()                   # this part's previous result is on the host
+            p.set_states_async(h)
+            p.run(1, wait=False)
+            p.get_states_async(h)
+    flags = 0
+    for p in parts:
+        flags |= p.sync()
+    solo_flags = 0
+    for s in solo:
+        solo_flags |= s.run(6)
+    assert flags == solo_flags
+    _check_equal(solo, inb)
+    for m, h in zip(inb, hosts[0] + hosts[1]):
+        assert np.array_equal(h, m.get_state())
+    for p in parts:
+        p.close()
+
+
 def test_batch_rejects_mixed_models(built):
     """Models of one batch share the kernels: cooling kind, limiting form
     and variable count must agree."""
