@@ -858,6 +858,13 @@ def _rooflines(out, wl, stage_ms, per_kernel):
         ach = ops * wl.cells / (stage_ms * 1e-3)
         out["roofline_fp64"].update({"achieved": ach / 1e9, "frac": ach / fp64,
                                      "ops_per_cell_stage": ops})
+    insts = _profile_value(wl, "fp64_insts_per_cell_stage")
+    if fp64 > 0 and insts:
+        # DADD, DMUL and DFMA take one issue slot each: the share of the
+        # FMA instruction rate they fill
+        out["roofline_fp64"].update({
+            "insts_per_cell_stage": insts,
+            "issue_frac": insts * wl.cells / (stage_ms * 1e-3) / (fp64 / 2)})
 
 
 def reference_bench(wl, steps, warmup, rank, world):

@@ -206,3 +206,27 @@ def test_batch_with_surrogate_matches_individual(trained):
     for a, b in zip(solo, inb):
         assert np.array_equal(a.get_state(), b.get_state())
     batch.close()
+
+
+@pytest.mark.parametrize("grid", [(64, 32), (128, 64)])
+def test_fallback_equals_reference_method(built, grid):
+    """Every cell outside the surrogate's box goes to the fallback, which
+    must give the reference method's state bit for bit, alone and in a
+    batch: a queue that fits the first warp of every multiprocessor (64x32:
+    2048 cells) and one that spills into the others (128x64: 8192 cells)."""
+    import psgb
+    spec = dict(grid=grid, l_star=1e37, krad=0.2, alpharad=-0.6)
+    sg = psgb.Surrogate((40.0,) * 4, (41.0,) * 4)     # a box no cell is in
+    plain, fast, inb = (psgb.wind_model_solver(spec) for _ in range(3))
+    psgb.lib().ps_set_surrogate(fast.ctx, sg.h, 1)
+    batch = psgb.Batch([inb])
+    psgb.lib().ps_batch_set_surrogate(batch.h, sg.h, 1)
+    sg.stats(reset=True)
+    for chunk in (1, 4):
+        fa, fb, fc = plain.run(chunk), fast.run(chunk), batch.run(chunk)
+        assert fa == fb == fc
+        assert np.array_equal(plain.get_state(), fast.get_state())
+        assert np.array_equal(plain.get_state(), inb.get_state())
+    acc, oob, rej, below, evals, stiff = sg.stats()
+    assert acc == 0 and oob > 0
+    batch.close()
