@@ -43,6 +43,28 @@ __device__ __forceinline__ bool is_nan_bits(double x)
   return (b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
 }
 
+// Sign tests and the maximum of two non-negative values on the bit pattern,
+// in the integer units: the FP64 pipe, at two lanes per cycle and
+// multiprocessor, is what bounds the stage kernels.  Equal to x > 0, x < 0
+// and dmax for every value but NaN (a NaN state is flagged before it is
+// used).
+__device__ __forceinline__ bool gt0(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool lt0(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) > 0x8000000000000000ull;
+}
+__device__ __forceinline__ double nn_max(double a, double b)
+{
+  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  return __longlong_as_double(x >= y ? x : y);
+}
+// DBL_MIN <= x <= DBL_MAX
+__device__ __forceinline__ bool normal_pos(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) - 0x0010000000000000ull <
+         0x7FE0000000000000ull;
+}
+
 // Limited slope on a uniform Cartesian grid (cp = cm = 2, d = 1/2).
 template <int LIM>
 __device__ __forceinline__ double limited_slope(double dvp, double dvm)
@@ -155,16 +177,16 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
   const double aL = gpL * rsqrt(gpL * vL[RHO]), aR = gpR * rsqrt(gpR * vR[RHO]);
   const double SL = dmin(vL[VN] - aL, vR[VN] - aR);
   const double SR = dmax(vL[VN] + aL, vR[VN] + aR);
-  cmax = dmax(fabs(SL), fabs(SR));
+  cmax = nn_max(fabs(SL), fabs(SR));
 
-  if (SL > 0.0) {
+  if (gt0(SL)) {
     f[RHO] = uL[VN];
     f[VX1] = uL[VX1] * vL[VN];
     f[VX2] = uL[VX2] * vL[VN];
     f[VX3] = uL[VX3] * vL[VN];
     f[PRS] = (uL[PRS] + vL[PRS]) * vL[VN];
     pr = vL[PRS];
-  } else if (SR < 0.0) {
+  } else if (lt0(SR)) {
     f[RHO] = uR[VN];
     f[VX1] = uR[VX1] * vR[VN];
     f[VX2] = uR[VX2] * vR[VN];

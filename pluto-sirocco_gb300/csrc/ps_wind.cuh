@@ -48,8 +48,8 @@ struct LineList {
   // point (c2a, c2b)
   const double *c1a, *c1b, *c2a, *c2b;
   const double *inv_ds;  // 1 / ds; 0 for a bin without direction (dv/ds = -999)
-  double *lq;            // per entry and stage: -alpharad * log(dv/ds) (power law;
-                         // -inf if dv/ds <= 0), for cells with two or more
+  double *lq;            // per entry and stage: (dv/ds)^-2 (power law, one bin;
+                         // 0 if dv/ds <= 0), for cells with two or more
                          // bins exp(lf_a0 - alpharad log(dv/ds)) (0 if dv/ds <= 0),
                          // or -log10(dv/ds) (table, -inf if dv/ds <= 0)
   // tabulated force multiplier (KRAD = ALPHARAD = 999): log10 t at the

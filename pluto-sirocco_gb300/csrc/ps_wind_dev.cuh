@@ -81,13 +81,13 @@ __device__ __forceinline__ void vl_slopes(const double (&dvp)[N], const double (
 #pragma unroll
   for (int k = 0; k < N; k++) {
     const double pm = dvp[k] * dvm[k];
-    const bool on = pm > 0.0;
+    const bool on = gt0(pm);
     num[k] = on ? pm * (cp * dvm[k] + cm * dvp[k]) : 0.0;
     den[k] = on ? dvp[k] * dvp[k] + dvm[k] * dvm[k] + c2 * pm : 1.0;
     pre[k] = prod;
     prod *= den[k];
   }
-  if (prod >= 2.2250738585072014e-308 && prod <= 1.7976931348623157e308) {
+  if (normal_pos(prod)) {
     double r = 1.0 / prod;
 #pragma unroll
     for (int k = N - 1; k >= 0; k--) {
@@ -540,10 +540,16 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
     }
     return g * w.lf_cf;
   }
-  const double base = w.lf_a0 + 0.5 * w.alpharad * log(vg[RHO] * vg[PRS]);
+  // one bin: M = exp(lf_a0 + alpharad/2 log(rho p) - alpharad log(dv/ds))
+  // with the two logarithms as one, of rho p (dv/ds)^-2
+  const double rp = vg[RHO] * vg[PRS];
   for (int e = e0; e < e1; e++) {
-    double M = exp(base + L.lq[e]);
-    if (M > 4400.) M = 4400.;
+    const double q = L.lq[e];
+    double M = 0.0;
+    if (gt0(q)) {
+      M = exp(w.lf_a0 + 0.5 * w.alpharad * log(rp * q));
+      if (M > 4400.) M = 4400.;
+    }
     const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
     g += (1.0 + M) * F;
   }
@@ -853,7 +859,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       const bool fact = e1 - e0 >= 2;
       for (int e = e0; e < e1; e++) {
         const double ids = A.L.inv_ds[e];
-        double lq = (fact && !A.w.mfit) ? 0.0 : -INFINITY;
+        double lq = A.w.mfit ? -INFINITY : 0.0;
         if (ids != 0.0) {
           double ans2[2];
           bilinear_w(A.L.fr1[e], A.L.fr2[e], v11, v12, v21, v22, ans2);
@@ -864,7 +870,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
           if (dvds > 0.0)
             lq = A.w.mfit ? -log10(dvds)
                  : fact   ? exp(A.w.lf_a0 - alpha * log(dvds))
-                          : -alpha * log(dvds);
+                          : 1.0 / (dvds * dvds);
         }
         A.L.lq[e] = lq;
       }
