@@ -43,20 +43,32 @@ __device__ __forceinline__ bool is_nan_bits(double x)
   return (b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
 }
 
-// Sign tests and the maximum of two non-negative values on the bit pattern,
-// in the integer units: the FP64 pipe, at two lanes per cycle and
-// multiprocessor, is what bounds the stage kernels.  Equal to x > 0, x < 0
-// and dmax for every value but NaN (a NaN state is flagged before it is
-// used).
-__device__ __forceinline__ bool gt0(double x) { return __double_as_longlong(x) > 0; }
+// Comparisons on the bit pattern, in the integer units: the FP64 pipe, at
+// two lanes per cycle and multiprocessor, is what bounds the stage kernels.
+// Each equals its floating-point form for every value, NaN and signed zeros
+// included: x > 0 (the patterns of +min_subnormal..+inf), x < 0 (those of
+// -min_subnormal..-inf), x > c for a positive finite constant c, and
+// a >= b ? a : b for a, b with the sign bit clear.
+__device__ __forceinline__ bool gt0(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) - 1ull < 0x7FF0000000000000ull;
+}
 __device__ __forceinline__ bool lt0(double x)
 {
-  return (unsigned long long)__double_as_longlong(x) > 0x8000000000000000ull;
+  return (unsigned long long)__double_as_longlong(x) - 0x8000000000000001ull <
+         0x7FF0000000000000ull;
+}
+template <unsigned long long CBITS>
+__device__ __forceinline__ bool gt_pos(double x)
+{
+  static_assert(CBITS > 0 && CBITS < 0x7FF0000000000000ull, "positive finite constant");
+  return (unsigned long long)__double_as_longlong(x) - (CBITS + 1ull) <
+         0x7FF0000000000000ull - CBITS;
 }
 __device__ __forceinline__ double nn_max(double a, double b)
 {
-  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
-  return __longlong_as_double(x >= y ? x : y);
+  const unsigned long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  return (x >= y && x <= 0x7FF0000000000000ull) ? a : b;
 }
 // DBL_MIN <= x <= DBL_MAX
 __device__ __forceinline__ bool normal_pos(double x)
@@ -71,15 +83,15 @@ __device__ __forceinline__ double limited_slope(double dvp, double dvm)
 {
   if constexpr (LIM == LIM_MC) {
     double dv = 0.0;
-    if (dvp * dvm > 0.0) {
+    if (gt0(dvp * dvm)) {
       double qc = 0.5 * (dvm + dvp), scrh = 2.0 * abs_min(dvp, dvm);
       dv = abs_min(qc, scrh);
     }
     return dv;
   } else if constexpr (LIM == LIM_VL) {
-    return dvp * dvm > 0.0 ? 2.0 * dvp * dvm / (dvp + dvm) : 0.0;
+    return gt0(dvp * dvm) ? 2.0 * dvp * dvm / (dvp + dvm) : 0.0;
   } else {
-    return dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0;
+    return gt0(dvp * dvm) ? abs_min(dvp, dvm) : 0.0;
   }
 }
 
@@ -116,7 +128,7 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
   // (Src/HD/mappers.c:185-221)
   unsigned flag = 0;
   const double m2 = u[VX1] * u[VX1] + u[VX2] * u[VX2] + u[VX3] * u[VX3];
-  if (u[RHO] < 0.0) {
+  if (lt0(u[RHO])) {
     u[RHO] = kSmallDensity;
     flag |= F_CONS2PRIM | F_NEG_DENSITY;
   }
@@ -126,7 +138,7 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
   v[VX2] = u[VX2] * tau;
   v[VX3] = u[VX3] * tau;
   const double kin = 0.5 * m2 * tau;
-  if (u[PRS] < 0.0) {
+  if (lt0(u[PRS])) {
     u[PRS] = kSmallPressure / gmm1 + kin;
     flag |= F_CONS2PRIM;
   }
@@ -134,7 +146,7 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
     if (ent == 2) {
       const double rhog1 = rho_pow(u[RHO], gmm1);
       v[PRS] = u[NV - 1] * rhog1;
-      if (v[PRS] < 0.0) {
+      if (lt0(v[PRS])) {
         v[PRS] = kSmallPressure;
         flag |= F_CONS2PRIM;
       }
@@ -143,7 +155,7 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
   }
   if (ent != 2) {
     v[PRS] = gmm1 * (u[PRS] - kin);
-    if (v[PRS] < 0.0) {
+    if (lt0(v[PRS])) {
       v[PRS] = kSmallPressure;
       u[PRS] = v[PRS] / gmm1 + kin;
       flag |= F_CONS2PRIM;
@@ -246,7 +258,7 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
     pr = v[PRS];
   }
   if constexpr (NV > NFLX) {
-    const bool up = f[RHO] > 0.0;
+    const bool up = gt0(f[RHO]);
 #pragma unroll
     for (int nv = NFLX; nv < NV; nv++) f[nv] = f[RHO] * (up ? vL[nv] : vR[nv]);
   }

@@ -50,17 +50,17 @@ __device__ __forceinline__ double limited_slope_general(double dvp, double dvm, 
 {
   if constexpr (LIM == LIM_MC) {
     double dv = 0.0;
-    if (dvp * dvm > 0.0) {
+    if (gt0(dvp * dvm)) {
       double qc = 0.5 * (dvm + dvp), scrh = abs_min(dvp * cp, dvm * cm);
       dv = abs_min(qc, scrh);
     }
     return dv;
   } else if constexpr (LIM == LIM_VL) {
-    return dvp * dvm > 0.0 ? dvp * dvm * (cp * dvm + cm * dvp) /
+    return gt0(dvp * dvm) ? dvp * dvm * (cp * dvm + cm * dvp) /
                                  (dvp * dvp + dvm * dvm + (cp + cm - 2.0) * dvp * dvm)
                            : 0.0;
   } else {
-    return dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0;
+    return gt0(dvp * dvm) ? abs_min(dvp, dvm) : 0.0;
   }
 }
 
@@ -135,7 +135,7 @@ __device__ __forceinline__ void char_slopes(const double (&v)[NV], const double 
   wp[4] = dvp[vb];
   if (minmod) {   // FLAG_MINMOD
 #pragma unroll
-    for (int k = 0; k < 5; k++) wl[k] = wp[k] * wm[k] > 0.0 ? abs_min(wp[k], wm[k]) : 0.0;
+    for (int k = 0; k < 5; k++) wl[k] = gt0(wp[k] * wm[k]) ? abs_min(wp[k], wm[k]) : 0.0;
   } else {
 #pragma unroll
     for (int k = 0; k < 5; k++) wl[k] = limited_slope_general<LIM>(wp[k], wm[k], cp, cm);
@@ -150,9 +150,9 @@ __device__ __forceinline__ void char_slopes(const double (&v)[NV], const double 
   dc[vb] = 0.0 + wl[4] * 1.0;
 #pragma unroll
   for (int nv = 0; nv < 5; nv++) {
-    if (dvp[nv] * dvm[nv] > 0.0) {
+    if (gt0(dvp[nv] * dvm[nv])) {
       const double d2v = abs_min(cp * dvp[nv], cm * dvm[nv]);
-      dv[nv] = d2v * dc[nv] > 0.0 ? (fabs(d2v) < fabs(dc[nv]) ? d2v : dc[nv]) : 0.0;
+      dv[nv] = gt0(d2v * dc[nv]) ? (fabs(d2v) < fabs(dc[nv]) ? d2v : dc[nv]) : 0.0;
     } else {
       dv[nv] = 0.0;
     }
@@ -488,6 +488,8 @@ __device__ __forceinline__ void bilinear_w(double fx, double fy, const double (&
 // stage in VGradCalc (one log and one exp per call).  With KRAD = ALPHARAD
 // = 999, M is interpolated in the cell's table at log10 t = lt0 +
 // log10(rho p)/2 + lq, lq = -log10(dv/ds).
+constexpr unsigned long long kM4400 = 0x40B1300000000000ull;   // 4400.0
+
 template <int NV>
 __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineList &L,
                                              const WindParams &w, int e0, int e1, int comp,
@@ -517,7 +519,7 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
         }
         M = exp10(y);
         if (is_nan_bits(M)) M = 0.0;
-        if (M > 4400.) M = 4400.;
+        if (gt_pos<kM4400>(M)) M = 4400.;
       }
       const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
       g += (1.0 + M) * F;
@@ -531,9 +533,9 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
     for (int e = e0; e < e1; e++) {
       const double B = L.lq[e];
       double M = 0.0;
-      if (B > 0.0) {
+      if (gt0(B)) {
         M = Q * B;
-        if (M > 4400.) M = 4400.;
+        if (gt_pos<kM4400>(M)) M = 4400.;
       }
       const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
       g += (1.0 + M) * F;
@@ -548,7 +550,7 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
     double M = 0.0;
     if (gt0(q)) {
       M = exp(w.lf_a0 + 0.5 * w.alpharad * log(rp * q));
-      if (M > 4400.) M = 4400.;
+      if (gt_pos<kM4400>(M)) M = 4400.;
     }
     const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
     g += (1.0 + M) * F;
@@ -619,7 +621,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
         const double vm1 = sv[nv * G::VS + s0 - SST], v0 = sv[nv * G::VS + s0],
                      vp1 = sv[nv * G::VS + s0 + SST];
         const double dvp = (vp1 - v0) * wp, dvm = (v0 - vm1) * wm;
-        const double dv = dvp * dvm > 0.0 ? abs_min(dvp, dvm) : 0.0;
+        const double dv = gt0(dvp * dvm) ? abs_min(dvp, dvm) : 0.0;
         svp[nv * G::NPMAX + q] = v0 + dv * dp;
         svm[nv * G::NPMAX + q] = v0 - dv * dm;
       }
@@ -867,7 +869,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
           const double v2 = ans2[0] * A.L.c2a[e] + ans2[1] * A.L.c2b[e];
           const double dvds = fabs(v2 - v1) * ids;
           if (is_nan_bits(dvds)) flags |= F_NAN;
-          if (dvds > 0.0)
+          if (gt0(dvds))
             lq = A.w.mfit ? -log10(dvds)
                  : fact   ? exp(A.w.lf_a0 - alpha * log(dvds))
                           : 1.0 / (dvds * dvds);
