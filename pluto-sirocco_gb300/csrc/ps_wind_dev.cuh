@@ -813,6 +813,24 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
     __syncthreads();
   }
 
+  // VGradCalc's corner velocities (line_connect.c:637-660: the mean of the
+  // four zones that meet at a zone corner), formed once per corner of the
+  // tile for the four zones that share it; kept in the flux buffer, which
+  // the sweeps write only after their PLM pass
+  constexpr int CX = TL::X + 1, CY = TL::Y + 1;
+  static_assert(2 * CX * CY <= NV * G::NFMAX, "corner velocities fit the flux buffer");
+  const double *cv1 = sf, *cv2 = sf + CX * CY;
+  if (A.w.line_force) {
+    const double *V1 = sv + VX1 * G::VS, *V2 = sv + VX2 * G::VS;
+    for (int k = tid; k < CX * CY; k += G::NT) {
+      const int kx = k % CX, ky = k / CX;
+      const int s = (ky + TL::HY) * G::SX + kx + TL::HX, sm = s - G::SX;
+      sf[k] = (V1[sm - 1] + V1[sm] + V1[s - 1] + V1[s]) / 4.0;
+      sf[CX * CY + k] = (V2[sm - 1] + V2[sm] + V2[s - 1] + V2[s]) / 4.0;
+    }
+    __syncthreads();
+  }
+
   const int cx = tid % TL::X, cy = tid / TL::X;
   const bool own = tid < G::NC && (ox + cx < p.nx[0]) && (oy + cy < p.nx[1]);
   const int gi = p.beg[0] + ox + cx, gj = p.beg[1] + oy + cy;
@@ -841,18 +859,17 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       const int dc = (oy + cy) * p.nx[0] + (ox + cx);
       e0 = A.L.off[dc];
       e1 = A.L.off[dc + 1];
-      const int sc0 = (cy + TL::HY) * G::SX + cx + TL::HX;
-      const double *V1 = sv + VX1 * G::VS, *V2 = sv + VX2 * G::VS;
-      const int jm = sc0 - G::SX, jp = sc0 + G::SX;
+      // the corners (i-1/2, j-1/2), (i-1/2, j+1/2), (i+1/2, j+1/2), (i+1/2, j-1/2)
+      const int k0 = cy * CX + cx;
       double v11[2], v12[2], v21[2], v22[2], ans1[2];
-      v11[0] = (V1[jm - 1] + V1[jm] + V1[sc0 - 1] + V1[sc0]) / 4.0;
-      v11[1] = (V2[jm - 1] + V2[jm] + V2[sc0 - 1] + V2[sc0]) / 4.0;
-      v12[0] = (V1[jp - 1] + V1[sc0 - 1] + V1[jp] + V1[sc0]) / 4.0;
-      v12[1] = (V2[jp - 1] + V2[sc0 - 1] + V2[jp] + V2[sc0]) / 4.0;
-      v22[0] = (V1[jp] + V1[jp + 1] + V1[sc0 + 1] + V1[sc0]) / 4.0;
-      v22[1] = (V2[jp] + V2[jp + 1] + V2[sc0 + 1] + V2[sc0]) / 4.0;
-      v21[0] = (V1[sc0 + 1] + V1[jm + 1] + V1[jm] + V1[sc0]) / 4.0;
-      v21[1] = (V2[sc0 + 1] + V2[jm + 1] + V2[jm] + V2[sc0]) / 4.0;
+      v11[0] = cv1[k0];
+      v11[1] = cv2[k0];
+      v12[0] = cv1[k0 + CX];
+      v12[1] = cv2[k0 + CX];
+      v22[0] = cv1[k0 + CX + 1];
+      v22[1] = cv2[k0 + CX + 1];
+      v21[0] = cv1[k0 + 1];
+      v21[1] = cv2[k0 + 1];
       bilinear_w(g.fx[gi], g.fy[gj], v11, v12, v21, v22, ans1);
       const double alpha = A.w.alpharad;
       // two or more bins: the bin's factor k C^alpha (dv/ds)^-alpha is kept
