@@ -481,11 +481,11 @@ __device__ __forceinline__ void bilinear_w(double fx, double fy, const double (&
 // LineForce component `comp` (0: r, 1: theta) for the state vg of one cell
 // (line_connect.c:815-903): sum over the cell's bins of
 // (1 + M) sigma_e F / c, M = min(krad t^alpharad, 4400), t = sigma_e rho
-// v_th / (dv/ds), M = 0 where dv/ds <= 0.  Evaluated as
-// M = exp(lf_a0 + alpharad/2 log(rho p) + lq) with lq = -alpharad log(dv/ds)
-// from VGradCalc (one log per call, one exp per bin); for cells with two or
-// more bins as M = (rho p)^(alpharad/2) B, B = exp(lf_a0 + lq) formed once per
-// stage in VGradCalc (one log and one exp per call).  With KRAD = ALPHARAD
+// v_th / (dv/ds), M = 0 where dv/ds <= 0.  Evaluated for a cell with one
+// bin as M = exp(lf_a0 + alpharad/2 log(rho p lq)) with lq = (dv/ds)^-2 from
+// VGradCalc (one log and one exp per call); for cells with two or more bins
+// as M = (rho p)^(alpharad/2) B, B = exp(lf_a0 - alpharad log(dv/ds)) formed
+// once per stage in VGradCalc (one log and one exp per call).  With KRAD = ALPHARAD
 // = 999, M is interpolated in the cell's table at log10 t = lt0 +
 // log10(rho p)/2 + lq, lq = -log10(dv/ds).
 constexpr unsigned long long kM4400 = 0x40B1300000000000ull;   // 4400.0
