@@ -180,9 +180,9 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
                                         double gam, double igmm1, double (&f)[NV],
                                         double &pr, double &cmax, bool hll = false)
 {
+  // the conserved states are formed in the branches that read them: a
+  // supersonic face needs only its upwind side's
   double uL[NV], uR[NV];
-  prim_to_cons<NV>(vL, uL, igmm1);
-  prim_to_cons<NV>(vR, uR, igmm1);
   // sound speeds sqrt(gamma p / rho) as (gamma p) rsqrt(gamma p rho): one
   // reciprocal square root in place of a division and a square root
   const double gpL = gam * vL[PRS], gpR = gam * vR[PRS];
@@ -192,6 +192,7 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
   cmax = nn_max(fabs(SL), fabs(SR));
 
   if (gt0(SL)) {
+    prim_to_cons<NV>(vL, uL, igmm1);
     f[RHO] = uL[VN];
     f[VX1] = uL[VX1] * vL[VN];
     f[VX2] = uL[VX2] * vL[VN];
@@ -199,6 +200,7 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
     f[PRS] = (uL[PRS] + vL[PRS]) * vL[VN];
     pr = vL[PRS];
   } else if (lt0(SR)) {
+    prim_to_cons<NV>(vR, uR, igmm1);
     f[RHO] = uR[VN];
     f[VX1] = uR[VX1] * vR[VN];
     f[VX2] = uR[VX2] * vR[VN];
@@ -206,6 +208,8 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
     f[PRS] = (uR[PRS] + vR[PRS]) * vR[VN];
     pr = vR[PRS];
   } else if (SOLVER == HLL || hll) {
+    prim_to_cons<NV>(vL, uL, igmm1);
+    prim_to_cons<NV>(vR, uR, igmm1);
     double fL[NFLX], fR[NFLX];
     fL[RHO] = uL[VN];
     fL[VX1] = uL[VX1] * vL[VN];
@@ -227,6 +231,8 @@ __device__ __forceinline__ void riemann(const double (&vL)[NV], const double (&v
   } else {
     // HLLC: only the star state on the side selected by the contact speed
     // is formed; the reference forms both and discards one.
+    prim_to_cons<NV>(vL, uL, igmm1);
+    prim_to_cons<NV>(vR, uR, igmm1);
     const double qL = vL[PRS] + uL[VN] * (vL[VN] - SL);
     const double qR = vR[PRS] + uR[VN] * (vR[VN] - SR);
     const double wL = vL[RHO] * (vL[VN] - SL);

@@ -20,6 +20,7 @@
 #include <cuda_bf16.h>
 
 #include "ps_blondin.cuh"
+#include "ps_physics.cuh"
 #include "ps_tc.cuh"
 
 namespace ps {
@@ -293,22 +294,22 @@ __device__ __forceinline__ int sg_judge(SgCtx &b, double T, double T0, bool from
   double dz = cth - b.dt * dhc * 0.5;
   bool conv = fabs(z) <= kSgResidual * T * cth;
   stiff = !conv;
-  if (!conv && from_net && T0 > 0.0 && isfinite(T0) && fabs(T0 - T) > kSgJump * T) {
+  if (!conv && from_net && gt0(T0) && isfinite(T0) && fabs(T0 - T) > kSgJump * T) {
     Tk = T0;
     z = sg_z(b, Tk, dz, hc);
     evals++;
     conv = fabs(z) <= kSgResidual * Tk * cth;
   }
   for (int it = 0; !conv; it++) {
-    if (evals >= kSgMaxNewton || !(dz > 0.0)) return SG_REJECT;
+    if (evals >= kSgMaxNewton || !gt0(dz)) return SG_REJECT;
     Tk = fmin(fmax(Tk - z / dz, 0.5 * Tk), 2.0 * Tk);
     z = sg_z(b, Tk, dz, hc);
     evals++;
     conv = fabs(z) <= kSgResidual * Tk * cth;
   }
-  if (!(dz > 0.0) || hc * b.hc_init < 0.0) return SG_REJECT;
+  if (!gt0(dz) || lt0(hc * b.hc_init)) return SG_REJECT;
   const double Tn = Tk - z / dz;
-  if (!(Tn > 0.0) || !isfinite(Tn) || (Tn - T) * b.hc_init < 0.0) return SG_REJECT;
+  if (!gt0(Tn) || !isfinite(Tn) || lt0((Tn - T) * b.hc_init)) return SG_REJECT;
   T_f = Tn;
   return SG_ACCEPT;
 }
