@@ -50,9 +50,9 @@ __device__ __forceinline__ int sg_decide(SgCtx &b, double T, bool inbox, float y
   evals = 0;
   stiff = false;
   if (!inbox) return SG_OUT_OF_BOX;
-  const double sq = sqrt(b.xi);
-  b.isqxi = 1.0 / sq;
-  b.sqsqxi = sqrt(sq);
+  // xi^-1/2 by one reciprocal square root, xi^1/4 as sqrt(xi xi^-1/2)
+  b.isqxi = rsqrt(b.xi);
+  b.sqsqxi = sqrt(b.xi * b.isqxi);
   T0 = T * (double)exp10f(4.0f * y);
   return sg_judge(b, T, T0, use_net != 0, T_f, evals, stiff);
 }
