@@ -257,6 +257,13 @@ __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params 
         for (int nv = 0; nv < NV; nv++) Us[nv * p.vstride + c] = u[nv];
       }
     }
+    if constexpr (NV == NFLX + 2) {
+      // ENTROPY_SWITCH: ComputeEntropy after Boundary (Src/entropy_switch.c:
+      // 14-37), s = p / rho^gamma, once per zone; the ghost copies below and
+      // in the x2 part carry it, and the stage kernels read it with the tile
+      v[NV - 1] = v[PRS] * rho_pow(v[RHO], -p.gamma);
+      V[(NV - 1) * p.vstride + c] = v[NV - 1];
+    }
     // ghost layers: 2, or 3 with SHOCK_FLATTENING MULTID (GetNghost)
     const int b = p.beg[0], e = p.beg[0] + p.nx[0] - 1, nn = p.nx[0], ng = p.beg[0];
 #pragma unroll
@@ -804,14 +811,8 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
     }
     return;
   }
-  if constexpr (NV == NFLX + 2) {
-    // ENTROPY_SWITCH: the entropy of every zone of the tile, s = p / rho^gamma,
-    // as ComputeEntropy leaves it after Boundary (Src/entropy_switch.c:14-37);
-    // the stored entropy plane is not read
-    for (int k = tid; k < G::VS; k += G::NT)
-      sv[(NV - 1) * G::VS + k] = sv[PRS * G::VS + k] * rho_pow(sv[RHO * G::VS + k], -p.gamma);
-    __syncthreads();
-  }
+  // (ENTROPY_SWITCH: the entropy plane of the tile holds s = p / rho^gamma of
+  // every zone, as the boundary kernel's ComputeEntropy left it)
 
   // VGradCalc's corner velocities (line_connect.c:637-660: the mean of the
   // four zones that meet at a zone corner), formed once per corner of the
@@ -907,7 +908,6 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       double v0[NV], U0[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
-      if constexpr (NV == NFLX + 2) v0[NV - 1] = v0[PRS] * rho_pow(v0[RHO], -p.gamma);
       prim_to_cons<NV>(v0, U0, p.igmm1);
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = 0.5 * U0[nv] + 0.5 * U[nv];
