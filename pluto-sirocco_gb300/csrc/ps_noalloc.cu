@@ -24,9 +24,11 @@
 // serialised by the caller.
 //
 // Set-up: the first call on a device looks up the device address of the
-// array with cudaGetSymbolAddress (with that device current) and keeps it;
-// make that first call before any stream capture that will contain this
-// entry point.
+// array with cudaGetSymbolAddress (with that device current) and keeps it.
+//
+// Streams: every call copies the dx arrays in from pageable host memory and
+// waits for its stream before it returns (the flags and invDt_hyp are read
+// back), so it cannot be called while that stream is being captured.
 #include "ps_gb300.h"
 #include "ps_hydro.cuh"
 #include "ps_physics.cuh"
@@ -125,17 +127,26 @@ __global__ void k_na_prepare(double *base, ps::Params p, double dt, double inv_i
   }
 }
 
+// The driver's tensor-map encoder, looked up once per process under the
+// lock (two host threads making their first calls together would race on
+// an unguarded static).
+PFN_cuTensorMapEncodeTiled_v12000 g_na_encode = nullptr;
+
 int na_encode(const ps::Params &p, const int *tile, double *base, CUtensorMap *tm)
 {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (!encode) {
-    cudaDriverEntryPointQueryResult q;
-    void *fn = nullptr;
-    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
-                                                     cudaEnableDefault, &q);
-    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
-      return na_cuda(e == cudaSuccess ? cudaErrorNotSupported : e, "cuTensorMapEncodeTiled");
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  PFN_cuTensorMapEncodeTiled_v12000 encode;
+  {
+    std::lock_guard<std::mutex> lk(g_na_mutex);
+    if (!g_na_encode) {
+      cudaDriverEntryPointQueryResult q;
+      void *fn = nullptr;
+      cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                       cudaEnableDefault, &q);
+      if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return na_cuda(e == cudaSuccess ? cudaErrorNotSupported : e, "cuTensorMapEncodeTiled");
+      g_na_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    encode = g_na_encode;
   }
   cuuint64_t dims[4] = {(cuuint64_t)p.ntot[0], (cuuint64_t)p.ntot[1], (cuuint64_t)p.ntot[2],
                         (cuuint64_t)p.nvar};
@@ -163,6 +174,12 @@ extern "C" int ps_advance_step_noalloc(const ps_config *cfg, const double *dx1, 
       cfg->geometry != PS_CARTESIAN || cfg->limiter < 0 || cfg->limiter > 2 ||
       (cfg->solver != PS_HLLC && cfg->solver != PS_HLL) || cfg->gamma <= 1.0)
     return na_error("ps_advance_step_noalloc: unsupported configuration");
+  // as ps_create on a Cartesian context: these switches belong to the
+  // spherical wind path (SHOCK_FLATTENING MULTID would also mean 3 ghost
+  // zones per side, which this entry point does not lay out)
+  if (cfg->char_limiting || cfg->shock_flattening || cfg->entropy_switch)
+    return na_error("ps_advance_step_noalloc: characteristic limiting, shock flattening and "
+                    "the entropy switch need a spherical wind context");
   ps::Params p;
   std::memset(&p, 0, sizeof(p));
   p.dims = cfg->dims;
