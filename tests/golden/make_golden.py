@@ -78,7 +78,7 @@ RHO_ALPHA                   1.5
 CENT_MASS                   1.4e34
 DISK_MDOT                   1.0e-8
 T_ISO                       4.0e4
-L_star                      1.0e37
+L_star                      {l_star}
 f_x                         1.0
 f_uv                        1.0
 T_x                         5.6e7
@@ -195,17 +195,17 @@ def run_case(ref, name, cfg, dims, n, solver, bc, steps, full):
     print(name, "t =", t_s, "dt =", dt_s)
 
 
-def write_flux_files(wd, nr, nt, dense=False):
+def write_flux_files(wd, nr, nt, dense=False, l_uv=1.0e37):
     """directional_flux_{r,theta,phi}.dat in the format read by
     read_sirocco_fluxes (Src/LineDriven/line_connect.c:84-165): two header
     lines (the second holds the angle count as its third token), then one
     row per active cell: i j k r[cm] theta[rad] F_0 .. F_35.  dense: flux in
-    every bin (oracle.dense_flux_bins)."""
+    every bin (oracle.dense_flux_bins).  l_uv = L_star f_uv."""
     import psgb
     from oracle import synthetic_flux, NANGLES, WIND
     x1 = psgb.build_grid(nr, 2, 10.0, 1000.0, "log")[0]
     x2 = psgb.build_grid(nt, 2, 0.0, 1.5707963267948966, "uniform")[0]
-    fl = synthetic_flux(x1, x2, (nr + 4, nt + 4, 1), dense=dense)
+    fl = synthetic_flux(x1, x2, (nr + 4, nt + 4, 1), dense=dense, l_uv=l_uv)
     for ax, name in enumerate(("r", "theta", "phi")):
         with open(os.path.join(wd, f"directional_flux_{name}.dat"), "w") as f:
             f.write("# synthetic directional UV flux\n")
@@ -268,7 +268,7 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux, opts):
     with open(os.path.join(wd, "pluto.ini"), "w") as f:
         mfit = opts.get("mfit", False)
         f.write(WIND_INI.format(nr=n[0], nt=n[1], every=every,
-                                solver=opts.get("solver", "hll"),
+                                solver=opts.get("solver", "hll"), l_star="1.0e37",
                                 krad=999 if mfit else 0.2, alpharad=999 if mfit else -0.6))
     if flux:
         write_flux_files(wd, n[0], n[1], dense=bool(opts.get("dense_flux", 0)))
@@ -299,9 +299,67 @@ def run_wind_case(ref, name, cfg, n, steps, every, flux, opts):
     print(name, "t =", meta["t"][-1])
 
 
+def batch_probe_models():
+    """The first model of each grid size in the 64-model batch (seed 4):
+    (index, spec) pairs, smallest grid first."""
+    import psgb
+    specs = psgb.batch_models(64, seed=4)
+    seen, out = set(), []
+    for m, sp in enumerate(specs):
+        if sp["grid"] not in seen:
+            seen.add(sp["grid"])
+            out.append((m, sp))
+    return sorted(out, key=lambda e: e[1]["grid"][0])
+
+
+def wind_full_cases():
+    """Digest-only wind cases at full size: the 512 x 256 wind with every
+    term on for 100 steps, and one model of each grid size of the 64-model
+    batch (its own L_x, k and alpha) for 20 steps."""
+    cases = [("wind2d_full_512x256", (512, 256), 100, dict(l_star=1.0e37, krad=0.2,
+                                                           alpharad=-0.6), None)]
+    for m, sp in batch_probe_models():
+        cases.append(("wind2d_batch_m%02d_%dx%d" % ((m,) + sp["grid"]), sp["grid"], 20,
+                      dict(l_star=sp["l_star"], krad=sp["krad"], alpharad=sp["alpharad"]), m))
+    return cases
+
+
+def run_wind_full_case(ref, name, n, steps, prm, model):
+    """The reference on a full-size wind: only the digests, per-variable
+    sums, t and dt of the initial and final states are kept (the states
+    themselves come from the oracle, pinned by these digests, at test time)."""
+    cfg = "wind2d"
+    subprocess.run(["make", "-s", "-f", os.path.join(ORACLE, "ref.mk"), f"CFG={cfg}",
+                    f"REF={ref}", "-j8"], check=True)
+    exe = os.path.join(ORACLE, "_ref", cfg, "pluto")
+    wd = os.path.join(ORACLE, "_ref", "runs", name)
+    shutil.rmtree(wd, ignore_errors=True)
+    os.makedirs(wd)
+    with open(os.path.join(wd, "pluto.ini"), "w") as f:
+        f.write(WIND_INI.format(nr=n[0], nt=n[1], every=steps, solver="hll",
+                                l_star=repr(float(prm["l_star"])), krad=repr(float(prm["krad"])),
+                                alpharad=repr(float(prm["alpharad"]))))
+    write_flux_files(wd, n[0], n[1], l_uv=prm["l_star"])
+    subprocess.run([exe, "-maxsteps", str(steps - 1)], cwd=wd, check=True,
+                   stdout=subprocess.DEVNULL)
+    v0 = np.fromfile(os.path.join(wd, "data.0000.dbl"), dtype="<f8").reshape(6, n[1], n[0])
+    v1 = np.fromfile(os.path.join(wd, "data.0001.dbl"), dtype="<f8").reshape(6, n[1], n[0])
+    lines = [l.split() for l in open(os.path.join(wd, "dbl.out")).read().split("\n") if l]
+    meta = dict(name=name, ref_config=cfg, kind="wind_full", dims=2, n=[n[0], n[1], 1],
+                steps=steps, batch_model=model, l_star=float(prm["l_star"]),
+                krad=float(prm["krad"]), alpharad=float(prm["alpharad"]),
+                t=[lines[0][1], lines[1][1]], dt=[lines[0][2], lines[1][2]],
+                ic_sha256=digest(v0), final_sha256=digest(v1),
+                final_sums=[float(x) for x in v1.reshape(6, -1).sum(axis=1)])
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print(name, "t =", meta["t"][-1])
+    shutil.rmtree(wd, ignore_errors=True)   # the flux files of a full-size grid run to 0.3 GB
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PLUTO_REF", "/root/reference"))
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     if not os.path.isdir(os.path.join(args.ref, "Src")):
@@ -312,6 +370,9 @@ def main():
     for c in WIND_CASES:
         if args.only is None or args.only in c[0]:
             run_wind_case(args.ref, *c)
+    for c in wind_full_cases():
+        if args.only is None or args.only in c[0]:
+            run_wind_full_case(args.ref, *c)
 
 
 if __name__ == "__main__":

@@ -16,11 +16,11 @@ pytestmark = pytest.mark.gpu
 N = (16, 12, 10)
 
 
-def _oracle(V):
+def _oracle(V, n=N):
     import psgb
     from oracle import Oracle
     cp = psgb.COOL_PARAMS
-    o = Oracle(dims=3, nx=N, nvar=5, limiter="mc", solver="hllc", bc="periodic", cfl=0.4,
+    o = Oracle(dims=3, nx=n, nvar=5, limiter="mc", solver="hllc", bc="periodic", cfl=0.4,
                cfl_max_var=1.1, tstop=1e10, first_dt=1e-3, cooling=1,
                params=dict(unit_density=cp["unit_density"], unit_length=cp["unit_length"],
                            unit_velocity=cp["unit_velocity"], mu=cp["mu"], t_x=cp["t_x"],

@@ -1,0 +1,141 @@
+"""Parity at the configurations' own sizes, on the GPU.
+
+* The 512 x 256 line-driven wind with every term on (BLONDIN, line force,
+  gravity, floors), 100 steps: the device state against the oracle, whose
+  result at this size is pinned bit for bit to the reference's own build
+  (tests/test_oracle_fullsize.py, digest in
+  tests/golden/wind2d_full_512x256.json): relative L1 per variable within
+  1e-11, conserved mass and energy within 1e-12, t and dt within 1e-12.
+* The 64-model batch (seed 4, grids 128x64 .. 512x256), advanced as one
+  batch for 20 steps: one model of each grid size against the oracle run of
+  that model (its own L_x, k and alpha; pinned to the reference by the
+  wind2d_batch_m*.json digests), same bounds.
+* The 3-D periodic cooling cube at 64^3 (4 x 16 x 16 stage tiles), 10 steps,
+  against the oracle: BLONDIN's exp/pow are CUDA's on the device and
+  glibc's in the oracle, so the state is held to 1e-9 as for the small cube.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import CONSERVED_REL, GOLDEN, HYDRO_REL_L1, rel_l1
+
+pytestmark = pytest.mark.gpu
+
+GAMMA = 5.0 / 3.0
+
+
+def _golden(name):
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        return json.load(f)
+
+
+def _sph_volumes(grid):
+    """Cell volumes of the active 2-D spherical cells over 2 pi."""
+    _, xl1, xr1, _ = grid.arrays[0]
+    _, xl2, xr2, _ = grid.arrays[1]
+    g = grid.ngh[0]
+    dr3 = (xr1[g:-g] ** 3 - xl1[g:-g] ** 3) / 3.0
+    dmu = np.cos(xl2[g:-g]) - np.cos(xr2[g:-g])
+    return dmu[:, None] * dr3[None, :]
+
+
+def _conserved(a, dV):
+    """Total mass and total energy of active primitive states [nv][j][i]."""
+    rho, v1, v2, v3, p = a[0], a[1], a[2], a[3], a[4]
+    e = 0.5 * rho * (v1 * v1 + v2 * v2 + v3 * v3) + p / (GAMMA - 1.0)
+    return np.array([(rho * dV).sum(), (e * dV).sum()])
+
+
+def _check_wind(a, ref, dV, what):
+    r = rel_l1(a, ref)
+    c, c_ref = _conserved(a, dV), _conserved(ref, dV)
+    cr = np.abs(c - c_ref) / np.abs(c_ref)
+    print(f"{what}: relative L1 per variable {r}; mass, energy {cr}")
+    assert np.all(r <= HYDRO_REL_L1), (what, r)
+    assert np.all(cr <= CONSERVED_REL), (what, cr)
+    return r
+
+
+@pytest.fixture(scope="module")
+def wind_512():
+    """The oracle's 512 x 256 wind after 100 steps (about a minute)."""
+    from oracle import wind_oracle
+    o = wind_oracle(512, 256, cooling=1, line_force=1)
+    o.run(100)
+    return o.active().copy(), o.time()
+
+
+def test_wind_512x256_matches_oracle_after_100_steps(built, wind_512):
+    import psgb
+    meta = _golden("wind2d_full_512x256")
+    ref, (t_o, dt_o, step_o) = wind_512
+    s = psgb.wind_model_solver(dict(grid=(512, 256), l_star=meta["l_star"], krad=meta["krad"],
+                                    alpharad=meta["alpharad"]))
+    flags = s.run(100)
+    assert flags & ~0x2 == 0, flags   # PS_F_CONS2PRIM: a repaired cell, as the reference flags it
+    a = s.get_state()[:, 0, 2:-2, 2:-2]
+    _check_wind(a, ref, _sph_volumes(s.grid), "512x256 wind, 100 steps")
+    t, dt, step, _ = s.time()
+    assert step == step_o == 100
+    assert abs(t - t_o) <= 1e-12 * t_o and abs(dt - dt_o) <= 1e-12 * dt_o
+    # and the reference's own record of t (printed to 7 digits in dbl.out)
+    assert abs(t - float(meta["t"][1])) <= 6e-7 * t
+    s.close()
+
+
+def test_batch_models_match_oracle_inside_the_64_model_batch(built):
+    import psgb
+    from oracle import wind_oracle
+    specs = psgb.batch_models(64, seed=4)
+    probes = sorted(((json.load(open(os.path.join(GOLDEN, f)))) for f in os.listdir(GOLDEN)
+                     if f.startswith("wind2d_batch_m") and f.endswith(".json")),
+                    key=lambda m: m["n"][0])
+    assert [tuple(m["n"][:2]) for m in probes] == list(psgb.BATCH_GRIDS)
+    solvers = [psgb.wind_model_solver(sp) for sp in specs]
+    batch = psgb.Batch(solvers)
+    batch.autotune(reps=2)
+    flags = batch.run(20)
+    assert flags & ~0x2 == 0, flags
+    for meta in probes:
+        m = meta["batch_model"]
+        sp = specs[m]
+        assert tuple(sp["grid"]) == tuple(meta["n"][:2])
+        assert sp["l_star"] == meta["l_star"] and sp["krad"] == meta["krad"]
+        o = wind_oracle(sp["grid"][0], sp["grid"][1], cooling=1, line_force=1,
+                        l_star=sp["l_star"], krad=sp["krad"], alpharad=sp["alpharad"])
+        o.run(20)
+        s = solvers[m]
+        a = s.get_state()[:, 0, 2:-2, 2:-2]
+        _check_wind(a, o.active(), _sph_volumes(s.grid),
+                    "batch model %d (%dx%d), 20 steps" % ((m,) + tuple(sp["grid"])))
+        t, dt, step, _ = s.time()
+        t_o, dt_o, step_o = o.time()
+        assert step == step_o == 20
+        assert abs(t - t_o) <= 1e-12 * t_o and abs(dt - dt_o) <= 1e-12 * dt_o
+    batch.close()
+
+
+def test_cube_64_matches_oracle(built):
+    import psgb
+    from test_gpu_cube import _oracle
+    n = (64, 64, 64)
+    cfg = psgb.cube_config(n)
+    g = psgb.Grid(cfg)
+    V0 = psgb.cube_state(cfg, g, seed=5)
+    s = psgb.Solver(cfg, g)
+    s.set_state(V0)
+    s.set_time(0.0, cfg.first_dt, 0)
+    s.set_cooling(psgb.make_cooling())
+    o = _oracle(V0, n)
+    s.run(10)
+    o.run(10)
+    r = rel_l1(s.get_state()[:, 2:-2, 2:-2, 2:-2], o.active())
+    print("64^3 cube, 10 steps: relative L1 per variable", r)
+    assert np.all(r <= 1e-9), r
+    t_g, dt_g, step_g, _ = s.time()
+    t_o, dt_o, step_o = o.time()
+    assert step_g == step_o == 10
+    assert abs(t_g - t_o) <= 1e-12 * t_o and abs(dt_g - dt_o) <= 1e-12 * dt_o
