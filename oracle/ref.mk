@@ -4,14 +4,15 @@
 # oracle/_ref/<CFG>/ (git-ignored) and is used to generate and pin golden
 # vectors for the oracle restatement.
 #
-#   make -f oracle/ref.mk CFG=blast2d REF=/root/reference
+#   make -f oracle/ref.mk CFG=blast2d [REF=<reference tree>]   (default $PLUTO_REF)
 #
 # Flags follow Config/Linux.gcc.defs of the reference (-O3 -std=c17, no
 # -march, so no FMA contraction); the object list follows
 # Src/Templates/makefile plus the module makefiles for HD, EOS/Ideal,
 # Math_Tools and the RK2/PLM choices made by setup.py.
 
-REF     ?= /root/reference
+PLUTO_REF ?= /root/reference
+REF     ?= $(PLUTO_REF)
 CFG     ?= blast2d
 HERE    := $(dir $(abspath $(lastword $(MAKEFILE_LIST))))
 CFGDIR  := $(HERE)ref_cfg/$(CFG)
