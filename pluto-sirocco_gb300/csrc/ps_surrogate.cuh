@@ -20,6 +20,7 @@
 #include <cuda_bf16.h>
 
 #include "ps_blondin.cuh"
+#include "ps_fastmath.cuh"
 #include "ps_physics.cuh"
 #include "ps_tc.cuh"
 
@@ -225,11 +226,11 @@ __device__ __forceinline__ double sg_heatcool_d(const SgCtx &b, double T, double
   const double rT = rsqrt(T), sqT = T * rT, iT = rT * rT;
   double r, dr;
   if (T < 1.5e4) {
-    const double q = exp(2.302585092994046 * (-51.59417133) + 12.27740153 * log(T));
+    const double q = fm::exp(2.302585092994046 * (-51.59417133) + 12.27740153 * fm::log(T));
     r = 1e-2 + q;
     dr = 12.27740153 * q * iT;
   } else if (T < 3.3e4) {
-    const double q = exp(2.302585092994046 * (-3.80749689) + 0.86092628 * log(T));
+    const double q = fm::exp(2.302585092994046 * (-3.80749689) + 0.86092628 * fm::log(T));
     r = q;
     dr = 0.86092628 * q * iT;
   } else {
@@ -240,7 +241,7 @@ __device__ __forceinline__ double sg_heatcool_d(const SgCtx &b, double T, double
   const double comp_heat = 8.9e-36 * b.xi * b.tx;
   const double comp_cool = 8.9e-36 * b.xi * (4.0 * T), dcomp_cool = 8.9e-36 * b.xi * 4.0;
   const double xray_heat = 1.5e-21 * b.sqsqxi * rT, dxray_heat = -0.5 * xray_heat * iT;
-  const double l1 = 1e-16 * exp(-1.3e5 * iT) * b.isqxi * iT;
+  const double l1 = 1e-16 * fm::exp(-1.3e5 * iT) * b.isqxi * iT;
   const double dl1 = l1 * (1.3e5 * iT - 1.0) * iT;
   const double m1 = 5e-27 * sqT, m2 = 1.5e-17 * iT;
   double l2, dl2;

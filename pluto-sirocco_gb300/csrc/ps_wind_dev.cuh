@@ -15,11 +15,13 @@
 #pragma once
 
 #include "ps_blondin.cuh"
+#include "ps_fastmath.cuh"
 #include "ps_ode_cool.cuh"
 #include "ps_ctx.cuh"
 #include "ps_physics.cuh"
 #include "ps_stage.cuh"
 #include "ps_tma.cuh"
+#include "ps_userdef.cuh"
 #include "ps_wind.cuh"
 
 namespace ps {
@@ -206,36 +208,9 @@ __device__ __forceinline__ void cell_of(const Params &p, long long q, int &gi, i
   gk = (int)(r / p.nx[1]) + p.beg[2];
 }
 
-// density / pressure floors of the problem's UserDefBoundary(side 0);
-// returns true if the cell was repaired.
-template <int NV>
-__device__ __forceinline__ bool apply_floors(double (&v)[NV], const WindParams &w, double gamma)
-{
-  bool convert = false;
-  const double K = w.kelvin, mu = w.mu;
-  if (v[RHO] < w.dfloor) {
-    if (v[RHO] < 0.0) v[RHO] = w.dfloor;
-    const double cs = sqrt(gamma * v[PRS] / v[RHO]);
-    const double dfact = v[RHO] / w.dfloor;
-    v[RHO] = w.dfloor;
-    v[VX1] = dfact * v[VX1];
-    v[VX2] = dfact * v[VX2];
-    v[VX3] = dfact * v[VX3];
-    v[PRS] = cs * cs * v[RHO] / gamma;
-    const double temp = v[PRS] / v[RHO] * K * mu;
-    if (temp < w.tfloor) v[PRS] = v[RHO] * w.tfloor / (K * mu);
-    if constexpr (NV > NFLX) v[NFLX] = 0.0;
-    convert = true;
-  }
-  if (v[PRS] < w.pfloor) {
-    v[PRS] = w.pfloor;
-    convert = true;
-  }
-  return convert;
-}
-
-// Boundary() part 1: floors on the active cells, then the x1 ghost cells
-// of the active rows, each written by the active cell it comes from.
+// Boundary() part 1: the problem's side-0 hook (floors) on the active cells,
+// then the x1 ghost cells of the active rows, each written by the active
+// cell it comes from (user sides through the X1 hooks of ps_userdef.cuh).
 template <int NV>
 __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params &p,
                                             const WindParams &w, int stage, int q)
@@ -244,10 +219,24 @@ __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params 
     const int i = q % p.nx[0], j = q / p.nx[0];
     const int gi = i + p.beg[0], gj = j + p.beg[1];
     const long long c = vcell(p, gj, gi);
+    // density and pressure decide the floors; the other variables are
+    // read only for a floored cell or a cell whose x1 ghosts it writes
+    // (the first and last active columns, or every column within the ghost
+    // width of either end for periodic and reflective boundaries)
+    const int ng = p.beg[0];
+    const bool edge = gi < p.beg[0] + ng || gi > p.beg[0] + p.nx[0] - 1 - ng;
     double v[NV];
+    v[RHO] = V[RHO * p.vstride + c];
+    v[PRS] = V[PRS * p.vstride + c];
+    const bool floored = w.floors && (v[RHO] < w.dfloor || v[PRS] < w.pfloor);
+    if (floored || edge) {
+      v[VX1] = V[VX1 * p.vstride + c];
+      v[VX2] = V[VX2 * p.vstride + c];
+      v[VX3] = V[VX3 * p.vstride + c];
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) v[nv] = V[nv * p.vstride + c];
-    if (w.floors && apply_floors<NV>(v, w, p.gamma)) {
+      for (int nv = NFLX; nv < NV; nv++) v[nv] = V[nv * p.vstride + c];
+    }
+    if (floored && UserDefBoundary_Internal<NV>(v, w, p.gamma)) {
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) V[nv * p.vstride + c] = v[nv];
       if (stage == 2) {
@@ -264,19 +253,20 @@ __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params 
       v[NV - 1] = v[PRS] * rho_pow(v[RHO], -p.gamma);
       V[(NV - 1) * p.vstride + c] = v[NV - 1];
     }
+    if (!edge) return;
     // ghost layers: 2, or 3 with SHOCK_FLATTENING MULTID (GetNghost)
-    const int b = p.beg[0], e = p.beg[0] + p.nx[0] - 1, nn = p.nx[0], ng = p.beg[0];
+    const int b = p.beg[0], e = p.beg[0] + p.nx[0] - 1, nn = p.nx[0];
 #pragma unroll
     for (int side = 0; side < 2; side++) {
       const int type = p.bc[side];
       int tg[3] = {-1, -1, -1};
-      bool flip = false, inflow = false;
-      if (type == BC_OUTFLOW || type == PS_BC_USERDEF) {
+      bool flip = false;
+      const bool user = type == PS_BC_USERDEF;
+      if (type == BC_OUTFLOW || user) {
         for (int k = 0; k < ng; k++) {
           if (side == 0 && gi == b) tg[k] = b - 1 - k;
           if (side == 1 && gi == e) tg[k] = e + 1 + k;
         }
-        inflow = (type == PS_BC_USERDEF) && side == 0;
       } else if (type == BC_PERIODIC) {
         if (side == 0 && gi >= e - (ng - 1)) tg[0] = gi - nn;
         if (side == 1 && gi <= b + (ng - 1)) tg[0] = gi + nn;
@@ -294,7 +284,7 @@ __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params 
         for (int nv = 0; nv < NV; nv++) {
           double val = v[nv];
           if (flip && (nv == VX1 || (type == BC_AXISYM && nv == VX3))) val = -1 * val;
-          if (inflow && nv == VX1) val = dmin(val, 0.0);
+          if (user) val = side == 0 ? UserDefBoundary_X1Beg(nv, val) : UserDefBoundary_X1End(nv, val);
           V[nv * p.vstride + g] = val;
         }
       }
@@ -315,6 +305,16 @@ __device__ __forceinline__ void bnd_x2_item(double *V, const Params &p, int q)
     const int type = p.bc[2 + side];
     int src;
     bool flip = false;
+    if (type == PS_BC_USERDEF) {
+      // X2_BEG of the production problem (X2_END user sides are refused by
+      // ps_set_wind): velocities mirrored, density and pressure copied
+      const int mirror = 2 * b - 1 - gj;
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++)
+        V[nv * p.vstride + vcell(p, gj, gi)] = UserDefBoundary_X2Beg<NV>(
+            nv, V[nv * p.vstride + vcell(p, mirror, gi)], V[nv * p.vstride + vcell(p, b, gi)]);
+      return;
+    }
     if (type == BC_OUTFLOW)
       src = side == 0 ? b : e;
     else if (type == BC_PERIODIC)
@@ -492,7 +492,9 @@ __device__ __forceinline__ void bilinear_w(double fx, double fy, const double (&
 // bin as M = exp(lf_a0 + alpharad/2 log(rho p lq)) with lq = (dv/ds)^-2 from
 // VGradCalc (one log and one exp per call); for cells with two or more bins
 // as M = (rho p)^(alpharad/2) B, B = exp(lf_a0 - alpharad log(dv/ds)) formed
-// once per stage in VGradCalc (one log and one exp per call).  With KRAD = ALPHARAD
+// once per stage in VGradCalc (one log and one exp per call).  The
+// exponentials and logarithms are the table-driven ones of ps_fastmath.cuh
+// (11 and 13 FP64 instructions against 15 and 29 for CUDA's).  With KRAD = ALPHARAD
 // = 999, M is interpolated in the cell's table at log10 t = lt0 +
 // log10(rho p)/2 + lq, lq = -log10(dv/ds).
 constexpr unsigned long long kM4400 = 0x40B1300000000000ull;   // 4400.0
@@ -536,7 +538,7 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
   if (e1 - e0 >= 2) {
     // M = (rho p)^(alpharad/2) times the bin's factor from VGradCalc (0 where
     // dv/ds <= 0)
-    const double Q = exp(0.5 * w.alpharad * log(vg[RHO] * vg[PRS]));
+    const double Q = fm::exp(0.5 * w.alpharad * fm::log(vg[RHO] * vg[PRS]));
     for (int e = e0; e < e1; e++) {
       const double B = L.lq[e];
       double M = 0.0;
@@ -556,7 +558,7 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
     const double q = L.lq[e];
     double M = 0.0;
     if (gt0(q)) {
-      M = exp(w.lf_a0 + 0.5 * w.alpharad * log(rp * q));
+      M = fm::exp(w.lf_a0 + 0.5 * w.alpharad * fm::log(rp * q));
       if (gt_pos<kM4400>(M)) M = 4400.;
     }
     const double F = comp == 0 ? L.Fr[e] : L.Ft[e];
@@ -889,7 +891,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
           if (is_nan_bits(dvds)) flags |= F_NAN;
           if (gt0(dvds))
             lq = A.w.mfit ? -log10(dvds)
-                 : fact   ? exp(A.w.lf_a0 - alpha * log(dvds))
+                 : fact   ? fm::exp(A.w.lf_a0 - alpha * fm::log(dvds))
                           : 1.0 / (dvds * dvds);
         }
         A.L.lq[e] = lq;

@@ -1,7 +1,13 @@
-// ps_probe.cu -- FP64 issue-rate probe used as the denominator of the FP64
-// roofline: independent chains of dependent double-precision FMAs in
-// registers, many warps per SM, no memory traffic.
-#include "ps_gb300.h"
+// ps_probe.cu -- measurement helpers kept out of the product library
+// (built into libps_probe.so, used by bench.py and the tests only):
+//   ps_probe_fp64_flops  FP64 issue-rate probe, the denominator of the FP64
+//                        roofline: independent chains of dependent
+//                        double-precision FMAs in registers, many warps per
+//                        SM, no memory traffic;
+//   ps_probe_fastmath    the table-driven exp / log of the stage kernels
+//                        (csrc/ps_fastmath.cuh) next to CUDA's on the same
+//                        arguments, for the accuracy test.
+#include "ps_fastmath.cuh"
 
 #include <cuda_runtime.h>
 
@@ -24,9 +30,36 @@ __global__ void k_fp64_fma_chains(double *out, int iters, double a, double b)
   if (s == 12345.678) out[0] = s;  // keeps the chains live
 }
 
+__global__ void k_fastmath(int op, const double *x, double *fast, double *ref, long n)
+{
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    fast[i] = op == 0 ? fm::exp(v) : fm::log(v);
+    ref[i] = op == 0 ? ::exp(v) : ::log(v);
+  }
+}
+
 }  // namespace ps
 
-extern "C" void ps_set_error_msg(const char *msg);
+// op 0: exp, 1: log.  x, fast and ref are host arrays of n doubles; returns
+// 0 or -1 on a CUDA error.
+extern "C" int ps_probe_fastmath(int op, const double *x, double *fast, double *ref, long n)
+{
+  if (n <= 0 || (op != 0 && op != 1)) return -1;
+  double *d = nullptr;
+  const size_t bytes = (size_t)n * sizeof(double);
+  if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return -1;
+  cudaError_t e = cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    ps::k_fastmath<<<1024, 256>>>(op, d, d + n, d + 2 * n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(fast, d + n, bytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(ref, d + 2 * n, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? 0 : -1;
+}
 
 // FP64 FLOP/s of the current device (2 flops per FMA), best of `reps`.
 extern "C" double ps_probe_fp64_flops(int reps)

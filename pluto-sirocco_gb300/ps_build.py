@@ -26,6 +26,8 @@ HOST = os.path.join(PKG, "host")
 INC = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libps_gb300.so")
+PROBE_SRC = os.path.join(PKG, "probe", "ps_probe.cu")
+PROBE = os.path.join(PKG, "libps_probe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-fmad=true", "-lineinfo", "-Xcompiler", "-fPIC",
@@ -81,7 +83,18 @@ def build_lib(force=False, verbose=False):
                 print(out)
     if force or jobs or not os.path.exists(LIB):
         _run([nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    build_probe(force)
     return LIB
+
+
+def build_probe(force=False):
+    """libps_probe.so: measurement helpers for bench.py and the tests (the
+    FP64 issue-rate probe, the fast-math check); not part of the C ABI."""
+    deps = [PROBE_SRC, os.path.join(CSRC, "ps_fastmath.cuh"),
+            os.path.join(CSRC, "ps_fastmath_tables.cuh")]
+    if force or _newer(deps, PROBE):
+        _run([nvcc()] + ARCH + NVFLAGS + ["-shared", PROBE_SRC, "-o", PROBE, "-lcudart"])
+    return PROBE
 
 
 def build_oracle():

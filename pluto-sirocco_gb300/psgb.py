@@ -10,6 +10,7 @@ import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libps_gb300.so")
+PROBE_PATH = os.path.join(PKG, "libps_probe.so")
 
 CARTESIAN, SPHERICAL = 0, 3
 LIM = {"mc": 0, "vl": 1, "mm": 2}
@@ -24,7 +25,7 @@ FLAGS = {0x01: "nan", 0x02: "cons2prim", 0x04: "negative_density", 0x08: "dt_too
 EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_destroy",
            "ps_set_grid", "ps_set_state", "ps_get_state", "ps_set_time", "ps_get_time",
            "ps_advance_step", "ps_run", "ps_sync", "ps_device_state", "ps_launch_count",
-           "ps_get_dt_history", "ps_set_stream", "ps_probe_fp64_flops", "ps_save_state",
+           "ps_get_dt_history", "ps_set_stream", "ps_save_state",
            "ps_restore_state", "ps_time_step_kernels", "ps_advance_step_noalloc",
            "ps_init_wind", "ps_wind_synthetic_flux", "ps_wind_synthetic_flux_dense",
            "ps_set_wind", "ps_split_source",
@@ -37,7 +38,8 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_set_cooling", "ps_write_dbl", "ps_read_dbl", "ps_read_sirocco_fluxes",
            "ps_read_sirocco_heatcool", "ps_read_sirocco_prefactors", "ps_set_sirocco",
            "ps_read_m_uv_fit", "ps_set_mfit", "ps_batch_set_states", "ps_batch_get_states",
-           "ps_batch_set_states_async", "ps_batch_get_states_async"]
+           "ps_batch_set_states_async", "ps_batch_get_states_async", "ps_batch_set_groups",
+           "ps_split_source_dt"]
 
 
 class Config(ctypes.Structure):
@@ -116,8 +118,6 @@ def lib():
         L.ps_launch_count.restype = ctypes.c_long
         L.ps_get_dt_history.argtypes = [P, DP, I]
         L.ps_set_stream.argtypes = [P, P]
-        L.ps_probe_fp64_flops.argtypes = [I]
-        L.ps_probe_fp64_flops.restype = D
         L.ps_save_state.argtypes = [P]
         L.ps_restore_state.argtypes = [P]
         L.ps_time_step_kernels.argtypes = [P, DP]
@@ -131,6 +131,7 @@ def lib():
                                                    ctypes.POINTER(Wind), DP, DP, DP, DP, DP]
         L.ps_set_wind.argtypes = [P, ctypes.POINTER(Wind), DP, DP, DP]
         L.ps_split_source.argtypes = [P, D, D]
+        L.ps_split_source_dt.argtypes = [P, D, D, DP]
         L.ps_batch_create.argtypes = [ctypes.POINTER(P), I, ctypes.POINTER(P)]
         L.ps_batch_destroy.argtypes = [P]
         L.ps_batch_run.argtypes = [P, I]
@@ -140,6 +141,7 @@ def lib():
         L.ps_batch_set_states_async.argtypes = [P, ctypes.POINTER(DP)]
         L.ps_batch_get_states_async.argtypes = [P, ctypes.POINTER(DP)]
         L.ps_batch_set_stream.argtypes = [P, P]
+        L.ps_batch_set_groups.argtypes = [P, I]
         L.ps_batch_launch_count.argtypes = [P]
         L.ps_batch_launch_count.restype = ctypes.c_long
         L.ps_batch_set_shape.argtypes = [P, I, I]
@@ -178,6 +180,25 @@ def lib():
     return _lib
 
 
+_probe = None
+
+
+def probe():
+    """The measurement helpers (libps_probe.so, not part of the C ABI): the
+    FP64 issue-rate probe of the roofline and the fast-math check."""
+    global _probe
+    if _probe is None:
+        if not os.path.exists(PROBE_PATH):
+            raise OSError(f"{PROBE_PATH} not built: run pluto-sirocco_gb300/ps_build.py")
+        L = ctypes.CDLL(PROBE_PATH)
+        DP = ctypes.POINTER(ctypes.c_double)
+        L.ps_probe_fp64_flops.argtypes = [ctypes.c_int]
+        L.ps_probe_fp64_flops.restype = ctypes.c_double
+        L.ps_probe_fastmath.argtypes = [ctypes.c_int, DP, DP, DP, ctypes.c_long]
+        _probe = L
+    return _probe
+
+
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
@@ -210,13 +231,20 @@ def check(rc, what):
     return rc
 
 
+WIND_BC = ["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"]
+# the production disk-wind problem (Test_Problems/LineDrivenWind/cv_idl): its
+# X2-beg is the hybrid user side (pluto_sirocco_sub.py:78-81)
+CVIDL_BC = ["userdef", "outflow", "userdef", "reflective", "outflow", "outflow"]
+
+
 def make_wind_config(nr=512, nt=256, cooling=1, limiter="vl", solver="hll", cfl=0.4,
-                     first_dt=1e-4, char_limiting=0, shock_flattening=0, entropy_switch=0):
+                     first_dt=1e-4, char_limiting=0, shock_flattening=0, entropy_switch=0,
+                     bc=None):
     """The wind's configuration.  entropy_switch: 0 NO, 1 SELECTIVE, 2 ALWAYS
-    (the entropy becomes a seventh variable)."""
+    (the entropy becomes a seventh variable).  bc: six boundary names
+    (default WIND_BC)."""
     c = make_config(dims=2, nx=(nr, nt, 1), nvar=7 if entropy_switch else 6, limiter=limiter,
-                    solver=solver,
-                    bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
+                    solver=solver, bc=list(bc or WIND_BC),
                     cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt, cooling=cooling)
     c.geometry = SPHERICAL
     c.char_limiting = char_limiting
@@ -448,9 +476,11 @@ class Solver:
                                 ctypes.byref(inv)), "ps_get_time")
         return t.value, dt.value, st.value, inv.value
 
-    def run(self, nsteps):
+    def run(self, nsteps, wait=True):
+        """nsteps steps on the device; wait=False only queues them on the
+        context's stream (sync() then returns the flags)."""
         check(lib().ps_run(self.ctx, nsteps), "ps_run")
-        return self.sync()
+        return self.sync() if wait else 0
 
     def advance_step(self, dt, inv_dt_hyp=0.0):
         inv = ctypes.c_double(inv_dt_hyp)
@@ -459,6 +489,13 @@ class Solver:
 
     def split_source(self, dt, t):
         return check(lib().ps_split_source(self.ctx, dt, t), "ps_split_source")
+
+    def split_source_dt(self, dt, t):
+        """(flags, dt_cool of this pass)."""
+        out = ctypes.c_double()
+        rc = check(lib().ps_split_source_dt(self.ctx, dt, t, ctypes.byref(out)),
+                   "ps_split_source_dt")
+        return rc, out.value
 
     def sync(self):
         return check(lib().ps_sync(self.ctx), "ps_sync")
@@ -562,6 +599,9 @@ class Batch:
 
     def set_stream(self, handle):
         check(lib().ps_batch_set_stream(self.h, ctypes.c_void_p(handle)), "ps_batch_set_stream")
+
+    def set_groups(self, n):
+        check(lib().ps_batch_set_groups(self.h, n), "ps_batch_set_groups")
 
     def launches(self):
         return lib().ps_batch_launch_count(self.h)
