@@ -136,9 +136,9 @@ __global__ void k_batch_sg_fallback(const BatchModel *__restrict__ models, const
   }
 }
 
-__global__ void k_batch_finish(const BatchModel *__restrict__ models)
+__global__ void k_batch_finish(const BatchModel *__restrict__ models, const int *__restrict__ list)
 {
-  finish_block(models[blockIdx.x].fin);
+  finish_block(models[list[blockIdx.x]].fin);
 }
 
 // stage kernels for the 6-variable state with primitive PLM; the others
@@ -169,34 +169,47 @@ static size_t batch_smem(int nv, int shape)
 // host side
 // ------------------------------------------------------------------
 
+// The models are split into groups (balanced by cells) whose steps run as
+// independent branches of the step graph: one group's latency-bound
+// kernels (boundaries, the learned step's fallback, the dt kernel) overlap
+// the other groups' stage kernels.  Each group has its own work lists.
+struct BatchGroup {
+  std::vector<int> models;
+  ps::TileItem *d_items[ps::kNumShapes] = {};  // tiles per tile shape
+  int nitems[ps::kNumShapes] = {};
+  ps::BlockItem *d_cells = nullptr, *d_x2 = nullptr;
+  int ncells_blocks = 0, nx2_blocks = 0;
+  ps::BlockItem *d_shock = nullptr;  // total-box blocks of the MULTID models
+  int nshock_blocks = 0;
+  ps::BlockItem *d_cells128 = nullptr;  // 128-cell blocks (surrogate kernel)
+  int ncells128 = 0;
+  int *d_list = nullptr;             // the group's model indices (dt kernel)
+  long cells = 0, queue_off = 0;     // its cells and its slice of the queue
+  cudaStream_t st = nullptr;         // branch stream while a graph is captured
+  cudaStream_t side[ps::kNumShapes] = {};  // tile-shape branches
+  cudaEvent_t fork = nullptr, join[ps::kNumShapes] = {}, done = nullptr;
+};
+
 struct ps_batch {
   int n = 0;
   std::vector<ps_ctx *> ctx;
   ps::BatchModel *d_models = nullptr;
   std::vector<ps::BatchModel> h_models;
   std::vector<int> shape;              // chosen tile shape per model
-  // per shape group: work list of tiles
-  ps::TileItem *d_items[ps::kNumShapes] = {};
-  int nitems[ps::kNumShapes] = {};
-  ps::BlockItem *d_cells = nullptr, *d_x2 = nullptr;
-  int ncells_blocks = 0, nx2_blocks = 0;
-  ps::BlockItem *d_shock = nullptr;  // total-box blocks of the MULTID models
-  int nshock_blocks = 0;
+  std::vector<BatchGroup> grp;
+  int ngroups = 1;
   const double **d_xi = nullptr, **d_tr = nullptr, **d_pre = nullptr;
-  ps::BlockItem *d_cells128 = nullptr;  // 128-cell blocks (surrogate kernel)
-  int ncells128 = 0;
   long total_cells = 0;
   ps_surrogate *sg = nullptr;
   int sg_use_net = 1;
   int num_sms = 148;
   int2 *sg_queue = nullptr;
-  int *sg_qcount = nullptr;
+  int *sg_qcount = nullptr;            // one counter per group
   int lim = 0, solver = 0, cooling = 0, nvar = 6;
   bool char_lim = false;  // CHAR_LIMITING YES (its own stage kernels)
   cudaStream_t stream = nullptr;      // stream the work is issued on
   cudaStream_t own_stream = nullptr;  // stream created by the batch
-  cudaStream_t side[ps::kNumShapes] = {};  // tile-shape groups
-  cudaEvent_t fork = nullptr, join[ps::kNumShapes] = {};
+  cudaEvent_t fork = nullptr;
   cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};
   long long host_step = 0;
   long launches = 0;
@@ -247,12 +260,36 @@ static int encode_box(const ps::Params &p, double *base, int tx, int ty, CUtenso
   return 0;
 }
 
-// Rebuilds the per-model descriptors and the work lists for the current
-// shape choice and uploads them.
+template <class T>
+static int upload_list(const std::vector<T> &v, T **dst)
+{
+  cudaFree(*dst);
+  *dst = nullptr;
+  if (v.empty()) return 0;
+  BCK(cudaMalloc(dst, v.size() * sizeof(T)));
+  BCK(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// Models of each group: sorted by cells, dealt out in turn so that every
+// group gets a like share of each grid size.
+static void batch_partition(ps_batch *b)
+{
+  std::vector<int> order(b->n);
+  for (int m = 0; m < b->n; m++) order[m] = m;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const ps::Params &px = b->ctx[x]->p, &py = b->ctx[y]->p;
+    return (long)px.nx[0] * px.nx[1] > (long)py.nx[0] * py.nx[1];
+  });
+  for (BatchGroup &g : b->grp) g.models.clear();
+  for (int k = 0; k < b->n; k++) b->grp[k % b->ngroups].models.push_back(order[k]);
+  for (BatchGroup &g : b->grp) std::sort(g.models.begin(), g.models.end());
+}
+
+// Rebuilds the per-model descriptors and every group's work lists for the
+// current shape choice and uploads them.
 static int batch_upload(ps_batch *b)
 {
-  std::vector<ps::TileItem> items[ps::kNumShapes];
-  std::vector<ps::BlockItem> cells, x2, cells128, shock;
   b->total_cells = 0;
   for (int m = 0; m < b->n; m++) {
     ps_ctx *c = b->ctx[m];
@@ -284,51 +321,46 @@ static int batch_upload(ps_batch *b)
     }
     M.fin.p = p;
     M.fin.mode = ps::MODE_STEP;
-    const int ntx = (p.nx[0] + tx - 1) / tx, nty = (p.nx[1] + ty - 1) / ty;
-    for (int by = 0; by < nty; by++)
-      for (int bx = 0; bx < ntx; bx++) items[sh].push_back({m, bx, by, 0});
-    const int nc = (p.nx[0] * p.nx[1] + 255) / 256, n2 = (p.ntot[0] * 2 * p.beg[1] + 255) / 256;
-    for (int k = 0; k < nc; k++) cells.push_back({m, k});
-    const int nc128 = (p.nx[0] * p.nx[1] + 127) / 128;
-    for (int k = 0; k < nc128; k++) cells128.push_back({m, k});
     b->total_cells += (long)p.nx[0] * p.nx[1];
-    for (int k = 0; k < n2; k++) x2.push_back({m, k});
-    if (ps::needs_shock_flags(p))
-      for (int k = 0; k < (p.ntot[0] * p.ntot[1] + 255) / 256; k++) shock.push_back({m, k});
   }
   BCK(cudaMemcpy(b->d_models, b->h_models.data(), sizeof(ps::BatchModel) * b->n,
                  cudaMemcpyHostToDevice));
-  for (int s = 0; s < ps::kNumShapes; s++) {
-    cudaFree(b->d_items[s]);
-    b->d_items[s] = nullptr;
-    b->nitems[s] = (int)items[s].size();
-    if (items[s].empty()) continue;
-    BCK(cudaMalloc(&b->d_items[s], items[s].size() * sizeof(ps::TileItem)));
-    BCK(cudaMemcpy(b->d_items[s], items[s].data(), items[s].size() * sizeof(ps::TileItem),
-                   cudaMemcpyHostToDevice));
+  long qoff = 0;
+  for (BatchGroup &g : b->grp) {
+    std::vector<ps::TileItem> items[ps::kNumShapes];
+    std::vector<ps::BlockItem> cells, x2, cells128, shock;
+    g.cells = 0;
+    for (int m : g.models) {
+      const ps::Params &p = b->ctx[m]->p;
+      const int sh = b->shape[m], tx = ps::kShapeX[sh], ty = ps::kShapeY[sh];
+      const int ntx = (p.nx[0] + tx - 1) / tx, nty = (p.nx[1] + ty - 1) / ty;
+      for (int by = 0; by < nty; by++)
+        for (int bx = 0; bx < ntx; bx++) items[sh].push_back({m, bx, by, 0});
+      const int nc = (p.nx[0] * p.nx[1] + 255) / 256, n2 = (p.ntot[0] * 2 * p.beg[1] + 255) / 256;
+      for (int k = 0; k < nc; k++) cells.push_back({m, k});
+      const int nc128 = (p.nx[0] * p.nx[1] + 127) / 128;
+      for (int k = 0; k < nc128; k++) cells128.push_back({m, k});
+      for (int k = 0; k < n2; k++) x2.push_back({m, k});
+      if (ps::needs_shock_flags(p))
+        for (int k = 0; k < (p.ntot[0] * p.ntot[1] + 255) / 256; k++) shock.push_back({m, k});
+      g.cells += (long)p.nx[0] * p.nx[1];
+    }
+    for (int sh = 0; sh < ps::kNumShapes; sh++) {
+      if (int r = upload_list(items[sh], &g.d_items[sh])) return r;
+      g.nitems[sh] = (int)items[sh].size();
+    }
+    if (int r = upload_list(cells, &g.d_cells)) return r;
+    if (int r = upload_list(x2, &g.d_x2)) return r;
+    if (int r = upload_list(cells128, &g.d_cells128)) return r;
+    if (int r = upload_list(shock, &g.d_shock)) return r;
+    if (int r = upload_list(g.models, &g.d_list)) return r;
+    g.ncells_blocks = (int)cells.size();
+    g.nx2_blocks = (int)x2.size();
+    g.ncells128 = (int)cells128.size();
+    g.nshock_blocks = (int)shock.size();
+    g.queue_off = qoff;
+    qoff += g.cells;
   }
-  cudaFree(b->d_cells);
-  cudaFree(b->d_x2);
-  BCK(cudaMalloc(&b->d_cells, cells.size() * sizeof(ps::BlockItem)));
-  BCK(cudaMalloc(&b->d_x2, x2.size() * sizeof(ps::BlockItem)));
-  BCK(cudaMemcpy(b->d_cells, cells.data(), cells.size() * sizeof(ps::BlockItem),
-                 cudaMemcpyHostToDevice));
-  BCK(cudaMemcpy(b->d_x2, x2.data(), x2.size() * sizeof(ps::BlockItem), cudaMemcpyHostToDevice));
-  cudaFree(b->d_cells128);
-  BCK(cudaMalloc(&b->d_cells128, cells128.size() * sizeof(ps::BlockItem)));
-  BCK(cudaMemcpy(b->d_cells128, cells128.data(), cells128.size() * sizeof(ps::BlockItem),
-                 cudaMemcpyHostToDevice));
-  b->ncells128 = (int)cells128.size();
-  cudaFree(b->d_shock);
-  b->d_shock = nullptr;
-  if (!shock.empty()) {
-    BCK(cudaMalloc(&b->d_shock, shock.size() * sizeof(ps::BlockItem)));
-    BCK(cudaMemcpy(b->d_shock, shock.data(), shock.size() * sizeof(ps::BlockItem),
-                   cudaMemcpyHostToDevice));
-  }
-  b->nshock_blocks = (int)shock.size();
-  b->ncells_blocks = (int)cells.size();
-  b->nx2_blocks = (int)x2.size();
   for (int k = 0; k < 3; k++) {
     if (b->g[k]) cudaGraphExecDestroy(b->g[k]);
     b->g[k] = nullptr;
@@ -336,45 +368,44 @@ static int batch_upload(ps_batch *b)
   return 0;
 }
 
-// The stage kernels of the tile-shape groups run side by side (a fork onto
-// the group streams and a join back), so that one group's tail overlaps the
-// others' work; the groups touch disjoint models.
-static int batch_stage(ps_batch *b, int stage)
+// The stage kernels of a group's tile-shape sets run side by side (a fork
+// onto the shape streams and a join back), so that one set's tail overlaps
+// the others' work; the sets touch disjoint models.
+static int batch_stage(ps_batch *b, BatchGroup &g, int stage, cudaStream_t st0)
 {
   int first = -1;
   for (int s = 0; s < ps::kNumShapes; s++)
-    if (b->nitems[s] && first < 0) first = s;
-  BCK(cudaEventRecord(b->fork, b->stream));
+    if (g.nitems[s] && first < 0) first = s;
+  BCK(cudaEventRecord(g.fork, st0));
   for (int s = 0; s < ps::kNumShapes; s++) {
-    if (!b->nitems[s]) continue;
-    cudaStream_t st = s == first ? b->stream : b->side[s];
-    if (s != first) BCK(cudaStreamWaitEvent(st, b->fork, 0));
+    if (!g.nitems[s]) continue;
+    cudaStream_t st = s == first ? st0 : g.side[s];
+    if (s != first) BCK(cudaStreamWaitEvent(st, g.fork, 0));
     const void *k = ps::batch_kernel(b->nvar, b->char_lim, s, b->lim, b->solver, stage);
-    void *args[2] = {&b->d_models, &b->d_items[s]};
-    BCK(cudaLaunchKernel(k, dim3(b->nitems[s]), dim3(ps::kShapeNT[s]), args, ps::batch_smem(b->nvar, s),
-                         st));
+    void *args[2] = {&b->d_models, &g.d_items[s]};
+    BCK(cudaLaunchKernel(k, dim3(g.nitems[s]), dim3(ps::kShapeNT[s]), args,
+                         ps::batch_smem(b->nvar, s), st));
     b->launches++;
-    if (s != first) BCK(cudaEventRecord(b->join[s], st));
+    if (s != first) BCK(cudaEventRecord(g.join[s], st));
   }
   for (int s = 0; s < ps::kNumShapes; s++)
-    if (b->nitems[s] && s != first) BCK(cudaStreamWaitEvent(b->stream, b->join[s], 0));
+    if (g.nitems[s] && s != first) BCK(cudaStreamWaitEvent(st0, g.join[s], 0));
   return 0;
 }
 
-static int batch_bnd(ps_batch *b, int stage)
+static int batch_bnd(ps_batch *b, BatchGroup &g, int stage, cudaStream_t st)
 {
+  if (g.models.empty()) return 0;
   if (b->nvar == 7) {
-    ps::k_batch_bnd_x1<7><<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells,
-                                                                    stage);
-    ps::k_batch_bnd_x2<7><<<b->nx2_blocks, 256, 0, b->stream>>>(b->d_models, b->d_x2, stage);
+    ps::k_batch_bnd_x1<7><<<g.ncells_blocks, 256, 0, st>>>(b->d_models, g.d_cells, stage);
+    ps::k_batch_bnd_x2<7><<<g.nx2_blocks, 256, 0, st>>>(b->d_models, g.d_x2, stage);
   } else {
-    ps::k_batch_bnd_x1<6><<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells,
-                                                                    stage);
-    ps::k_batch_bnd_x2<6><<<b->nx2_blocks, 256, 0, b->stream>>>(b->d_models, b->d_x2, stage);
+    ps::k_batch_bnd_x1<6><<<g.ncells_blocks, 256, 0, st>>>(b->d_models, g.d_cells, stage);
+    ps::k_batch_bnd_x2<6><<<g.nx2_blocks, 256, 0, st>>>(b->d_models, g.d_x2, stage);
   }
   b->launches += 2;
-  if (stage == 1 && b->nshock_blocks) {
-    ps::k_batch_shock<<<b->nshock_blocks, 256, 0, b->stream>>>(b->d_models, b->d_shock);
+  if (stage == 1 && g.nshock_blocks) {
+    ps::k_batch_shock<<<g.nshock_blocks, 256, 0, st>>>(b->d_models, g.d_shock);
     b->launches++;
   }
   return 0;
@@ -384,46 +415,116 @@ ps::SgNet ps_sg_net(const ps_surrogate *s);
 ps::SgBox ps_sg_boxv(const ps_surrogate *s);
 unsigned long long *ps_sg_stats_dev(ps_surrogate *s);
 
-static int batch_cool(ps_batch *b)
+static int batch_cool(ps_batch *b, BatchGroup &g, cudaStream_t st)
 {
-  if (!b->cooling) return 0;
+  if (!b->cooling || g.models.empty()) return 0;
   if (b->sg) {
-    BCK(cudaMemsetAsync(b->sg_qcount, 0, sizeof(int), b->stream));
-    const int grid = std::min(b->ncells128, b->num_sms * ps::kInfCtasPerSm);
-    ps::k_batch_sg_cool<<<grid, 128, ps::kInfBytes, b->stream>>>(
-        b->d_models, b->d_cells128, b->ncells128, b->d_xi, b->d_tr, b->d_pre, ps_sg_net(b->sg),
-        ps_sg_boxv(b->sg), b->sg_use_net, b->sg_queue, b->sg_qcount, ps_sg_stats_dev(b->sg));
-    ps::k_batch_sg_fallback<<<1216, 128, 0, b->stream>>>(b->d_models, b->d_xi, b->d_tr, b->d_pre,
-                                                         b->sg_queue, b->sg_qcount);
+    const int gi = (int)(&g - b->grp.data());
+    int *qcount = b->sg_qcount + gi;
+    int2 *queue = b->sg_queue + g.queue_off;
+    BCK(cudaMemsetAsync(qcount, 0, sizeof(int), st));
+    const int grid = std::min(g.ncells128, b->num_sms * ps::kInfCtasPerSm);
+    ps::k_batch_sg_cool<<<grid, 128, ps::kInfBytes, st>>>(
+        b->d_models, g.d_cells128, g.ncells128, b->d_xi, b->d_tr, b->d_pre, ps_sg_net(b->sg),
+        ps_sg_boxv(b->sg), b->sg_use_net, queue, qcount, ps_sg_stats_dev(b->sg));
+    ps::k_batch_sg_fallback<<<1216, 128, 0, st>>>(b->d_models, b->d_xi, b->d_tr, b->d_pre, queue,
+                                                  qcount);
     b->launches += 2;
     return 0;
   }
   if (b->cooling == 2) {   // the ODE path
-    ps::k_batch_ode<<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, b->d_xi,
-                                                             b->d_tr, b->d_pre);
+    ps::k_batch_ode<<<g.ncells_blocks, 256, 0, st>>>(b->d_models, g.d_cells, b->d_xi, b->d_tr,
+                                                     b->d_pre);
     b->launches++;
     return 0;
   }
-  ps::k_batch_blondin<<<b->ncells_blocks, 256, 0, b->stream>>>(b->d_models, b->d_cells, b->d_xi,
-                                                               b->d_tr, b->d_pre);
+  ps::k_batch_blondin<<<g.ncells_blocks, 256, 0, st>>>(b->d_models, g.d_cells, b->d_xi, b->d_tr,
+                                                       b->d_pre);
   b->launches++;
   return 0;
 }
 
-static int batch_step(ps_batch *b, int odd)
+static int batch_finish(ps_batch *b, BatchGroup &g, cudaStream_t st)
+{
+  if (g.models.empty()) return 0;
+  ps::k_batch_finish<<<(unsigned)g.models.size(), 256, 0, st>>>(b->d_models, g.d_list);
+  b->launches++;
+  return 0;
+}
+
+// One step of one group on stream st.
+static int batch_step_group(ps_batch *b, BatchGroup &g, int odd, cudaStream_t st)
 {
   int r = 0;
-  if (odd) r = batch_cool(b);
-  for (int st = 1; !r && st <= 2; st++) {
-    r = batch_bnd(b, st);
-    if (!r) r = batch_stage(b, st);
+  if (odd) r = batch_cool(b, g, st);
+  for (int stage = 1; !r && stage <= 2; stage++) {
+    r = batch_bnd(b, g, stage, st);
+    if (!r) r = batch_stage(b, g, stage, st);
   }
-  if (!r && !odd) r = batch_cool(b);
-  if (!r) {
-    ps::k_batch_finish<<<b->n, 256, 0, b->stream>>>(b->d_models);
-    b->launches++;
-  }
+  if (!r && !odd) r = batch_cool(b, g, st);
+  if (!r) r = batch_finish(b, g, st);
   return r;
+}
+
+// The steps `odd` (a list of 0 / 1) of every group, each group's steps in
+// order on its own stream (forked from and joined back to the batch's
+// stream; a single group runs on the batch's stream itself).
+static int batch_steps(ps_batch *b, const int *odd, int nsteps)
+{
+  if (b->ngroups == 1) {
+    for (int k = 0; k < nsteps; k++)
+      if (int r = batch_step_group(b, b->grp[0], odd[k], b->stream)) return r;
+    return 0;
+  }
+  BCK(cudaEventRecord(b->fork, b->stream));
+  for (BatchGroup &g : b->grp) {
+    BCK(cudaStreamWaitEvent(g.st, b->fork, 0));
+    for (int k = 0; k < nsteps; k++)
+      if (int r = batch_step_group(b, g, odd[k], g.st)) return r;
+    BCK(cudaEventRecord(g.done, g.st));
+  }
+  for (BatchGroup &g : b->grp) BCK(cudaStreamWaitEvent(b->stream, g.done, 0));
+  return 0;
+}
+
+static void batch_free_groups(ps_batch *b)
+{
+  for (BatchGroup &g : b->grp) {
+    for (int s = 0; s < ps::kNumShapes; s++) {
+      cudaFree(g.d_items[s]);
+      if (g.side[s]) cudaStreamDestroy(g.side[s]);
+      if (g.join[s]) cudaEventDestroy(g.join[s]);
+    }
+    cudaFree(g.d_cells);
+    cudaFree(g.d_x2);
+    cudaFree(g.d_cells128);
+    cudaFree(g.d_shock);
+    cudaFree(g.d_list);
+    if (g.st) cudaStreamDestroy(g.st);
+    if (g.fork) cudaEventDestroy(g.fork);
+    if (g.done) cudaEventDestroy(g.done);
+  }
+  b->grp.clear();
+}
+
+static int batch_make_groups(ps_batch *b, int ngroups)
+{
+  batch_free_groups(b);
+  b->ngroups = std::max(1, std::min(ngroups, b->n));
+  b->grp.resize(b->ngroups);
+  for (BatchGroup &g : b->grp) {
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&g.fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming)) != cudaSuccess)
+      return batch_cuda(e, "ps_batch: group streams");
+    for (int k = 0; k < ps::kNumShapes; k++)
+      if ((e = cudaStreamCreateWithFlags(&g.side[k], cudaStreamNonBlocking)) != cudaSuccess ||
+          (e = cudaEventCreateWithFlags(&g.join[k], cudaEventDisableTiming)) != cudaSuccess)
+        return batch_cuda(e, "ps_batch: group streams");
+  }
+  batch_partition(b);
+  return 0;
 }
 
 static void batch_free(ps_batch *b)
@@ -432,24 +533,20 @@ static void batch_free(ps_batch *b)
   for (int k = 0; k < 3; k++)
     if (b->g[k]) cudaGraphExecDestroy(b->g[k]);
   cudaFree(b->d_models);
-  for (int s = 0; s < ps::kNumShapes; s++) cudaFree(b->d_items[s]);
-  cudaFree(b->d_cells);
-  cudaFree(b->d_x2);
+  batch_free_groups(b);
   cudaFree(b->d_xi);
   cudaFree(b->d_tr);
   cudaFree(b->d_pre);
-  cudaFree(b->d_cells128);
-  cudaFree(b->d_shock);
   cudaFree(b->sg_queue);
   cudaFree(b->sg_qcount);
-  for (int k = 0; k < ps::kNumShapes; k++) {
-    if (b->side[k]) cudaStreamDestroy(b->side[k]);
-    if (b->join[k]) cudaEventDestroy(b->join[k]);
-  }
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
 }
+
+// Default number of model groups: 4 when the batch has at least 16 models
+// (measured on the 64-model benchmark batch), else 1.
+static int default_groups(int n) { return n >= 16 ? 4 : 1; }
 
 extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
 {
@@ -487,12 +584,9 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
     return batch_cuda(e, "ps_batch_create");
   }
   b->stream = b->own_stream;
-  for (int k = 0; k < ps::kNumShapes; k++) {
-    if ((e = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming)) != cudaSuccess) {
-      batch_free(b);
-      return batch_cuda(e, "ps_batch_create: streams");
-    }
+  if (int r = batch_make_groups(b, default_groups(n))) {
+    batch_free(b);
+    return r;
   }
   {
     int dev = 0;
@@ -527,6 +621,22 @@ extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
   }
   *out = b;
   return 0;
+}
+
+// Number of model groups whose steps run as parallel branches (1 to the
+// number of models); the models are dealt out by size.  No reference
+// counterpart.
+extern "C" int ps_batch_set_groups(ps_batch *b, int ngroups)
+{
+  if (!b || ngroups < 1) return batch_fail("ps_batch_set_groups: bad arguments");
+  BCK(cudaStreamSynchronize(b->stream));
+  if (int r = batch_make_groups(b, ngroups)) return r;
+  if (b->sg) {   // queue counters, one per group
+    cudaFree(b->sg_qcount);
+    b->sg_qcount = nullptr;
+    BCK(cudaMalloc(&b->sg_qcount, sizeof(int) * b->ngroups));
+  }
+  return batch_upload(b);
 }
 
 extern "C" int ps_batch_destroy(ps_batch *b)
@@ -628,9 +738,8 @@ static int batch_graph(ps_batch *b, int kind, cudaGraphExec_t *out)
   cudaGraph_t g;
   const long before = b->launches;
   BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  int r = 0;
-  if (kind == 0 || kind == 2) r = batch_step(b, 0);
-  if (!r && (kind == 1 || kind == 2)) r = batch_step(b, 1);
+  static const int kSteps[3][2] = {{0, 0}, {1, 0}, {0, 1}};
+  const int r = batch_steps(b, kSteps[kind], kind == 2 ? 2 : 1);
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   b->launches = before;
   if (r) return r;
@@ -644,10 +753,14 @@ static int batch_graph(ps_batch *b, int kind, cudaGraphExec_t *out)
 extern "C" int ps_batch_run(ps_batch *b, int nsteps)
 {
   if (!b || nsteps < 0) return PS_EINVAL;
-  int nshape = 0;
-  for (int s = 0; s < ps::kNumShapes; s++) nshape += b->nitems[s] > 0;
-  const long per_step = 4 + 2 * nshape + (b->cooling ? (b->sg ? 2 : 1) : 0) + 1 +
-                        (b->nshock_blocks ? 1 : 0);
+  long per_step = 0;   // kernels of one step over every group
+  for (const BatchGroup &g : b->grp) {
+    if (g.models.empty()) continue;
+    int nshape = 0;
+    for (int s = 0; s < ps::kNumShapes; s++) nshape += g.nitems[s] > 0;
+    per_step += 4 + 2 * nshape + (b->cooling ? (b->sg ? 2 : 1) : 0) + 1 +
+                (g.nshock_blocks ? 1 : 0);
+  }
   for (int k = 0; k < 3; k++)
     if (!b->g[k]) {
       int r = batch_graph(b, k, &b->g[k]);
@@ -845,9 +958,9 @@ extern "C" int ps_batch_set_surrogate(ps_batch *b, ps_surrogate *s, int use_net)
     return batch_fail("ps_batch_set_surrogate: the learned step replaces BLONDIN's implicit "
                       "solve, not the ODE cooling path");
   BCK(cudaStreamSynchronize(b->stream));
-  if (s && !b->sg_queue) {
+  if (s && !b->sg_queue) {   // each group's slice of the queue and its counter
     BCK(cudaMalloc(&b->sg_queue, sizeof(int2) * (size_t)b->total_cells));
-    BCK(cudaMalloc(&b->sg_qcount, sizeof(int)));
+    BCK(cudaMalloc(&b->sg_qcount, sizeof(int) * b->ngroups));
   }
   b->sg = s;
   b->sg_use_net = use_net;
@@ -869,22 +982,28 @@ extern "C" int ps_batch_time_step_kernels(ps_batch *b, float *ms)
   b->host_step = b->ctx[0]->host_step;
   const int odd = (int)(b->host_step & 1);
   int r = 0;
-  BCK(cudaEventRecord(ev[0], b->stream));
-  if (odd) r = batch_cool(b);
-  if (!r) r = batch_bnd(b, 1);
-  BCK(cudaEventRecord(ev[1], b->stream));
-  if (!r) r = batch_stage(b, 1);
-  BCK(cudaEventRecord(ev[2], b->stream));
-  if (!r) r = batch_bnd(b, 2);
-  BCK(cudaEventRecord(ev[3], b->stream));
-  if (!r) r = batch_stage(b, 2);
-  BCK(cudaEventRecord(ev[4], b->stream));
-  if (!r && !odd) r = batch_cool(b);
-  if (!r) {
-    ps::k_batch_finish<<<b->n, 256, 0, b->stream>>>(b->d_models);
-    b->launches++;
-  }
-  BCK(cudaEventRecord(ev[5], b->stream));
+  cudaStream_t st = b->stream;
+  // phase by phase, every group's launches of a phase in turn on one stream
+  BCK(cudaEventRecord(ev[0], st));
+  for (BatchGroup &g : b->grp)
+    if (!r && odd) r = batch_cool(b, g, st);
+  for (BatchGroup &g : b->grp)
+    if (!r) r = batch_bnd(b, g, 1, st);
+  BCK(cudaEventRecord(ev[1], st));
+  for (BatchGroup &g : b->grp)
+    if (!r) r = batch_stage(b, g, 1, st);
+  BCK(cudaEventRecord(ev[2], st));
+  for (BatchGroup &g : b->grp)
+    if (!r) r = batch_bnd(b, g, 2, st);
+  BCK(cudaEventRecord(ev[3], st));
+  for (BatchGroup &g : b->grp)
+    if (!r) r = batch_stage(b, g, 2, st);
+  BCK(cudaEventRecord(ev[4], st));
+  for (BatchGroup &g : b->grp)
+    if (!r && !odd) r = batch_cool(b, g, st);
+  for (BatchGroup &g : b->grp)
+    if (!r) r = batch_finish(b, g, st);
+  BCK(cudaEventRecord(ev[5], st));
   BCK(cudaEventSynchronize(ev[5]));
   float t[5];
   for (int k = 0; k < 5; k++) cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]);

@@ -10,6 +10,8 @@
 
 #include <cudaTypedefs.h>
 
+#include <type_traits>
+
 namespace ps {
 
 struct BatchModel {
@@ -28,7 +30,7 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap *tm)
 }
 
 template <int NV, int LIM, int SOLVER, int STAGE, class TL, bool CHAR>
-__global__ void __launch_bounds__(TileGeom<TL>::NT)
+__global__ void __launch_bounds__(TileGeom<TL>::NT, TileMinBlocks<TL>::value)
     k_batch_stage(const BatchModel *__restrict__ models, const TileItem *__restrict__ items)
 {
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -43,13 +45,22 @@ __global__ void __launch_bounds__(TileGeom<TL>::NT)
 // kernel tables for the tile shapes the autotuner chooses from
 // ------------------------------------------------------------------
 
-constexpr int kNumShapes = 4;
-const int kShapeX[kNumShapes] = {32, 16, 64, 16};
-const int kShapeY[kNumShapes] = {8, 16, 4, 16};
+constexpr int kNumShapes = 6;
+const int kShapeX[kNumShapes] = {32, 16, 64, 16, 16, 32};
+const int kShapeY[kNumShapes] = {8, 16, 4, 16, 16, 8};
 // threads per CTA: one per cell, plus one warp for the halo work of the
-// 16x16 tile's PLM (18 x 16 items) in shape 3
-const int kShapeNT[kNumShapes] = {256, 256, 256, 288};
+// 16x16 tile's PLM (18 x 16 items) in shapes 3 and 4
+const int kShapeNT[kNumShapes] = {256, 256, 256, 288, 288, 256};
 using Shape3 = Tile2D<16, 16, 32>;
+// Shapes 4 and 5: shapes 3 and 0 compiled for three CTAs per multiprocessor
+// (at most 72 / 80 registers, with some spilling) instead of two, for the
+// primitive-PLM 6-variable kernels; other variants run them as 3 and 0.
+template <int NV, bool CHAR> struct Shape4 {
+  using T = typename std::conditional<NV == 6 && !CHAR, Tile2D<16, 16, 32, 3>, Shape3>::type;
+};
+template <int NV, bool CHAR> struct Shape5 {
+  using T = typename std::conditional<NV == 6 && !CHAR, Tile2D<32, 8, 0, 3>, Tile2D<32, 8>>::type;
+};
 
 template <int NV, bool CHAR, int LIM, int SOLVER, class TL>
 const void *pick_batch(int stage)
@@ -80,6 +91,8 @@ const void *batch_kernel_nv(int shape, int lim, int solver, int stage)
     case 1: return pick_batch_shape<NV, CHAR, Tile2D<16, 16>>(lim, solver, stage);
     case 2: return pick_batch_shape<NV, CHAR, Tile2D<64, 4>>(lim, solver, stage);
     case 3: return pick_batch_shape<NV, CHAR, Shape3>(lim, solver, stage);
+    case 4: return pick_batch_shape<NV, CHAR, typename Shape4<NV, CHAR>::T>(lim, solver, stage);
+    case 5: return pick_batch_shape<NV, CHAR, typename Shape5<NV, CHAR>::T>(lim, solver, stage);
     default: return pick_batch_shape<NV, CHAR, Tile2D<32, 8>>(lim, solver, stage);
   }
 }
@@ -90,7 +103,8 @@ size_t batch_smem_nv(int shape)
   switch (shape) {
     case 1: return stage_smem_bytes<NV, Tile2D<16, 16>>();
     case 2: return stage_smem_bytes<NV, Tile2D<64, 4>>();
-    case 3: return stage_smem_bytes<NV, Shape3>();
+    case 3:
+    case 4: return stage_smem_bytes<NV, Shape3>();
     default: return stage_smem_bytes<NV, Tile2D<32, 8>>();
   }
 }

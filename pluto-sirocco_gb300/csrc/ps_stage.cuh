@@ -35,8 +35,10 @@ template <> struct TileT<3> {
 // XT extra threads (whole warps) share the halo work of the PLM and
 // Riemann phases, which have more items than the tile has cells; they own
 // no cell.
-template <int TX, int TY, int XT = 0> struct Tile2D {
-  static constexpr int X = TX, Y = TY, Z = 1, HX = 2, HY = 2, HZ = 0, EXTRA = XT;
+// MB: the CTAs per multiprocessor the kernel is compiled for (its
+// register budget, __launch_bounds__'s second argument).
+template <int TX, int TY, int XT = 0, int MB = 1> struct Tile2D {
+  static constexpr int X = TX, Y = TY, Z = 1, HX = 2, HY = 2, HZ = 0, EXTRA = XT, MINB = MB;
 };
 
 template <class TL, class = void> struct TileExtra {
@@ -44,6 +46,12 @@ template <class TL, class = void> struct TileExtra {
 };
 template <class TL> struct TileExtra<TL, decltype((void)TL::EXTRA)> {
   static constexpr int value = TL::EXTRA;
+};
+template <class TL, class = void> struct TileMinBlocks {
+  static constexpr int value = 1;
+};
+template <class TL> struct TileMinBlocks<TL, decltype((void)TL::MINB)> {
+  static constexpr int value = TL::MINB;
 };
 
 template <class TL> struct TileGeom {

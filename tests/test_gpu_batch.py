@@ -42,6 +42,13 @@ def test_batch_matches_individual_runs(built, cooling):
             flags |= s.run(chunk)
         assert batch.run(chunk) == flags
         _check_equal(solo, inb)
+    # the models as parallel groups (here one per model): the same bits
+    batch.set_groups(3)
+    for chunk in (5, 4):
+        for s in solo:
+            s.run(chunk)
+        batch.run(chunk)
+        _check_equal(solo, inb)
     batch.close()
 
 
@@ -65,6 +72,15 @@ def test_batch_tile_shapes_and_autotune(built):
     _check_equal(solo, inb)
     for m in range(len(SPECS)):
         assert batch.shape(m) in [(32, 8), (16, 16), (64, 4)]
+    # the shapes compiled for three CTAs per multiprocessor (4: 16x16 with
+    # the halo warp, 5: 32x8) give the same bits
+    batch.set_shape(4, model=0)
+    batch.set_shape(5, model=1)
+    assert batch.shape(0) == (16, 16) and batch.shape(1) == (32, 8)
+    for s in solo:
+        s.run(4)
+    batch.run(4)
+    _check_equal(solo, inb)
     batch.close()
 
 

@@ -49,8 +49,10 @@ def test_forward_matches_oracle(built):
     y_ref, _ = M.forward(p.astype(np.float64), u)
     d = np.abs(y_gpu - y_ref)
     print("forward |dy|: median %.2e  p99 %.2e  max %.2e" % (np.median(d), np.percentile(d, 99), d.max()))
-    assert np.percentile(d, 99) < 1e-4
-    assert d.max() < 1e-2
+    # measured on the GPU: p99 2.4e-8, max 3.6e-5 (bf16 activations and FP32
+    # accumulation against the oracle's emulation of the same rounding)
+    assert np.percentile(d, 99) < 2e-7
+    assert d.max() < 4e-4
 
 
 def test_backward_matches_oracle(built):
@@ -71,7 +73,7 @@ def test_backward_matches_oracle(built):
                        ("w3", 4480, 4544), ("b3", 4544, 4545)):
         err = np.linalg.norm(g[a:b] - g_ref[a:b]) / np.linalg.norm(g_ref[a:b])
         print(name, "relative gradient error %.2e" % err)
-        assert err < 1e-2, name
+        assert err < 1e-6, name   # measured 6e-8 .. 1e-7
 
 
 def test_labels_match_oracle(built):
@@ -203,6 +205,13 @@ def test_batch_with_surrogate_matches_individual(trained):
     for s in solo:
         s.run(9)
     batch.run(9)
+    for a, b in zip(solo, inb):
+        assert np.array_equal(a.get_state(), b.get_state())
+    # in parallel groups (each with its own fallback queue): the same bits
+    batch.set_groups(2)
+    for s in solo:
+        s.run(6)
+    batch.run(6)
     for a, b in zip(solo, inb):
         assert np.array_equal(a.get_state(), b.get_state())
     batch.close()
