@@ -107,7 +107,8 @@ typedef struct ps_wind {
   double cent_mass;    /* CENT_MASS: central point mass [g]                 */
   double t_iso;        /* T_ISO: initial isothermal temperature [K]        */
   double l_star;       /* L_star [erg s^-1]                                 */
-  double f_x, f_uv;    /* X-ray and UV fractions of L_star                  */
+  double frac_x, frac_uv; /* X-ray and UV fractions of L_star (the problem's
+                          f_x, f_uv parameters)                          */
   double t_x;          /* T_x: X-ray (Compton) temperature [K]              */
   double krad, alpharad; /* force multiplier M = krad * t^alpharad          */
   double dfloor;       /* DFLOOR: density floor [g cm^-3]                   */
@@ -251,6 +252,13 @@ int ps_advance_step(ps_ctx *ctx, double dt, double *inv_dt_hyp);
  * cooling. */
 int ps_split_source(ps_ctx *ctx, double dt, double t);
 
+/* ps_split_source, and *dt_cool = the smallest cooling time step the cells
+ * asked for in this pass (1e38 when none did: BLONDIN sets none; the ODE
+ * path of cooling = 2 sets it, Src/Cooling/cooling_source.c), for the host's
+ * Dts->dt_cool = MIN(Dts->dt_cool, *dt_cool), which NextTimeStep reads
+ * (Src/main.c:644). */
+int ps_split_source_dt(ps_ctx *ctx, double dt, double t, double *dt_cool);
+
 /* The main loop of Src/main.c:215-337 (Integrate + NextTimeStep and the
  * tstop clamp) for nsteps steps, entirely on the device and replayed
  * from a captured CUDA graph; no host synchronisation between steps. */
@@ -340,10 +348,16 @@ int  ps_batch_get_states(ps_batch *b, double *const *Vc);
 int  ps_batch_set_states_async(ps_batch *b, const double *const *Vc);
 int  ps_batch_get_states_async(ps_batch *b, double *const *Vc);
 int  ps_batch_set_stream(ps_batch *b, void *stream);
+/* The models are dealt out by size into ngroups groups (default 4 for 16
+ * models or more, else 1) whose steps run as parallel branches of the step
+ * graph, so that one group's short, latency-bound kernels overlap the
+ * others' stage kernels.  Results do not depend on it. */
+int  ps_batch_set_groups(ps_batch *b, int ngroups);
 long ps_batch_launch_count(const ps_batch *b);
 /* Tile shape of the stage kernels per model: 0 = 32x8, 1 = 16x16,
- * 2 = 64x4, 3 = 16x16 with one extra warp sharing the halo work (model =
- * -1: all models).  ps_batch_autotune times the stage
+ * 2 = 64x4, 3 = 16x16 with one extra warp sharing the halo work, 4 and 5 =
+ * shapes 3 and 0 compiled for three CTAs per multiprocessor instead of two
+ * (model = -1: all models).  ps_batch_autotune times the stage
  * kernel of every distinct grid size with each shape and keeps the fastest
  * (`reps` timed launches each); the state is left unchanged. */
 int  ps_batch_set_shape(ps_batch *b, int model, int shape);
@@ -444,17 +458,16 @@ int ps_time_step_kernels(ps_ctx *ctx, double *ms);
  * stage scratch comes from a fixed array inside the library (3.3 MB per
  * GPU, held until exit).  Limits: 32768 total-box cells per variable,
  * 6 variables, 2048 cells per direction, even total-box row length;
- * larger grids get PS_EINVAL.  Calls that overlap on the GPU share the
- * scratch and race.  The first call on each device looks up the scratch
- * address; make it before any stream capture.  stream may be NULL. */
+ * larger grids get PS_EINVAL, as do the characteristic-limiting,
+ * shock-flattening and entropy-switch options (spherical wind contexts
+ * only).  Calls that overlap on the GPU share the scratch and race.  The
+ * first call on each device looks up the scratch address.  Every call
+ * copies dx in and waits for its stream before returning, so it cannot be
+ * called while that stream is being captured.  stream may be NULL. */
 int ps_advance_step_noalloc(const ps_config *cfg, const double *dx1,
                             const double *dx2, const double *dx3,
                             double *Vc_dev, double dt, double *inv_dt_hyp,
                             void *stream);
-
-/* Diagnostic with no reference counterpart: measured FP64 FMA throughput
- * of the current device in FLOP/s (2 per FMA), or < 0 on error. */
-double ps_probe_fp64_flops(int reps);
 
 #ifdef __cplusplus
 }

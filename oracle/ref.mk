@@ -64,9 +64,21 @@ INCS    += -I$(SRC)/LineDriven -I$(SRC)/Cooling
 OBJ     += line_connect.o cooling_ode_solver.o jacobian.o maxrate.o cv_radiat.o cv_cooling_source.o
 endif
 
-# The configuration directory comes first so that its init.c (and any
-# file it overrides) wins, as with PLUTO's own VPATH.
-VPATH := $(CFGDIR) $(SRCDIRS)
+# The production disk-wind problem itself (marker CVIDL): its own
+# definitions.h and init.c (UserDefBoundary, BodyForceVector, Init), and
+# the rest of its directory, compiled where they lie; the configuration
+# directory only holds pluto.ini.
+DEFS    := $(CFGDIR)/definitions.h
+PROBDIR := $(CFGDIR)
+ifneq ($(wildcard $(CFGDIR)/CVIDL),)
+PROBDIR := $(REF)/Test_Problems/LineDrivenWind/cv_idl
+DEFS    := $(PROBDIR)/definitions.h
+INCS    := -I$(PROBDIR) $(filter-out -I$(CFGDIR),$(INCS))
+endif
+
+# The problem directory comes first so that its init.c (and any file it
+# overrides) wins, as with PLUTO's own VPATH.
+VPATH := $(PROBDIR) $(SRCDIRS)
 
 OBJS := $(addprefix $(OUT)/,$(OBJ))
 
@@ -75,19 +87,35 @@ all: $(OUT)/pluto $(OUT)/pluto.ini
 $(OUT)/pluto: $(OBJS)
 	$(CC) $(OBJS) $(LDFLAGS) -o $@
 
+# The reference's own main loop with the GB300 path dropped in: PLUTO's
+# objects without AdvanceStep (rk_step.o) and SplitSource (split_source.o),
+# plus the shim that calls libps_gb300.so through include/ps_gb300.h.
+#   make -f oracle/ref.mk CFG=<cfg> shim   -> oracle/_ref/<cfg>/pluto_gb300
+PKG      := $(abspath $(HERE)../pluto-sirocco_gb300)
+SHIM_OBJS := $(filter-out $(OUT)/rk_step.o $(OUT)/split_source.o,$(OBJS)) $(OUT)/ps_pluto_shim.o
+
+shim: $(OUT)/pluto_gb300 $(OUT)/pluto.ini
+
+$(OUT)/ps_pluto_shim.o: $(PKG)/shim/ps_pluto_shim.c $(HERE)../include/ps_gb300.h \
+                        $(DEFS) | $(OUT)
+	$(CC) $(CFLAGS) $(INCS) -I$(HERE)../include -include string.h -c $< -o $@
+
+$(OUT)/pluto_gb300: $(SHIM_OBJS) $(PKG)/libps_gb300.so
+	$(CC) $(SHIM_OBJS) -L$(PKG) -lps_gb300 -Wl,-rpath,$(PKG) $(LDFLAGS) -o $@
+
 $(OUT)/pluto.ini: $(CFGDIR)/pluto.ini
 	cp $< $@
 
-$(OUT)/%.o: %.c $(CFGDIR)/definitions.h | $(OUT)
+$(OUT)/%.o: %.c $(DEFS) | $(OUT)
 	$(CC) $(CFLAGS) $(INCS) -c $< -o $@
 
-$(OUT)/cv_radiat.o: $(CVIDL)/radiat.c $(CFGDIR)/definitions.h | $(OUT)
+$(OUT)/cv_radiat.o: $(CVIDL)/radiat.c $(DEFS) | $(OUT)
 	$(CC) $(CFLAGS) $(INCS) -c $< -o $@
 
-$(OUT)/cv_cooling_source.o: $(CVIDL)/cooling_source.c $(CFGDIR)/definitions.h | $(OUT)
+$(OUT)/cv_cooling_source.o: $(CVIDL)/cooling_source.c $(DEFS) | $(OUT)
 	$(CC) $(CFLAGS) $(INCS) -c $< -o $@
 
 $(OUT):
 	mkdir -p $@
 
-.PHONY: all
+.PHONY: all shim

@@ -212,7 +212,9 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   }
   for (int s = 0; s < 2 * cfg->dims; s++) {
     int b = cfg->bc[s];
-    const bool userdef_ok = sph && s == 0 && b == PS_BC_USERDEF;
+    // user sides of the spherical wind: X1_BEG, X1_END and X2_BEG, with the
+    // production problem's hooks (csrc/ps_userdef.cuh)
+    const bool userdef_ok = sph && s <= 2 && b == PS_BC_USERDEF;
     if (b != PS_BC_OUTFLOW && b != PS_BC_PERIODIC && b != PS_BC_REFLECTIVE &&
         b != PS_BC_AXISYM && b != PS_BC_EQTSYM && !userdef_ok) {
       ps_set_error_msg("ps_create: boundary type not supported on this path");
@@ -791,23 +793,42 @@ extern "C" int ps_time_step_kernels(ps_ctx *c, double *ms)
 }
 
 // SplitSource (Src/split_source.c:28-79): the BLONDIN pass with dt at time t.
-extern "C" int ps_split_source(ps_ctx *c, double dt, double t)
+// One split-source pass with the given dt at time t.  *dt_cool (may be
+// NULL) gets the smallest cooling time step the cells of this pass asked
+// for (1e38 when none did); the device's running minimum, which the
+// device main loop's NextTimeStep reads, keeps including it.
+static int split_source(ps_ctx *c, double dt, double t, double *dt_cool)
 {
   int r = check_ready(c, "ps_split_source");
   if (r) return r;
+  if (dt_cool) *dt_cool = 1.e38;
   if (!c->p.cooling || !(c->wind || c->cool_on)) return 0;
   ps::Scalars s;
   CK(cudaStreamSynchronize(c->stream));
   CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
+  const double running = s.dt_cool;
   s.dt = dt;
   s.t = t;
   s.done = 0;
+  s.dt_cool = 1.e38;
   CK(cudaMemcpy(c->sc, &s, sizeof(s), cudaMemcpyHostToDevice));
   r = c->wind ? ps_wind_cool_launch(c) : ps_cart_cool_launch(c);
   if (r) return r;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->stream));
-  unsigned flags = 0;
-  CK(cudaMemcpy(&flags, &c->sc->flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
-  return (int)flags;
+  CK(cudaMemcpy(&s, c->sc, sizeof(s), cudaMemcpyDeviceToHost));
+  if (dt_cool) *dt_cool = s.dt_cool;
+  const double keep = running <= s.dt_cool ? running : s.dt_cool;
+  CK(cudaMemcpy(&c->sc->dt_cool, &keep, sizeof(double), cudaMemcpyHostToDevice));
+  return (int)s.flags;
+}
+
+extern "C" int ps_split_source(ps_ctx *c, double dt, double t)
+{
+  return split_source(c, dt, t, nullptr);
+}
+
+extern "C" int ps_split_source_dt(ps_ctx *c, double dt, double t, double *dt_cool)
+{
+  return split_source(c, dt, t, dt_cool);
 }

@@ -192,7 +192,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
     A1(G_RDR, i) = std::fabs(x1[i]) * dx1[i];
     const double rt = (xR * xR * xR - xL * xL * xL) / (xR * xR - xL * xL) / 1.5;
     A1(G_RTINV, i) = 1.0 / rt;
-    A1(G_G0, i) = -1.0 * gm_code / (x1[i] * x1[i]);
+    A1(G_G0, i) = ps::BodyForceVector_r(x1[i], gm_code);
     A1(G_XGC1, i) = x1[i] + 2.0 * x1[i] * dx1[i] * dx1[i] / (12.0 * x1[i] * x1[i] + dx1[i] * dx1[i]);
     A1(G_LOCR, i) = x1[i] * UL;
     if (i >= 1 && i + 1 < n0) {
@@ -398,7 +398,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   W.alpharad = wp->alpharad;
   W.sigma_e = ps::kSigmaT / ps::kAmu / 1.18;
   W.unit_acc = UV * UV / UL;
-  W.lx = wp->l_star * wp->f_x;
+  W.lx = wp->l_star * wp->frac_x;
   W.t_x = wp->t_x;
   W.unit_pressure = UD * UV * UV;
   W.unit_time = UL / UV;

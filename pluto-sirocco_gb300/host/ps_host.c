@@ -246,7 +246,7 @@ int ps_wind_synthetic_flux(const ps_config *cfg, const ps_wind *w,
   memset(fr, 0, (size_t)na * nc * sizeof(double));
   memset(ft, 0, (size_t)na * nc * sizeof(double));
   memset(fp, 0, (size_t)na * nc * sizeof(double));
-  l_uv = w->l_star * w->f_uv;
+  l_uv = w->l_star * w->frac_uv;
   for (j = ng; j < n1 - ng; j++) {
     a = (int)floor(x2[j] / (2 * W_PI / 36));
     if (a < 0 || a >= na) continue;
@@ -279,7 +279,7 @@ int ps_wind_synthetic_flux_dense(const ps_config *cfg, const ps_wind *w, const d
   memset(fr, 0, (size_t)na * nc * sizeof(double));
   memset(ft, 0, (size_t)na * nc * sizeof(double));
   memset(fp, 0, (size_t)na * nc * sizeof(double));
-  l_uv = w->l_star * w->f_uv;
+  l_uv = w->l_star * w->frac_uv;
   /* the rounded values depend on the column i and the bin offset d only:
    * tabulate them once per column (d in [-(na-1), na-1]) */
   const int nd = 2 * na - 1;
