@@ -69,6 +69,7 @@ def lib():
         L.or_set_time.argtypes = [P, D, D, ctypes.c_long]
         L.or_history.argtypes = [P, DP, DP, I]
         L.or_init_wind.argtypes = [P]
+        L.or_wind_reset.argtypes = [P]
         L.or_set_flux.argtypes = [P, I, DP, DP, DP]
         L.or_set_mfit.argtypes = [P, I, DP, DP]
         L.or_cooling.argtypes = [P, D, D]
@@ -266,18 +267,27 @@ class Oracle:
         return a[:, 0] if self.dims == 2 else a
 
 
+WIND_BC = ["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"]
+# the production problem (Test_Problems/LineDrivenWind/cv_idl): X2-beg is
+# its hybrid user side (pluto_sirocco_sub.py:78-81)
+CVIDL_BC = ["userdef", "outflow", "userdef", "reflective", "outflow", "outflow"]
+
+
 def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, char_limiting=0,
                 shock_flattening=0, solver="hll", entropy_switch=0, mfit=False, ode_cooling=0,
-                dense_flux=False, **params):
+                dense_flux=False, bc=None, initial=None, **params):
     """The 2-D spherical line-driven disk wind (PLM van Leer, HLL, RK2,
     userdef/outflow/axisymmetric/reflective boundaries, point-mass gravity,
     floors, BLONDIN cooling and the line force), initialised.  mfit: the
-    tabulated force multiplier (KRAD = ALPHARAD = 999, synthetic table)."""
+    tabulated force multiplier (KRAD = ALPHARAD = 999, synthetic table).
+    bc: the six boundary codes (default WIND_BC).  initial: active-cell
+    state [nv][j][i] to start from instead of this problem's Init (the
+    reference's own first snapshot of another problem)."""
     if mfit:
         params = dict(params, krad=999.0, alpharad=999.0)
     o = Oracle(dims=2, nx=(nr, nt, 1), nvar=7 if entropy_switch else 6, limiter="vl",
                solver=solver,
-               bc=["userdef", "outflow", "axisymmetric", "reflective", "outflow", "outflow"],
+               bc=bc or WIND_BC,
                cfl=cfl, cfl_max_var=1.1, tstop=1e10, first_dt=first_dt,
                cooling=2 if (cooling and ode_cooling) else cooling, geometry=3, gridtype=WIND_GRID["gridtype"], xbeg=WIND_GRID["xbeg"],
                xend=WIND_GRID["xend"], body_force=1, line_force=line_force, floors=1,
@@ -291,6 +301,11 @@ def wind_oracle(nr=64, nt=32, cooling=1, line_force=1, cfl=0.4, first_dt=1e-4, c
     if mfit:   # KRAD = ALPHARAD = 999: the tabulated force multiplier
         o.set_mfit(*synthetic_mfit(o.grid(0), o.grid(1), o.ntot, ngh=o.ngh[0]))
     o.init_wind()
+    if initial is not None:
+        g = o.ngh[0]
+        init = np.asarray(initial)
+        o.V[:init.shape[0], 0, g:-g, g:-g] = init
+        lib().or_wind_reset(o.s)
     return o
 
 

@@ -519,6 +519,17 @@ void or_init_wind(or_sim *s)
     wind_init_point(s, v, s->xgc[0][i], s->xgc[1][j]);
     for (nv = 0; nv < s->c.nvar; nv++) s->V[nv * nc + cidx(s, k, j, i)] = v[nv];
   }
+  or_wind_reset(s);
+}
+
+/* The start of a wind run from the state in s->V (set by or_init_wind, or
+ * by the caller, e.g. the reference's own initial snapshot of a problem
+ * whose Init this oracle does not restate): read_sirocco_heatcool(flag = 0)
+ * and Startup's ComputeEntropy. */
+void or_wind_reset(or_sim *s)
+{
+  int i, j, k;
+  size_t nc = (size_t)s->ntot[0] * s->ntot[1] * s->ntot[2];
   /* read_sirocco_heatcool(flag = 0): frozen xi and radiation temperature */
   for (k = s->beg[2]; k <= s->end[2]; k++)
   for (j = s->beg[1]; j <= s->end[1]; j++)
@@ -665,6 +676,23 @@ static void boundary(or_sim *s)
         src[0] = s->beg[0];
         val = s->V[vidx(s, nv, src[2], src[1], src[0])];
         if (nv == VX1) val = MIND(val, 0.0);
+        s->V[vidx(s, nv, k, j, i)] = val;
+        continue;
+      } else if (type == OR_BC_USERDEF && side == 1) {
+        /* production wind, X1_END: copy the last active cell, outflow only
+         * (Test_Problems/LineDrivenWind/cv_idl/init.c:331-340) */
+        src[0] = s->end[0];
+        val = s->V[vidx(s, nv, src[2], src[1], src[0])];
+        if (nv == VX1) val = MAXD(val, 0.0);
+        s->V[vidx(s, nv, k, j, i)] = val;
+        continue;
+      } else if (type == OR_BC_USERDEF && side == 2) {
+        /* production wind, X2_BEG: every variable from the mirrored active
+         * row, v_theta times -1, then density and pressure from the first
+         * active row (cv_idl/init.c:343-356) */
+        src[1] = (nv == RHO || nv == PRS) ? s->beg[1] : 2 * s->beg[1] - 1 - j;
+        val = s->V[vidx(s, nv, src[2], src[1], src[0])];
+        if (nv == VX2) val *= -1.0;
         s->V[vidx(s, nv, k, j, i)] = val;
         continue;
       } else {

@@ -93,6 +93,9 @@ void    or_init_blast(or_sim *s, double p_amb, double p_in, double r_in,
  * on every cell of the total box at the volume centroids, as Startup does)
  * followed by read_sirocco_heatcool(flag = 0): frozen xi and T_r. */
 void    or_init_wind(or_sim *s);
+/* The frozen xi / T_r and the entropy of the state the caller put in the
+ * context (read_sirocco_heatcool(flag = 0), Startup's ComputeEntropy). */
+void    or_wind_reset(or_sim *s);
 
 /* Directional UV fluxes, [angle][k][j][i] over the total box, for the
  * line force (flux_r_UV / flux_t_UV / flux_p_UV, Src/globals.h:191-210). */

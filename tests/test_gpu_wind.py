@@ -253,6 +253,54 @@ def test_wind_full_physics_close_to_reference(built):
         rl1 = _rel_l1(a, snaps[k])
         report.append((step, rl1))
         print("step", step, "rel L1 per variable", rl1)
-    # the first 20 steps stay within a few ulps of the reference
-    assert np.all(report[1][1] < 1e-11), report[1]
-    assert np.all(report[-1][1] < 1e-2), report[-1]
+    # every snapshot (steps 20, 100, 200) within 1e-11 of the reference:
+    # measured 4e-13, 2.4e-13 and 8e-13; at this size the flow is not
+    # sensitive (the oracle perturbed by 1e-15 moves 1.4e-12 by step 200)
+    for step, rl1 in report:
+        assert np.all(rl1 <= 1e-11), (step, rl1)
+
+
+def test_production_problem_hooks_match_reference(built):
+    """The production disk-wind problem's own hooks (cv_idl/init.c compiled by
+    the reference build: floors, X1-beg inflow copy, X2-beg hybrid condition
+    -- reflected velocities, density and pressure copied -- and gravity) with
+    its numerics (characteristic PLM, MULTID, entropy switch, BLONDIN, line
+    force), started from the reference's own first snapshot: every snapshot
+    through step 100 within 1e-11 (the oracle perturbed by 1e-15 moves 2e-15
+    by then)."""
+    import psgb
+    meta = _case("wind2d_cvidl")
+    snaps = np.load(meta["npz"])["snaps"]
+    nr, nt = meta["n"][0], meta["n"][1]
+    cfg = psgb.make_wind_config(nr, nt, cooling=1, char_limiting=1, shock_flattening=1,
+                                entropy_switch=2, bc=psgb.CVIDL_BC)
+    w = psgb.make_wind(line_force=1)
+    g = psgb.WindGrid(cfg)
+    ng = psgb.nghost(cfg)
+    V = np.zeros((cfg.nvar, 1, g.ntot[1], g.ntot[0]))
+    V[:6, 0, ng:-ng, ng:-ng] = snaps[0]     # ghosts come from the first Boundary
+    s = psgb.Solver(cfg, g)
+    s.set_state(V)
+    s.set_time(0.0, 1e-4, 0)
+    s.set_wind(w, psgb.wind_flux(cfg, w, g))
+    done = 0
+    for k, step in enumerate(meta["snap_steps"]):
+        if step > done:
+            s.run(step - done)
+            done = step
+        a = _active(s.get_state(), ng)
+        r = assert_hydro_close(a, snaps[k], f"step {step}")
+        print("production hooks, step", step, "relative L1 per variable", r)
+        t, dt, _, _ = s.time()
+        assert abs(t - float(meta["t"][k])) <= 6e-7 * max(t, 1e-300)
+        assert abs(dt - float(meta["dt"][k])) <= 6e-7 * dt
+    # the X2-beg user side differs from the axisymmetric one of the test
+    # problem: run with that instead and the state moves
+    cfg2 = psgb.make_wind_config(nr, nt, cooling=1, char_limiting=1, shock_flattening=1,
+                                 entropy_switch=2)
+    s2 = psgb.Solver(cfg2, g)
+    s2.set_state(V)
+    s2.set_time(0.0, 1e-4, 0)
+    s2.set_wind(w, psgb.wind_flux(cfg2, w, g))
+    s2.run(20)
+    assert not np.allclose(_active(s2.get_state(), ng), snaps[1], rtol=1e-9, atol=0)
