@@ -15,9 +15,11 @@
  * one of oracle.synthetic_flux: L_UV / (4 pi r^2) in the bin
  * floor(theta / (2 pi / 36)) of the radial file, zero elsewhere and in the
  * theta and phi files.  x1, x2 are the cell-centre arrays of the total box
- * (x1 in code units), ngh the ghost zones per side. */
+ * (x1 in code units), ngh the ghost zones per side; bit a of `axes` selects
+ * the file of axis a (r, theta, phi). */
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #define OR_PI 3.14159265358979323846
@@ -27,8 +29,9 @@ static int write_one(const char *path, int axis, int nr, int nt, const double *x
 {
   FILE *f = fopen(path, "w");
   if (!f) return -1;
-  static char buf[1 << 20];
-  setvbuf(f, buf, _IOFBF, sizeof(buf));
+  /* a buffer of the call's own: several threads write files at once */
+  char *buf = malloc(1 << 20);
+  if (buf) setvbuf(f, buf, _IOFBF, 1 << 20);
   fprintf(f, "# synthetic directional UV flux\n# nangles %d\n", na);
   static const char zero[] = " 0.000000000000e+00";
   for (int j = ngh; j < nt + ngh; j++) {
@@ -45,16 +48,19 @@ static int write_one(const char *path, int axis, int nr, int nt, const double *x
       fputc('\n', f);
     }
   }
-  return fclose(f) == 0 ? 0 : -1;
+  const int rc = fclose(f) == 0 ? 0 : -1;
+  free(buf);
+  return rc;
 }
 
 int or_write_wind_flux(const char *dir, int nr, int nt, const double *x1, const double *x2,
-                       int ngh, double l_uv, double unit_length, int na)
+                       int ngh, double l_uv, double unit_length, int na, int axes)
 {
   static const char *names[3] = {"directional_flux_r.dat", "directional_flux_theta.dat",
                                  "directional_flux_phi.dat"};
   char path[4096];
   for (int ax = 0; ax < 3; ax++) {
+    if (!(axes & (1 << ax))) continue;
     if (snprintf(path, sizeof(path), "%s/%s", dir, names[ax]) >= (int)sizeof(path)) return -1;
     if (write_one(path, ax, nr, nt, x1, x2, ngh, l_uv, unit_length, na)) return -1;
   }

@@ -147,31 +147,50 @@ def _num(v):
     return repr(float(v))
 
 
-def prepare_wind(wd, nr, nt, l_star=1.0e37, krad=0.2, alpharad=-0.6, solver="hll",
-                 every=-1, log=1, flux=True):
-    """pluto.ini (and the single-bin synthetic flux files) of one wind model."""
+FLUX_FILES = ("directional_flux_r.dat", "directional_flux_theta.dat", "directional_flux_phi.dat")
+
+
+def write_wind_flux(wd, nr, nt, l_star, axes=7):
+    """The single-bin synthetic flux files of a wind grid (bit a of axes:
+    the file of axis a), written by liboracle from the oracle's grid."""
     import numpy as np
     from oracle import WIND, WIND_GRID, NANGLES, Oracle, lib
+    o = Oracle(dims=2, nx=(nr, nt, 1), nvar=6, geometry=3, gridtype=WIND_GRID["gridtype"],
+               xbeg=WIND_GRID["xbeg"], xend=WIND_GRID["xend"])
+    x1, x2 = (np.ascontiguousarray(o.grid(d)) for d in (0, 1))
+    dp = ctypes.POINTER(ctypes.c_double)
+    L = lib()
+    L.or_write_wind_flux.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp, dp,
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_int, ctypes.c_int]
+    rc = L.or_write_wind_flux(os.fsencode(wd), nr, nt, x1.ctypes.data_as(dp),
+                              x2.ctypes.data_as(dp), o.ngh[0], float(l_star) * WIND["f_uv"],
+                              WIND["unit_length"], NANGLES, axes)
+    if rc:
+        raise OSError("could not write the flux files in " + wd)
+
+
+def prepare_wind(wd, nr, nt, l_star=1.0e37, krad=0.2, alpharad=-0.6, solver="hll",
+                 every=-1, log=1, flux=True, shared=None):
+    """pluto.ini (and the single-bin synthetic flux files) of one wind model.
+    shared: a directory holding this grid's theta and phi files (all zero
+    for the single-bin flux, whatever L_x), linked instead of written."""
     os.makedirs(wd, exist_ok=True)
     with open(os.path.join(wd, "pluto.ini"), "w") as f:
         f.write(WIND_INI.format(nr=nr, nt=nt, every=every, log=log, solver=solver,
                                 l_star=_num(l_star), krad=_num(krad), alpharad=_num(alpharad)))
     if not flux:
         return
-    o = Oracle(dims=2, nx=(nr, nt, 1), nvar=6, geometry=3, gridtype=WIND_GRID["gridtype"],
-               xbeg=WIND_GRID["xbeg"], xend=WIND_GRID["xend"])
-    x1, x2 = o.grid(0), o.grid(1)
-    dp = ctypes.POINTER(ctypes.c_double)
-    L = lib()
-    L.or_write_wind_flux.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp, dp,
-                                     ctypes.c_int, ctypes.c_double, ctypes.c_double,
-                                     ctypes.c_int]
-    x1, x2 = (np.ascontiguousarray(a) for a in (x1, x2))
-    rc = L.or_write_wind_flux(os.fsencode(wd), nr, nt, x1.ctypes.data_as(dp),
-                              x2.ctypes.data_as(dp), o.ngh[0], float(l_star) * WIND["f_uv"],
-                              WIND["unit_length"], NANGLES)
-    if rc:
-        raise OSError("could not write the flux files in " + wd)
+    if shared:
+        # the radial file too when the shared directory holds one (replicas
+        # of one model)
+        own_r = not os.path.exists(os.path.join(shared, FLUX_FILES[0]))
+        for name in FLUX_FILES[1 if own_r else 0:]:
+            os.symlink(os.path.join(shared, name), os.path.join(wd, name))
+        if own_r:
+            write_wind_flux(wd, nr, nt, l_star, axes=1)
+    else:
+        write_wind_flux(wd, nr, nt, l_star)
 
 
 def prepare_blast(wd, nx, ny, nz=1, solver="hllc", bc="outflow", cfl=0.4, tstop=10.0,
@@ -234,10 +253,12 @@ def run_timed(exe, wd, steps, skip, timeout=3600.0):
 
 
 def run_many(jobs, workers):
-    """jobs: (exe, wd, steps, skip, cells) tuples; at most `workers` reference
-    processes at a time, the largest first.  Returns the per-job
-    (timed seconds, rc, wall) in the order given and the wall time of all."""
-    order = sorted(range(len(jobs)), key=lambda k: -jobs[k][4])
+    """jobs: (prepare, exe, wd, steps, skip, cells) tuples; at most `workers`
+    reference processes at a time, the largest first; each job's directory
+    is made by prepare() just before its run and removed after it.  Returns
+    the per-job (timed seconds, rc, wall) in the order given and the wall
+    time of all."""
+    order = sorted(range(len(jobs)), key=lambda k: -jobs[k][5])
     res = [None] * len(jobs)
     lock = threading.Lock()
     nxt = [0]
@@ -249,8 +270,14 @@ def run_many(jobs, workers):
                     return
                 k = order[nxt[0]]
                 nxt[0] += 1
-            exe, wd, steps, skip, _ = jobs[k]
-            res[k] = run_timed(exe, wd, steps, skip)
+            prepare, exe, wd, steps, skip, _ = jobs[k]
+            try:
+                prepare()
+                res[k] = run_timed(exe, wd, steps, skip)
+            except Exception as e:   # reported as a failed run
+                res[k] = (None, repr(e), 0.0)
+            finally:
+                clean(wd)
 
     t0 = time.perf_counter()
     th = [threading.Thread(target=worker) for _ in range(max(1, workers))]

@@ -47,7 +47,7 @@ def test_sirocco_data_matches_oracle(built):
         done = step
         r = rel_l1(s.get_state()[:, 0, 2:-2, 2:-2], o.active())
         print("step", step, "t", s.time()[0], "relative L1 per variable", r)
-        assert np.all(r <= 1e-8), r
+        assert np.all(r <= 1e-11), r   # measured 1e-13 (v_theta) at most through step 80
     # the data matter: without prefactors the state differs
     plain = psgb_plain = None
     import psgb
@@ -70,3 +70,40 @@ def test_surrogate_leaves_prefactor_cells_to_the_reference(built):
     assert np.array_equal(a.get_state(), b.get_state())
     st = sg.stats()
     assert st[0] == 0 and st[2] > 0
+
+
+def test_sirocco_data_matches_reference(built, tmp_path):
+    """The same path against the reference itself: restarted at t = 3.5 from
+    its initial dump with py_heatcool.dat and prefactors.dat present (the
+    files tests/golden/make_golden.py writes, read here by this library's
+    readers), every snapshot through step 80 within 1e-11."""
+    import json
+    import os
+    import psgb
+    from conftest import GOLDEN
+    from make_golden import write_sirocco_files
+    meta = json.load(open(os.path.join(GOLDEN, "wind2d_sirocco_64x32.json")))
+    snaps = np.load(os.path.join(GOLDEN, "wind2d_sirocco_64x32.npz"))["snaps"]
+    nr, nt = meta["n"][0], meta["n"][1]
+    write_sirocco_files(str(tmp_path), nr, nt, snaps[0][0], seed=meta["sirocco_seed"])
+    cfg = psgb.make_wind_config(nr, nt)
+    g = psgb.WindGrid(cfg)
+    n0, n1 = nr + 4, nt + 4
+    xi, tr = np.zeros((1, n1, n0)), np.zeros((1, n1, n0))
+    pre = np.ones((6, 1, n1, n0))
+    assert psgb.read_sirocco_heatcool(cfg, g, str(tmp_path / "py_heatcool.dat"), xi[0],
+                                      tr[0]) == nr * nt
+    assert psgb.read_sirocco_prefactors(cfg, g, str(tmp_path / "prefactors.dat"),
+                                        pre[:, 0]) == nr * nt
+    s = _gpu(xi, tr, pre)
+    s.set_time(meta["t0"], 1e-4, 0)
+    done = 0
+    for k, step in enumerate(meta["snap_steps"]):
+        if step > done:
+            s.run(step - done)
+            done = step
+        r = rel_l1(s.get_state()[:, 0, 2:-2, 2:-2], snaps[k])
+        print("SIROCCO data vs reference, step", step, "relative L1 per variable", r)
+        assert np.all(r <= 1e-11), (step, r)
+        t, dt, _, _ = s.time()
+        assert abs(t - float(meta["t"][k])) <= 6e-7 * t

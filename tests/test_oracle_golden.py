@@ -58,16 +58,27 @@ def test_wind_oracle_matches_reference(built, meta):
     tracer, userdef boundary and floors, gravity and (full case) BLONDIN
     cooling with the Strang alternation and the line force: bit-exact at
     every stored snapshot."""
-    from oracle import wind_oracle
+    from oracle import CVIDL_BC, wind_oracle
     snaps = np.load(meta["npz"])["snaps"]
     nr, nt = meta["n"][0], meta["n"][1]
+    # the production problem starts from the reference's own first snapshot
+    # (its Init is not restated); its boundaries are its user sides
+    cvidl = bool(meta.get("cvidl", 0))
     o = wind_oracle(nr, nt, cooling=meta["cooling"], line_force=meta["line_force"],
+                    bc=CVIDL_BC if cvidl else None, initial=snaps[0] if cvidl else None,
                     char_limiting=meta.get("char_limiting", 0),
                     shock_flattening=meta.get("shock_flattening", 0),
                     solver=meta.get("solver", "hll"),
                     entropy_switch=meta.get("entropy_switch", 0), mfit=bool(meta.get("mfit", 0)),
                     ode_cooling=meta.get("ode_cooling", 0),
                     dense_flux=bool(meta.get("dense_flux", 0)))
+    if "sirocco_seed" in meta:
+        # restarted at t0 with the SIROCCO data files (make_golden.run_sirocco_case)
+        from make_golden import sirocco_as_read
+        from oracle import lib as olib
+        xi, tr, pre = sirocco_as_read(nr, nt, meta["sirocco_seed"])
+        o.set_sirocco(xi[None], tr[None], pre[:, None])
+        olib().or_set_time(o.s, meta["t0"], 1e-4, 0)
     done = 0
     for k, step in enumerate(meta["snap_steps"]):
         if step > done:
