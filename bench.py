@@ -69,6 +69,7 @@ IDL_NUMERICS = dict(char_limiting=1, shock_flattening=1, entropy_switch=2)
 
 class Workload:
     def __init__(self, name, numerics="plm", flux="radial"):
+        self.groups = 0
         self.name = name
         self.numerics = numerics
         self.flux = flux
@@ -608,6 +609,8 @@ def batch_bench(wl, steps, warmup, rank, world):
     # batched form, reference cooling
     solvers, V0s = make()
     batch = psgb.Batch(solvers)
+    if wl.groups:
+        batch.set_groups(wl.groups)
     batch.set_stream(stream.cuda_stream)
     t_tune = time.perf_counter()
     batch.autotune(reps=5)
@@ -670,6 +673,7 @@ def batch_bench(wl, steps, warmup, rank, world):
                             "perturbation of its initial state (the full-physics 512x256 "
                             "wind after 100 steps); the learned step changes the pressure only",
                    "tile_shapes": shapes, "autotune_s": t_tune,
+                   "groups": wl.groups or 1,
                    "line_force": _line_force_figures(wl),
                    "l2": "256 MiB buffer written before every timed step (L2 flushed)",
                    "parallelism": "replicas only" if world > 1 else "single GPU"},
@@ -1040,6 +1044,9 @@ def main():
     ap.add_argument("--numerics", default="plm", choices=["plm", "idl"],
                     help="batch workload: primitive PLM (default) or the production cv_idl "
                          "limiting (characteristic PLM, MULTID, entropy switch)")
+    ap.add_argument("--groups", type=int, default=0,
+                    help="batch workload: model groups run as parallel graph branches "
+                         "(ps_batch_set_groups; 0: the library's default)")
     ap.add_argument("--flux", default="radial", choices=["radial", "dense"],
                     help="batch workload: UV flux in each cell's radial bin (default) or in "
                          "all 36 bins")
@@ -1047,6 +1054,7 @@ def main():
     if (a.numerics != "plm" or a.flux != "radial") and a.workload != "batch":
         ap.error("--numerics and --flux are offered for the batch workload")
     wl = Workload(a.workload, a.numerics, a.flux)
+    wl.groups = a.groups
     if a.workload == "cube" and a.cube_n != 512:
         wl.nx = wl.ny = wl.nz = a.cube_n
         wl.cells = a.cube_n ** 3

@@ -348,10 +348,10 @@ int  ps_batch_get_states(ps_batch *b, double *const *Vc);
 int  ps_batch_set_states_async(ps_batch *b, const double *const *Vc);
 int  ps_batch_get_states_async(ps_batch *b, double *const *Vc);
 int  ps_batch_set_stream(ps_batch *b, void *stream);
-/* The models are dealt out by size into ngroups groups (default 4 for 16
- * models or more, else 1) whose steps run as parallel branches of the step
- * graph, so that one group's short, latency-bound kernels overlap the
- * others' stage kernels.  Results do not depend on it. */
+/* The models are dealt out by size into ngroups groups (default 1) whose
+ * steps run as parallel branches of the step graph, so that one group's
+ * short, latency-bound kernels can overlap the others' stage kernels.
+ * Results do not depend on it. */
 int  ps_batch_set_groups(ps_batch *b, int ngroups);
 long ps_batch_launch_count(const ps_batch *b);
 /* Tile shape of the stage kernels per model: 0 = 32x8, 1 = 16x16,

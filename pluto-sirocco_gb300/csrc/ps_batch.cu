@@ -544,9 +544,11 @@ static void batch_free(ps_batch *b)
   delete b;
 }
 
-// Default number of model groups: 4 when the batch has at least 16 models
-// (measured on the 64-model benchmark batch), else 1.
-static int default_groups(int n) { return n >= 16 ? 4 : 1; }
+// Default number of model groups: 1.  On the 64-model benchmark batch four
+// groups measured the same step time as one (14.73 against 14.76 ms): the
+// stage kernels fill the GPU either way, and the learned step's kernels,
+// split four ways, pay four set-ups and tails where one group pays one.
+static int default_groups(int) { return 1; }
 
 extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
 {
