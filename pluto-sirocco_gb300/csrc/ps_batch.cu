@@ -31,13 +31,12 @@ template <int NV>
 __global__ void k_batch_bnd_x1(const BatchModel *__restrict__ models,
                                const BlockItem *__restrict__ blocks, int stage)
 {
+  // a 256-cell block of the list per 64-thread CTA, 4 cells per thread
   const BlockItem bi = blocks[blockIdx.x];
   const WindStageArgs &A = models[bi.m].st[0];
   if (A.s.sc->done) return;
-  const int q = bi.b * blockDim.x + threadIdx.x;
-  if (q < A.s.p.nx[0] * A.s.p.nx[1])
-    bnd_x1_cell<NV>(stage == 1 ? const_cast<double *>(A.s.Vn) : A.s.Vout, A.s.Us, A.s.p, A.w,
-                    stage, q);
+  bnd_x1_cells<NV, 4>(stage == 1 ? const_cast<double *>(A.s.Vn) : A.s.Vout, A.s.Us, A.s.p, A.w,
+                      stage, bi.b * 256 + threadIdx.x, 64, A.s.p.nx[0] * A.s.p.nx[1]);
 }
 
 template <int NV>
@@ -397,10 +396,10 @@ static int batch_bnd(ps_batch *b, BatchGroup &g, int stage, cudaStream_t st)
 {
   if (g.models.empty()) return 0;
   if (b->nvar == 7) {
-    ps::k_batch_bnd_x1<7><<<g.ncells_blocks, 256, 0, st>>>(b->d_models, g.d_cells, stage);
+    ps::k_batch_bnd_x1<7><<<g.ncells_blocks, 64, 0, st>>>(b->d_models, g.d_cells, stage);
     ps::k_batch_bnd_x2<7><<<g.nx2_blocks, 256, 0, st>>>(b->d_models, g.d_x2, stage);
   } else {
-    ps::k_batch_bnd_x1<6><<<g.ncells_blocks, 256, 0, st>>>(b->d_models, g.d_cells, stage);
+    ps::k_batch_bnd_x1<6><<<g.ncells_blocks, 64, 0, st>>>(b->d_models, g.d_cells, stage);
     ps::k_batch_bnd_x2<6><<<g.nx2_blocks, 256, 0, st>>>(b->d_models, g.d_x2, stage);
   }
   b->launches += 2;

@@ -63,6 +63,7 @@ extern "C" int ps_set_cooling(ps_ctx *c, const ps_cooling *cp)
   W.unit_pressure = cp->unit_density * cp->unit_velocity * cp->unit_velocity;
   W.unit_time = cp->unit_length / cp->unit_velocity;
   W.xi_const = cp->xi;
+  ps::set_sg_units(W, c->cfg.gamma);
   c->cool_on = 1;
   ps_ctx_invalidate_graphs(c);
   return 0;

@@ -65,6 +65,14 @@ __device__ __forceinline__ bool gt_pos(double x)
   return (unsigned long long)__double_as_longlong(x) - (CBITS + 1ull) <
          0x7FF0000000000000ull - CBITS;
 }
+// x < c for a positive finite c known only at run time: the patterns of
+// +0..c (exclusive) and those of -0..-inf
+__device__ __forceinline__ bool lt_pos(double x, double c)
+{
+  const unsigned long long u = __double_as_longlong(x);
+  return u < (unsigned long long)__double_as_longlong(c) ||
+         u - 0x8000000000000000ull <= 0x7FF0000000000000ull;
+}
 __device__ __forceinline__ double nn_max(double a, double b)
 {
   const unsigned long long x = __double_as_longlong(a), y = __double_as_longlong(b);

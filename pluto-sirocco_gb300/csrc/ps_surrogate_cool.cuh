@@ -50,9 +50,9 @@ __device__ __forceinline__ int sg_decide(SgCtx &b, double T, bool inbox, float y
   evals = 0;
   stiff = false;
   if (!inbox) return SG_OUT_OF_BOX;
-  // xi^-1/2 by one reciprocal square root, xi^1/4 as sqrt(xi xi^-1/2)
+  // xi^-1/2 and xi^1/4 = (xi^-1/2)^-1/2 by two reciprocal square roots
   b.isqxi = rsqrt(b.xi);
-  b.sqsqxi = sqrt(b.xi * b.isqxi);
+  b.sqsqxi = rsqrt(b.isqxi);
   T0 = T * (double)exp10f(4.0f * y);
   return sg_judge(b, T, T0, use_net != 0, T_f, evals, stiff);
 }
@@ -88,24 +88,17 @@ struct SgCoolArgs {
   Scalars *sc;
 };
 
-// Unit conversions of the learned step (the exact path's divisions by
-// constants folded into factors): E = p e_of_p, n_H = rho nh_of_rho,
-// n = rho n_of_rho, T = (p / rho) t_of_pr, p_new = T_new n p_of_tn
-// (p, rho in code units; cooling.c:95-162).
+// Unit conversions of the learned step (set_sg_units, with the
+// parameters): E = p e_of_p, n_H = rho nh_of_rho, n = rho n_of_rho,
+// T = (p / rho) t_of_pr, p_new = T_new n p_of_tn.
 struct SgUnits {
   double e_of_p, nh_of_rho, n_of_rho, t_of_pr, p_of_tn;
 };
 
 __device__ __forceinline__ SgUnits sg_units(const SgCoolArgs &A)
 {
-  SgUnits u;
-  const double gm1 = A.p.gamma - 1.0;
-  u.e_of_p = A.w.unit_pressure / gm1;
-  u.nh_of_rho = A.w.unit_density / (1.43 * kMP);
-  u.n_of_rho = A.w.unit_density / (A.w.mu * kMP);
-  u.t_of_pr = u.e_of_p / (1.5 * u.n_of_rho * kKB);
-  u.p_of_tn = 1.5 * kKB * gm1 / A.w.unit_pressure;
-  return u;
+  return SgUnits{A.w.sg_e_of_p, A.w.sg_nh_of_rho, A.w.sg_n_of_rho, A.w.sg_t_of_pr,
+                 A.w.sg_p_of_tn};
 }
 
 // The cell's quantities for the learned step.  Returns 0 (below 1e4 K:

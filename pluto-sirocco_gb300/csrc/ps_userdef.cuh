@@ -34,28 +34,35 @@ namespace ps {
 
 // side 0: density and pressure floors of one cell's primitive state;
 // returns true if the cell was repaired (its conservative state then has to
-// be formed again, PrimToCons3D of the problem's loop)
+// be formed again, PrimToCons3D of the problem's loop).
+//
+// The problem's loop keeps the sound speed: cs = sqrt(gamma p / rho),
+// p' = cs^2 dfloor / gamma, T = p' / dfloor KELVIN mu, and at T < tfloor
+// p' = dfloor tfloor / (KELVIN mu), which is pfloor.  Algebraically
+// p' = (p / rho) dfloor and T = (p / rho) KELVIN mu: one division in place
+// of a square root and four divisions (the FP64 pipe bounds this pass, and
+// most cells of the wind sit at the density floor), within 2 ulp of the
+// loop's sequence.  The threshold tests run on the bit patterns.
 template <int NV>
 __device__ __forceinline__ bool UserDefBoundary_Internal(double (&v)[NV], const WindParams &w,
                                                          double gamma)
 {
+  (void)gamma;
   bool convert = false;
-  const double K = w.kelvin, mu = w.mu;
-  if (v[RHO] < w.dfloor) {
-    if (v[RHO] < 0.0) v[RHO] = w.dfloor;
-    const double cs = sqrt(gamma * v[PRS] / v[RHO]);
-    const double dfact = v[RHO] / w.dfloor;
+  if (lt_pos(v[RHO], w.dfloor)) {
+    const bool neg = lt0(v[RHO]);
+    const double rho = neg ? w.dfloor : v[RHO];
+    const double pr = v[PRS] / rho;
+    const double dfact = neg ? 1.0 : rho * w.inv_dfloor;
     v[RHO] = w.dfloor;
     v[VX1] = dfact * v[VX1];
     v[VX2] = dfact * v[VX2];
     v[VX3] = dfact * v[VX3];
-    v[PRS] = cs * cs * v[RHO] / gamma;
-    const double temp = v[PRS] / v[RHO] * K * mu;
-    if (temp < w.tfloor) v[PRS] = v[RHO] * w.tfloor / (K * mu);
+    v[PRS] = lt_pos(pr * w.kmu, w.tfloor) ? w.pfloor : pr * w.dfloor;
     if constexpr (NV > NFLX) v[NFLX] = 0.0;
     convert = true;
   }
-  if (v[PRS] < w.pfloor) {
+  if (lt_pos(v[PRS], w.pfloor)) {
     v[PRS] = w.pfloor;
     convert = true;
   }

@@ -41,10 +41,9 @@ template <int NV>
 __global__ void k_wind_bnd_x1(double *V, double *Us, const Params p, const WindParams w,
                               Scalars *sc, int stage)
 {
+  // 256 cells per 64-thread CTA, 4 cells per thread
   if (sc->done) return;
-  const int n = p.nx[0] * p.nx[1];
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
-    bnd_x1_cell<NV>(V, Us, p, w, stage, q);
+  bnd_x1_cells<NV, 4>(V, Us, p, w, stage, blockIdx.x * 256 + threadIdx.x, 64, p.nx[0] * p.nx[1]);
 }
 
 template <int NV>
@@ -394,6 +393,8 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   W.dfloor = wp->dfloor / UD;
   W.tfloor = 5.e2;
   W.pfloor = W.dfloor * W.tfloor / (W.kelvin * W.mu);
+  W.inv_dfloor = 1.0 / W.dfloor;
+  W.kmu = W.kelvin * W.mu;
   W.krad = wp->krad;
   W.alpharad = wp->alpharad;
   W.sigma_e = ps::kSigmaT / ps::kAmu / 1.18;
@@ -402,6 +403,7 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
   W.t_x = wp->t_x;
   W.unit_pressure = UD * UV * UV;
   W.unit_time = UL / UV;
+  ps::set_sg_units(W, c->cfg.gamma);
   {
     // t = sigma_e rho_cgs v_th / (dv/ds), v_th = sqrt(2 kB T / m_p),
     // T = p / rho KELVIN mu  =>  t = C sqrt(rho p) / (dv/ds) in code units
@@ -461,10 +463,10 @@ int ps_wind_bnd_launch(ps_ctx *c, int stage)
   const int nb2 = (p.ntot[0] * 2 * p.beg[1] + 255) / 256;
   double *Vin = stage == 1 ? c->V : c->Vs;
   if (p.nvar == 7) {
-    ps::k_wind_bnd_x1<7><<<nb, 256, 0, c->stream>>>(Vin, c->Us, p, w->a.w, c->sc, stage);
+    ps::k_wind_bnd_x1<7><<<nb, 64, 0, c->stream>>>(Vin, c->Us, p, w->a.w, c->sc, stage);
     ps::k_wind_bnd_x2<7><<<nb2, 256, 0, c->stream>>>(Vin, p, c->sc);
   } else {
-    ps::k_wind_bnd_x1<6><<<nb, 256, 0, c->stream>>>(Vin, c->Us, p, w->a.w, c->sc, stage);
+    ps::k_wind_bnd_x1<6><<<nb, 64, 0, c->stream>>>(Vin, c->Us, p, w->a.w, c->sc, stage);
     ps::k_wind_bnd_x2<6><<<nb2, 256, 0, c->stream>>>(Vin, p, c->sc);
   }
   c->launches += 2;

@@ -3,6 +3,7 @@
 // force, and the problem parameters (units, gravity, floors, cooling).
 #pragma once
 
+#include "ps_blondin.cuh"
 #include "ps_hydro.cuh"
 
 namespace ps {
@@ -62,6 +63,7 @@ struct WindParams {
   double unit_density, unit_length, unit_velocity;
   double mu, kelvin;     // KELVIN = UNIT_VELOCITY^2 * amu / kB
   double dfloor, tfloor, pfloor;
+  double inv_dfloor, kmu;   // 1 / dfloor, KELVIN * mu
   double krad, alpharad, sigma_e, unit_acc;
   double lx, t_x;        // L_star*f_x, T_x
   double unit_pressure, unit_time;
@@ -80,7 +82,25 @@ struct WindParams {
   // > 0: BLONDIN at this constant ionisation parameter with T_x (the
   // Cartesian cooling configuration); 0: xi from the state / sirocco_xi
   double xi_const;
+  // the learned cooling step's unit factors, set by set_sg_units
+  double sg_e_of_p, sg_nh_of_rho, sg_n_of_rho, sg_t_of_pr, sg_p_of_tn;
 };
+
+// The learned cooling step's unit conversions, the exact path's divisions by
+// constants folded into factors (cooling.c:95-162): E = p sg_e_of_p,
+// n_H = rho sg_nh_of_rho, n = rho sg_n_of_rho, T = (p / rho) sg_t_of_pr,
+// p_new = T_new n sg_p_of_tn (p, rho in code units).  Formed once on the
+// host with the units, the same products and quotients the device formed
+// per cell before.
+inline void set_sg_units(WindParams &W, double gamma)
+{
+  const double gm1 = gamma - 1.0;
+  W.sg_e_of_p = W.unit_pressure / gm1;
+  W.sg_nh_of_rho = W.unit_density / (1.43 * kMP);
+  W.sg_n_of_rho = W.unit_density / (W.mu * kMP);
+  W.sg_t_of_pr = W.sg_e_of_p / (1.5 * W.sg_n_of_rho * kKB);
+  W.sg_p_of_tn = 1.5 * kKB * gm1 / W.unit_pressure;
+}
 
 struct WindStageArgs {
   StageArgs s;

@@ -211,14 +211,14 @@ __device__ __forceinline__ void cell_of(const Params &p, long long q, int &gi, i
 // Boundary() part 1: the problem's side-0 hook (floors) on the active cells,
 // then the x1 ghost cells of the active rows, each written by the active
 // cell it comes from (user sides through the X1 hooks of ps_userdef.cuh).
+// One active cell q at state index c (column gi, row gj) whose density and
+// pressure the caller loaded.
 template <int NV>
-__device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params &p,
-                                            const WindParams &w, int stage, int q)
+__device__ __forceinline__ void bnd_x1_cell_rp(double *V, double *Us, const Params &p,
+                                               const WindParams &w, int stage, int gi, int gj,
+                                               long long c, double rho, double prs)
 {
   {
-    const int i = q % p.nx[0], j = q / p.nx[0];
-    const int gi = i + p.beg[0], gj = j + p.beg[1];
-    const long long c = vcell(p, gj, gi);
     // density and pressure decide the floors; the other variables are
     // read only for a floored cell or a cell whose x1 ghosts it writes
     // (the first and last active columns, or every column within the ghost
@@ -226,9 +226,9 @@ __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params 
     const int ng = p.beg[0];
     const bool edge = gi < p.beg[0] + ng || gi > p.beg[0] + p.nx[0] - 1 - ng;
     double v[NV];
-    v[RHO] = V[RHO * p.vstride + c];
-    v[PRS] = V[PRS * p.vstride + c];
-    const bool floored = w.floors && (v[RHO] < w.dfloor || v[PRS] < w.pfloor);
+    v[RHO] = rho;
+    v[PRS] = prs;
+    const bool floored = w.floors && (lt_pos(v[RHO], w.dfloor) || lt_pos(v[PRS], w.pfloor));
     if (floored || edge) {
       v[VX1] = V[VX1 * p.vstride + c];
       v[VX2] = V[VX2 * p.vstride + c];
@@ -290,6 +290,35 @@ __device__ __forceinline__ void bnd_x1_cell(double *V, double *Us, const Params 
       }
     }
   }
+}
+
+// K active cells per thread, q0 + k stride (k < K, below n): the densities
+// and pressures of all K are loaded before any is processed, so that a
+// pass in which few cells are floored is not bound by one load latency per
+// cell.
+template <int NV, int K>
+__device__ __forceinline__ void bnd_x1_cells(double *V, double *Us, const Params &p,
+                                             const WindParams &w, int stage, int q0, int stride,
+                                             int n)
+{
+  double rho[K], prs[K];
+  long long c[K];
+  int gi[K], gj[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const int q = q0 + k * stride;
+    if (q < n) {
+      const int j = q / p.nx[0];
+      gi[k] = q - j * p.nx[0] + p.beg[0];
+      gj[k] = j + p.beg[1];
+      c[k] = vcell(p, gj[k], gi[k]);
+      rho[k] = V[RHO * p.vstride + c[k]];
+      prs[k] = V[PRS * p.vstride + c[k]];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++)
+    if (q0 + k * stride < n) bnd_x1_cell_rp<NV>(V, Us, p, w, stage, gi[k], gj[k], c[k], rho[k], prs[k]);
 }
 
 // Boundary() part 2: the x2 ghost rows over every column (x1 ghosts

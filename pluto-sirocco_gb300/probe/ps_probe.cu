@@ -6,7 +6,11 @@
 //                        SM, no memory traffic;
 //   ps_probe_fastmath    the table-driven exp / log of the stage kernels
 //                        (csrc/ps_fastmath.cuh) next to CUDA's on the same
-//                        arguments, for the accuracy test.
+//                        arguments, for the accuracy test;
+//   ps_probe_fp64_lanes  the time of dependent FP64 FMAs in warps with only
+//                        some lanes active (how the cost of a double-
+//                        precision instruction depends on the active lanes,
+//                        for the kernels that run few cells per warp).
 #include "ps_fastmath.cuh"
 
 #include <cuda_runtime.h>
@@ -28,6 +32,25 @@ __global__ void k_fp64_fma_chains(double *out, int iters, double a, double b)
 #pragma unroll
   for (int c = 0; c < kChains; c++) s += x[c];
   if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+// `chains` (1..8) dependent FMA chains per active lane; lanes >= active
+// of every warp return at once
+__global__ void k_fp64_lanes(double *out, int active, int chains, int iters, double a, double b)
+{
+  if ((int)(threadIdx.x & 31) >= active) return;
+  double x[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; c++) x[c] = (double)(threadIdx.x + c) * 1e-3;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+      if (c < chains) x[c] = fma(x[c], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < kChains; c++) s += x[c];
+  if (s == 12345.678) out[0] = s;
 }
 
 __global__ void k_fastmath(int op, const double *x, double *fast, double *ref, long n)
@@ -85,6 +108,37 @@ extern "C" double ps_probe_fp64_flops(int reps)
     const double flops = 2.0 * ps::kChains * (double)iters * threads * blocks;
     const double rate = flops / (ms * 1e-3);
     if (rate > best) best = rate;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  return best;
+}
+
+// Milliseconds of `iters` steps of `chains` dependent FMA chains on `blocks`
+// CTAs of `warps` warps with `active` lanes of each warp running (best of
+// 3 after one warm-up); -1 on a bad argument or a CUDA error.
+extern "C" double ps_probe_fp64_lanes(int active, int chains, int blocks, int warps, int iters)
+{
+  if (active < 1 || active > 32 || chains < 1 || chains > ps::kChains || blocks < 1 ||
+      blocks > 65535 || warps < 1 || warps > 32 || iters < 1)
+    return -1.0;
+  double *out = nullptr;
+  if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return -1.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  ps::k_fp64_lanes<<<blocks, 32 * warps>>>(out, active, chains, 16, 0.999999, 1e-9);
+  float best = -1.f;
+  for (int r = 0; r < 3; r++) {
+    cudaEventRecord(e0);
+    ps::k_fp64_lanes<<<blocks, 32 * warps>>>(out, active, chains, iters, 0.999999, 1e-9);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (best < 0.f || ms < best) best = ms;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -185,7 +185,8 @@ _probe = None
 
 def probe():
     """The measurement helpers (libps_probe.so, not part of the C ABI): the
-    FP64 issue-rate probe of the roofline and the fast-math check."""
+    FP64 issue-rate probe of the roofline, the fast-math check and the
+    partial-warp FP64 timing."""
     global _probe
     if _probe is None:
         if not os.path.exists(PROBE_PATH):
@@ -195,6 +196,8 @@ def probe():
         L.ps_probe_fp64_flops.argtypes = [ctypes.c_int]
         L.ps_probe_fp64_flops.restype = ctypes.c_double
         L.ps_probe_fastmath.argtypes = [ctypes.c_int, DP, DP, DP, ctypes.c_long]
+        L.ps_probe_fp64_lanes.argtypes = [ctypes.c_int] * 5
+        L.ps_probe_fp64_lanes.restype = ctypes.c_double
         _probe = L
     return _probe
 
