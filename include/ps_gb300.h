@@ -356,7 +356,8 @@ int  ps_batch_set_groups(ps_batch *b, int ngroups);
 long ps_batch_launch_count(const ps_batch *b);
 /* Tile shape of the stage kernels per model: 0 = 32x8, 1 = 16x16,
  * 2 = 64x4, 3 = 16x16 with one extra warp sharing the halo work, 4 and 5 =
- * shapes 3 and 0 compiled for three CTAs per multiprocessor instead of two
+ * shapes 3 and 0 compiled for three CTAs per multiprocessor instead of two,
+ * 6 = 32x16 with two extra warps, one CTA per multiprocessor
  * (model = -1: all models).  ps_batch_autotune times the stage
  * kernel of every distinct grid size with each shape and keeps the fastest
  * (`reps` timed launches each); the state is left unchanged. */

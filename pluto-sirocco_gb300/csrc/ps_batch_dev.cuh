@@ -45,13 +45,18 @@ __global__ void __launch_bounds__(TileGeom<TL>::NT, TileMinBlocks<TL>::value)
 // kernel tables for the tile shapes the autotuner chooses from
 // ------------------------------------------------------------------
 
-constexpr int kNumShapes = 6;
-const int kShapeX[kNumShapes] = {32, 16, 64, 16, 16, 32};
-const int kShapeY[kNumShapes] = {8, 16, 4, 16, 16, 8};
+constexpr int kNumShapes = 7;
+const int kShapeX[kNumShapes] = {32, 16, 64, 16, 16, 32, 32};
+const int kShapeY[kNumShapes] = {8, 16, 4, 16, 16, 8, 16};
 // threads per CTA: one per cell, plus one warp for the halo work of the
-// 16x16 tile's PLM (18 x 16 items) in shapes 3 and 4
-const int kShapeNT[kNumShapes] = {256, 256, 256, 288, 288, 256};
+// 16x16 tile's PLM (18 x 16 items) in shapes 3 and 4, and two for the 32x16
+// tile's (34 x 16 and 32 x 18 items) in shape 6
+const int kShapeNT[kNumShapes] = {256, 256, 256, 288, 288, 256, 576};
 using Shape3 = Tile2D<16, 16, 32>;
+// Shape 6: 32x16, one CTA per multiprocessor; PLM recomputes 6% (x) and
+// 12.5% (y) of its cells in the halo and the Riemann solver 3% and 6% of
+// its faces, against 12.5% and 6% in both directions for 16x16
+using Shape6 = Tile2D<32, 16, 64>;
 // Shapes 4 and 5: shapes 3 and 0 compiled for three CTAs per multiprocessor
 // (at most 72 / 80 registers, with some spilling) instead of two, for the
 // primitive-PLM 6-variable kernels; other variants run them as 3 and 0.
@@ -93,6 +98,7 @@ const void *batch_kernel_nv(int shape, int lim, int solver, int stage)
     case 3: return pick_batch_shape<NV, CHAR, Shape3>(lim, solver, stage);
     case 4: return pick_batch_shape<NV, CHAR, typename Shape4<NV, CHAR>::T>(lim, solver, stage);
     case 5: return pick_batch_shape<NV, CHAR, typename Shape5<NV, CHAR>::T>(lim, solver, stage);
+    case 6: return pick_batch_shape<NV, CHAR, Shape6>(lim, solver, stage);
     default: return pick_batch_shape<NV, CHAR, Tile2D<32, 8>>(lim, solver, stage);
   }
 }
@@ -105,6 +111,7 @@ size_t batch_smem_nv(int shape)
     case 2: return stage_smem_bytes<NV, Tile2D<64, 4>>();
     case 3:
     case 4: return stage_smem_bytes<NV, Shape3>();
+    case 6: return stage_smem_bytes<NV, Shape6>();
     default: return stage_smem_bytes<NV, Tile2D<32, 8>>();
   }
 }

@@ -71,12 +71,13 @@ def test_batch_tile_shapes_and_autotune(built):
     batch.run(6)
     _check_equal(solo, inb)
     for m in range(len(SPECS)):
-        assert batch.shape(m) in [(32, 8), (16, 16), (64, 4)]
+        assert batch.shape(m) in [(32, 8), (16, 16), (64, 4), (32, 16)]
     # the shapes compiled for three CTAs per multiprocessor (4: 16x16 with
-    # the halo warp, 5: 32x8) give the same bits
+    # the halo warp, 5: 32x8) and the 32x16 tile (6) give the same bits
     batch.set_shape(4, model=0)
     batch.set_shape(5, model=1)
-    assert batch.shape(0) == (16, 16) and batch.shape(1) == (32, 8)
+    batch.set_shape(6, model=2)
+    assert batch.shape(0) == (16, 16) and batch.shape(1) == (32, 8) and batch.shape(2) == (32, 16)
     for s in solo:
         s.run(4)
     batch.run(4)
@@ -94,7 +95,9 @@ def test_batch_production_limiting_matches_individual_runs(built):
     solo = [psgb.wind_model_solver(s, **kw) for s in SPECS]
     inb = [psgb.wind_model_solver(s, **kw) for s in SPECS]
     batch = psgb.Batch(inb)
-    for chunk in (5, 8):
+    for chunk, shape in ((5, None), (8, 6)):
+        if shape is not None:   # the 32x16 tile for the characteristic kernels too
+            batch.set_shape(shape)
         flags = 0
         for s in solo:
             flags |= s.run(chunk)
