@@ -956,7 +956,8 @@ int ps_sg_cool_launch(ps_ctx *c)
   ps::k_sg_cool<<<std::min(nblk, nsm * ps::kInfCtasPerSm), 128, ps::kInfBytes, c->stream>>>(
       s->net(), s->box, A, reinterpret_cast<const ps::BlockItem *>(c->sg_items), nblk,
       c->sg_use_net, reinterpret_cast<int2 *>(c->sg_queue), c->sg_qcount, s->stats);
-  ps::k_sg_cool_fallback<<<608, 128, 0, c->stream>>>(A, reinterpret_cast<int2 *>(c->sg_queue),
+  // one warp per CTA: the few queued cells spread over every SM
+  ps::k_sg_cool_fallback<<<2432, 32, 0, c->stream>>>(A, reinterpret_cast<int2 *>(c->sg_queue),
                                                      c->sg_qcount);
   c->launches += 2;
   SCK(cudaGetLastError());

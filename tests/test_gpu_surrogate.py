@@ -221,8 +221,8 @@ def test_batch_with_surrogate_matches_individual(trained):
 def test_fallback_equals_reference_method(built, grid):
     """Every cell outside the surrogate's box goes to the fallback, which
     must give the reference method's state bit for bit, alone and in a
-    batch: a queue that fits the first warp of every multiprocessor (64x32:
-    2048 cells) and one that spills into the others (128x64: 8192 cells)."""
+    batch: queues of 2048 cells (64x32) and 8192 cells (128x64), one cell
+    per thread of one-warp CTAs."""
     import psgb
     spec = dict(grid=grid, l_star=1e37, krad=0.2, alpharad=-0.6)
     sg = psgb.Surrogate((40.0,) * 4, (41.0,) * 4)     # a box no cell is in
