@@ -285,19 +285,45 @@ __device__ __forceinline__ double sg_z(const SgCtx &b, double T, double &dz, dou
 // rate at the root of opposite sign to the initial one (the reference then
 // solves for the equilibrium temperature instead), or a root on the wrong
 // side of T.  Sets hc_init.
-__device__ __forceinline__ int sg_judge(SgCtx &b, double T, double T0, bool from_net, double &T_f,
-                                        int &evals, bool &stiff)
+//
+// In three parts, so that a kernel can settle the non-stiff cells before
+// it knows whether it needs the network at all (sg_cool_items):
+// sg_judge_first evaluates the rate at T and settles a non-stiff cell
+// (SG_PENDING for a stiff one, with z and dz at T), sg_judge_rest iterates
+// a stiff cell from there, and sg_judge_final is the polishing step and
+// the checks of both.
+constexpr int SG_PENDING = 4;
+
+__device__ __forceinline__ int sg_judge_final(const SgCtx &b, double T, double Tk, double z,
+                                              double dz, double hc, double &T_f)
+{
+  if (!gt0(dz) || lt0(hc * b.hc_init)) return SG_REJECT;
+  const double Tn = Tk - z / dz;
+  if (!gt0(Tn) || !isfinite(Tn) || lt0((Tn - T) * b.hc_init)) return SG_REJECT;
+  T_f = Tn;
+  return SG_ACCEPT;
+}
+
+__device__ __forceinline__ int sg_judge_first(SgCtx &b, double T, double &z, double &dz,
+                                              double &T_f)
 {
   const double cth = b.n * kKB * 1.5;
   double dhc;
   b.hc_init = sg_heatcool_d(b, T, dhc);
-  evals = 1;
+  z = T * cth - b.E - b.dt * b.hc_init;
+  dz = cth - b.dt * dhc * 0.5;
+  if (!(fabs(z) <= kSgResidual * T * cth)) return SG_PENDING;
+  return sg_judge_final(b, T, T, z, dz, b.hc_init, T_f);
+}
+
+// evals counts the evaluation of sg_judge_first
+__device__ __forceinline__ int sg_judge_rest(const SgCtx &b, double T, double T0, bool from_net,
+                                             double z, double dz, double &T_f, int &evals)
+{
+  const double cth = b.n * kKB * 1.5;
   double Tk = T, hc = b.hc_init;
-  double z = T * cth - b.E - b.dt * b.hc_init;
-  double dz = cth - b.dt * dhc * 0.5;
-  bool conv = fabs(z) <= kSgResidual * T * cth;
-  stiff = !conv;
-  if (!conv && from_net && gt0(T0) && isfinite(T0) && fabs(T0 - T) > kSgJump * T) {
+  bool conv = false;
+  if (from_net && gt0(T0) && isfinite(T0) && fabs(T0 - T) > kSgJump * T) {
     Tk = T0;
     z = sg_z(b, Tk, dz, hc);
     evals++;
@@ -310,11 +336,18 @@ __device__ __forceinline__ int sg_judge(SgCtx &b, double T, double T0, bool from
     evals++;
     conv = fabs(z) <= kSgResidual * Tk * cth;
   }
-  if (!gt0(dz) || lt0(hc * b.hc_init)) return SG_REJECT;
-  const double Tn = Tk - z / dz;
-  if (!gt0(Tn) || !isfinite(Tn) || lt0((Tn - T) * b.hc_init)) return SG_REJECT;
-  T_f = Tn;
-  return SG_ACCEPT;
+  return sg_judge_final(b, T, Tk, z, dz, hc, T_f);
+}
+
+__device__ __forceinline__ int sg_judge(SgCtx &b, double T, double T0, bool from_net, double &T_f,
+                                        int &evals, bool &stiff)
+{
+  double z, dz;
+  evals = 1;
+  const int st = sg_judge_first(b, T, z, dz, T_f);
+  stiff = st == SG_PENDING;
+  if (!stiff) return st;
+  return sg_judge_rest(b, T, T0, from_net, z, dz, T_f, evals);
 }
 
 }  // namespace ps

@@ -171,15 +171,35 @@ __device__ __forceinline__ void sg_cool_items(const SgNet &net, const SgBox &bx,
         if (!inbox) x[0] = x[1] = x[2] = x[3] = 0.f;
       }
     }
-    float y = 0.f;
-    const bool ok = sg_forward(smem, tmem, phase, x, 0, 0, y);
-    if (!ok && threadIdx.x == 0) atomicOr(&A.sc->flags, F_TMA_TIMEOUT);
+    // the judge's first rate evaluation settles the non-stiff cells, which
+    // do not read the network's prediction; the network runs only for a
+    // block that holds a stiff cell (CTA-uniform), to start its iterations
     int st = SG_BELOW_MIN, evals = 0;
     bool stiff = false;
+    double T_f = 0.0, z = 0.0, dz = 0.0;
+    if (kind == 1 && inbox) {
+      // xi^-1/2 and xi^1/4 = (xi^-1/2)^-1/2 by two reciprocal square roots
+      b.isqxi = rsqrt(b.xi);
+      b.sqsqxi = rsqrt(b.isqxi);
+      evals = 1;
+      st = sg_judge_first(b, T, z, dz, T_f);
+      stiff = st == SG_PENDING;
+    } else if (kind == 1) {
+      st = SG_OUT_OF_BOX;
+    } else if (kind == 2) {
+      st = SG_REJECT;
+    }
+    bool ok = true;
+    float y = 0.f;
+    if (__syncthreads_or(stiff && use_net)) {
+      ok = sg_forward(smem, tmem, phase, x, 0, 0, y);
+      if (!ok && threadIdx.x == 0) atomicOr(&A.sc->flags, F_TMA_TIMEOUT);
+    }
+    if (stiff) {
+      const double T0 = T * (double)exp10f(4.0f * y);
+      st = ok ? sg_judge_rest(b, T, T0, use_net != 0, z, dz, T_f, evals) : SG_REJECT;
+    }
     if (kind) {
-      double T_f = 0.0, T0;
-      st = (ok && kind == 1) ? sg_decide(b, T, inbox, y, use_net, T_f, T0, evals, stiff)
-                             : SG_REJECT;
       if (st == SG_ACCEPT) {
         A.V[PRS * A.p.vstride + c] = dmax(T_f, 1.e4) * b.n * u.p_of_tn;
       } else {
