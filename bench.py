@@ -693,7 +693,7 @@ def batch_bench(wl, steps, warmup, rank, world):
                             "perturbation of its initial state (the full-physics 512x256 "
                             "wind after 100 steps); the learned step changes the pressure only",
                    "tile_shapes": shapes, "autotune_s": t_tune,
-                   "groups": wl.groups or 1,
+                   "groups": wl.groups or "library default (2)",
                    "line_force": _line_force_figures(wl),
                    "l2": "256 MiB buffer written before every timed step (L2 flushed)",
                    "parallelism": "replicas only" if world > 1 else "single GPU"},

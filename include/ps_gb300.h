@@ -342,13 +342,15 @@ int  ps_batch_sync(ps_batch *b);      /* OR of every model's PS_F_* flags */
 int  ps_batch_set_states(ps_batch *b, const double *const *Vc);
 int  ps_batch_get_states(ps_batch *b, double *const *Vc);
 /* The same transfers by the copy engines only, queued without waiting:
- * two batches on their own streams then overlap one batch's transfers with
- * the other's steps.  The host arrays (pinned) are in use until
- * ps_batch_sync returns. */
+ * several batches on their own streams then overlap each batch's transfers
+ * with the others' steps (four batches hide them on the benchmark batch,
+ * two do not: both compute at once, then both copy).  The host arrays
+ * (pinned) are in use until ps_batch_sync returns. */
 int  ps_batch_set_states_async(ps_batch *b, const double *const *Vc);
 int  ps_batch_get_states_async(ps_batch *b, double *const *Vc);
 int  ps_batch_set_stream(ps_batch *b, void *stream);
-/* The models are dealt out by size into ngroups groups (default 1) whose
+/* The models are dealt out by size into ngroups groups (default 2, 1 for
+ * a single model) whose
  * steps run as parallel branches of the step graph, so that one group's
  * short, latency-bound kernels can overlap the others' stage kernels.
  * Results do not depend on it. */

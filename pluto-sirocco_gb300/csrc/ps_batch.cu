@@ -562,11 +562,14 @@ static void batch_free(ps_batch *b)
   delete b;
 }
 
-// Default number of model groups: 1.  On the 64-model benchmark batch four
-// groups measured the same step time as one (14.73 against 14.76 ms): the
-// stage kernels fill the GPU either way, and the learned step's kernels,
-// split four ways, pay four set-ups and tails where one group pays one.
-static int default_groups(int) { return 1; }
+// Default number of model groups: two (one for a single model).  On the
+// 64-model benchmark batch two groups measured 13.64 ms a step against
+// 13.74 ms for one: one group's cooling fallback (a few thousand cells, a
+// latency-bound tail of about 0.3 ms on an otherwise idle GPU) overlaps
+// the other group's work.  Four groups measured the same as two (13.64
+// ms): the stage kernels fill the GPU either way, and each group pays the
+// learned step's set-up and tail.
+static int default_groups(int n) { return n >= 2 ? 2 : 1; }
 
 extern "C" int ps_batch_create(ps_ctx **ctxs, int n, ps_batch **out)
 {
