@@ -57,14 +57,18 @@ using Shape3 = Tile2D<16, 16, 32>;
 // 12.5% (y) of its cells in the halo and the Riemann solver 3% and 6% of
 // its faces, against 12.5% and 6% in both directions for 16x16
 using Shape6 = Tile2D<32, 16, 64>;
-// Shapes 4 and 5: shapes 3 and 0 compiled for three CTAs per multiprocessor
-// (at most 72 / 80 registers, with some spilling) instead of two, for the
-// primitive-PLM 6-variable kernels; other variants run them as 3 and 0.
+// Shapes 4 and 5: shapes 3 and 0 compiled for more CTAs per multiprocessor:
+// three (at most 72 / 80 registers, with some spilling) instead of two for
+// the primitive-PLM 6-variable kernels, two (at most 112 / 128 registers)
+// instead of one for the others, whose natural register count (about 130
+// with characteristic limiting) leaves one CTA per multiprocessor.
 template <int NV, bool CHAR> struct Shape4 {
-  using T = typename std::conditional<NV == 6 && !CHAR, Tile2D<16, 16, 32, 3>, Shape3>::type;
+  using T = typename std::conditional<NV == 6 && !CHAR, Tile2D<16, 16, 32, 3>,
+                                      Tile2D<16, 16, 32, 2>>::type;
 };
 template <int NV, bool CHAR> struct Shape5 {
-  using T = typename std::conditional<NV == 6 && !CHAR, Tile2D<32, 8, 0, 3>, Tile2D<32, 8>>::type;
+  using T = typename std::conditional<NV == 6 && !CHAR, Tile2D<32, 8, 0, 3>,
+                                      Tile2D<32, 8, 0, 2>>::type;
 };
 
 template <int NV, bool CHAR, int LIM, int SOLVER, class TL>

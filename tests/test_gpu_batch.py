@@ -95,8 +95,11 @@ def test_batch_production_limiting_matches_individual_runs(built):
     solo = [psgb.wind_model_solver(s, **kw) for s in SPECS]
     inb = [psgb.wind_model_solver(s, **kw) for s in SPECS]
     batch = psgb.Batch(inb)
-    for chunk, shape in ((5, None), (8, 6)):
-        if shape is not None:   # the 32x16 tile for the characteristic kernels too
+    # the autotuner's default, then the shapes compiled for two CTAs per
+    # multiprocessor (4: 16x16 with the halo warp, 5: 32x8) and the 32x16
+    # tile (6), which the characteristic kernels use
+    for chunk, shape in ((5, None), (4, 4), (4, 5), (8, 6)):
+        if shape is not None:
             batch.set_shape(shape)
         flags = 0
         for s in solo:
