@@ -26,6 +26,7 @@ const void *stage_kernel_3d(int nv, int lim, int solver, int stage);
 size_t stage_smem_2d(int nv);
 size_t stage_smem_3d(int nv);
 void stage_tile_2d(int *t);
+void wind_tile_2d(int *t, int *threads);
 void stage_tile_3d(int *t);
 
 // One CTA: see finish_block().
@@ -257,8 +258,12 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
   p.tstop = cfg->tstop;
   p.first_dt = cfg->first_dt;
 
+  int threads = 0;  // one per tile cell unless the tile says otherwise
   if (cfg->dims == 2) {
-    ps::stage_tile_2d(c->tile);
+    if (sph)
+      ps::wind_tile_2d(c->tile, &threads);
+    else
+      ps::stage_tile_2d(c->tile);
     c->smem = ps::stage_smem_2d(p.nvar);
     c->k1 = sph ? nullptr : ps::stage_kernel_2d(p.nvar, p.limiter, p.solver, 1);
     c->k2 = sph ? nullptr : ps::stage_kernel_2d(p.nvar, p.limiter, p.solver, 2);
@@ -268,7 +273,7 @@ extern "C" int ps_create(const ps_config *cfg, ps_ctx **out)
     c->k1 = ps::stage_kernel_3d(p.nvar, p.limiter, p.solver, 1);
     c->k2 = ps::stage_kernel_3d(p.nvar, p.limiter, p.solver, 2);
   }
-  c->block = dim3(c->tile[0] * c->tile[1] * c->tile[2]);
+  c->block = dim3(threads ? threads : c->tile[0] * c->tile[1] * c->tile[2]);
   c->grid = dim3((p.nx[0] + c->tile[0] - 1) / c->tile[0], (p.nx[1] + c->tile[1] - 1) / c->tile[1],
                  (p.nx[2] + c->tile[2] - 1) / c->tile[2]);
 

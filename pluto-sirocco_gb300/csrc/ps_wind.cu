@@ -107,6 +107,15 @@ static const void *stage_kernel_sph(int nv, bool ch, int lim, int solver, int st
   return stage_kernel_sph_other(nv, ch, lim, solver, stage);
 }
 
+// Tile of the single-model wind kernels: cells per direction, ghost width
+// loaded around them (the tensor-map box), and threads per CTA.
+void wind_tile_2d(int *t, int *threads)
+{
+  t[0] = WindTile::X; t[1] = WindTile::Y; t[2] = WindTile::Z;
+  t[3] = WindTile::HX; t[4] = WindTile::HY; t[5] = WindTile::HZ;
+  *threads = TileGeom<WindTile>::NT;
+}
+
 }  // namespace ps
 
 // ------------------------------------------------------------------
@@ -430,8 +439,8 @@ extern "C" int ps_set_wind(ps_ctx *c, const ps_wind *wp, const double *flux_r,
 
   w->k1 = ps::stage_kernel_sph(p.nvar, p.char_lim != 0, p.limiter, p.solver, 1);
   w->k2 = ps::stage_kernel_sph(p.nvar, p.char_lim != 0, p.limiter, p.solver, 2);
-  w->smem = p.nvar == 7 ? ps::stage_smem_bytes<7, ps::TileT<2>>()
-                        : ps::stage_smem_bytes<6, ps::TileT<2>>();
+  w->smem = p.nvar == 7 ? ps::stage_smem_bytes<7, ps::WindTile>()
+                        : ps::stage_smem_bytes<6, ps::WindTile>();
   if (!w->k1 || !w->k2) {
     ps_wind_free(w);
     return wind_fail("ps_set_wind: no kernel for this configuration");

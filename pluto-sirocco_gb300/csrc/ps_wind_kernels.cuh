@@ -1,5 +1,5 @@
 // ps_wind_kernels.cuh -- the single-model wind stage kernel (one CTA per
-// 32x8 tile of one context, tensor map as a kernel parameter) and its table
+// 16x16 tile of one context, tensor map as a kernel parameter) and its table
 // over limiter, solver and stage, instantiated per variable count and
 // limiting form in ps_wind.cu and ps_wind_k.cu.
 #pragma once
@@ -8,12 +8,19 @@
 
 namespace ps {
 
+// The tile of the single-model wind kernels: 16x16 with a ninth warp for
+// the halo work of PLM and Riemann, compiled for two CTAs per
+// multiprocessor -- the shape the batch's autotuner keeps for every grid
+// size, with the primitive limiter (96 registers) and with characteristic
+// limiting (which otherwise takes about 130 registers and one CTA).
+using WindTile = Tile2D<16, 16, 32, 2>;
+
 template <int NV, int LIM, int SOLVER, int STAGE, bool CHAR>
-__global__ void __launch_bounds__(TileGeom<TileT<2>>::NT)
+__global__ void __launch_bounds__(TileGeom<WindTile>::NT, TileMinBlocks<WindTile>::value)
     k_stage_sph(const __grid_constant__ CUtensorMap tm, const WindStageArgs A)
 {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  stage_sph_tile<NV, LIM, SOLVER, STAGE, TileT<2>, CHAR>(&tm, A, blockIdx.x, blockIdx.y,
+  stage_sph_tile<NV, LIM, SOLVER, STAGE, WindTile, CHAR>(&tm, A, blockIdx.x, blockIdx.y,
                                                          smem_raw);
 }
 
