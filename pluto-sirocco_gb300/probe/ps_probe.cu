@@ -10,8 +10,15 @@
 //   ps_probe_fp64_lanes  the time of dependent FP64 FMAs in warps with only
 //                        some lanes active (how the cost of a double-
 //                        precision instruction depends on the active lanes,
-//                        for the kernels that run few cells per warp).
+//                        for the kernels that run few cells per warp);
+//   ps_probe_wait_timeout
+//                        the bounded mbarrier wait of the stage and learned-
+//                        step kernels (ps_tma.cuh) on a barrier that nothing
+//                        completes: it must give up after its poll limit and
+//                        report, leaving the context usable (the failure test
+//                        of a wait, without a GPU fault).
 #include "ps_fastmath.cuh"
+#include "ps_tma.cuh"
 
 #include <cuda_runtime.h>
 
@@ -51,6 +58,23 @@ __global__ void k_fp64_lanes(double *out, int active, int chains, int iters, dou
 #pragma unroll
   for (int c = 0; c < kChains; c++) s += x[c];
   if (s == 12345.678) out[0] = s;
+}
+
+// One CTA: an mbarrier for one arrival; with `arrive` the barrier's phase
+// is completed first (arrival with no transaction bytes), otherwise nothing
+// completes it.  out[0] = 1 if every thread's bounded wait saw the phase
+// complete, 0 if they gave up after `limit` polls.
+__global__ void k_wait_timeout(int limit, int arrive, int *out)
+{
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    if (arrive) mbar_expect_tx(&bar, 0);
+  }
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(&bar, 0, (uint32_t)limit);
+  const int all = __syncthreads_and(ok);
+  if (threadIdx.x == 0) out[0] = all ? 1 : 0;
 }
 
 __global__ void k_fastmath(int op, const double *x, double *fast, double *ref, long n)
@@ -145,4 +169,22 @@ extern "C" double ps_probe_fp64_lanes(int active, int chains, int blocks, int wa
   cudaFree(out);
   if (cudaGetLastError() != cudaSuccess) return -1.0;
   return best;
+}
+
+// The bounded wait (see k_wait_timeout) with a poll limit of `limit`
+// (1..65536): *completed = 1 if the wait saw the barrier complete, 0 if it
+// gave up.  Returns 0, or -1 on a bad argument or a CUDA error.
+extern "C" int ps_probe_wait_timeout(int limit, int arrive, int *completed)
+{
+  if (limit < 1 || limit > 65536 || !completed) return -1;
+  int *d = nullptr;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return -1;
+  cudaError_t e = cudaMemset(d, 0xFF, sizeof(int));
+  if (e == cudaSuccess) {
+    ps::k_wait_timeout<<<1, 128>>>(limit, arrive, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(completed, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? 0 : -1;
 }

@@ -185,8 +185,8 @@ _probe = None
 
 def probe():
     """The measurement helpers (libps_probe.so, not part of the C ABI): the
-    FP64 issue-rate probe of the roofline, the fast-math check and the
-    partial-warp FP64 timing."""
+    FP64 issue-rate probe of the roofline, the fast-math check, the
+    partial-warp FP64 timing and the bounded-wait failure check."""
     global _probe
     if _probe is None:
         if not os.path.exists(PROBE_PATH):
@@ -198,6 +198,8 @@ def probe():
         L.ps_probe_fastmath.argtypes = [ctypes.c_int, DP, DP, DP, ctypes.c_long]
         L.ps_probe_fp64_lanes.argtypes = [ctypes.c_int] * 5
         L.ps_probe_fp64_lanes.restype = ctypes.c_double
+        L.ps_probe_wait_timeout.argtypes = [ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_int)]
         _probe = L
     return _probe
 

@@ -78,6 +78,7 @@ def test_blast_ic_matches_reference(built, meta):
 
 
 @pytest.mark.parametrize("bad", [dict(dims=1), dict(nvar=7), dict(limiter="mc", nx=(3, 64, 1)),
+                                 dict(nx=(0, 64, 1)), dict(nx=(64, -4, 1)),
                                  dict(bc=["periodic", "outflow", "outflow", "outflow",
                                           "outflow", "outflow"])])
 def test_bad_config_rejected_without_gpu(built, bad):
