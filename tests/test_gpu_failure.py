@@ -12,6 +12,9 @@ bounded wait run out, never by a trap, a bad address or an endless loop.
   its own scalars, as the reference's QUIT_PLUTO ends only that run).
 * A truncated snapshot is refused with a message, and the context it was
   meant for still runs.
+* Halo poisoning: NaN in every ghost cell of the state handed in never
+  reaches the result (the ghost zones are refilled before every stage, as
+  the reference's Boundary does), for the Cartesian blast and the wind.
 """
 import numpy as np
 import pytest
@@ -57,3 +60,43 @@ def test_truncated_snapshot_is_refused(built, tmp_path):
     with pytest.raises(RuntimeError, match="does not hold"):
         s.read_dbl(path)
     assert s.run(2) & ~0x2 == 0      # still runs (PS_F_CONS2PRIM is a repaired cell)
+
+
+def _poison_ghosts(V, g):
+    """NaN in every ghost cell of a [nv][k][j][i] 2-D state with g ghost
+    layers per side."""
+    W = V.copy()
+    W[:, :, :g, :] = np.nan
+    W[:, :, -g:, :] = np.nan
+    W[:, :, :, :g] = np.nan
+    W[:, :, :, -g:] = np.nan
+    return W
+
+
+@pytest.mark.parametrize("case", ["blast", "wind"])
+def test_poisoned_ghost_cells_never_reach_the_result(built, case):
+    """The reference refills the ghost zones before every stage (Boundary),
+    so what the host hands in there must not matter: a state whose ghost
+    cells are all NaN gives, bit for bit, what the clean state gives."""
+    import psgb
+    if case == "blast":
+        cfg = psgb.make_config(dims=2, nx=(48, 40, 1), limiter="mc", solver="hllc", bc="outflow")
+        grid = psgb.Grid(cfg)
+        V0 = psgb.blast_state(cfg, grid)
+        runs = []
+        for V in (V0, _poison_ghosts(V0, 2)):
+            s = psgb.Solver(cfg, grid)
+            s.set_state(V)
+            s.set_time(0.0, 1e-4, 0)
+            assert s.run(5) == 0
+            runs.append(s.get_state()[:, 0, 2:-2, 2:-2])
+    else:
+        clean = psgb.wind_model_solver(SPEC)
+        poisoned = psgb.wind_model_solver(SPEC)
+        poisoned.set_state(_poison_ghosts(poisoned.get_state(), 2))
+        runs = []
+        for s in (clean, poisoned):
+            assert s.run(5) & ~0x2 == 0
+            runs.append(s.get_state()[:, 0, 2:-2, 2:-2])
+    assert not np.isnan(runs[1]).any()
+    assert np.array_equal(runs[0], runs[1])
