@@ -399,6 +399,14 @@ int ps_sg_create(const ps_sg_box *box, ps_surrogate **out);
 int ps_sg_destroy(ps_surrogate *s);
 int ps_sg_set_params(ps_surrogate *s, const float *params);
 int ps_sg_get_params(const ps_surrogate *s, float *params);
+/* A trained network (its box and parameters) to a file and back, so that a
+ * run can use a network trained once (the drop-in reads the file named by
+ * PS_LEARNED_COOLING).  Format: "PSSGNET1", lo[4], hi[4], t_x, mu (doubles),
+ * the parameter count (int32, 4545), the parameters (float), little-endian.
+ * ps_sg_load creates the surrogate; a file of another size or tag is
+ * refused. */
+int ps_sg_save(const ps_surrogate *s, const char *path);
+int ps_sg_load(const char *path, ps_surrogate **out);
 /* T_new of the reference method on the GPU for n tuples (row-major
  * n x 4: n_H, T, xi, dt [s]): the training labels.  t_cool (may be NULL)
  * gets the cooling time E / |net rate| at T in seconds. */

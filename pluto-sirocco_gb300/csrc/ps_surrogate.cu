@@ -22,6 +22,7 @@
 #include "ps_surrogate_cool.cuh"
 
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -649,6 +650,77 @@ extern "C" int ps_sg_get_params(const ps_surrogate *s, float *p)
   if (!s || !p) return sg_fail("ps_sg_get_params: null argument");
   SCK(cudaStreamSynchronize(s->stream));
   SCK(cudaMemcpy(p, s->prm, sizeof(float) * ps::kSgParams, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// A trained network on disk: the tag "PSSGNET1", the box (lo[4], hi[4],
+// t_x, mu: ten doubles), the parameter count (a 32-bit integer, 4545) and
+// the parameters (FP32, the layout of ps_sg_set_params), little-endian.
+static const char kSgTag[8] = {'P', 'S', 'S', 'G', 'N', 'E', 'T', '1'};
+
+static bool sg_little_endian()
+{
+  const uint32_t one = 1;
+  unsigned char b;
+  std::memcpy(&b, &one, 1);
+  return b == 1;
+}
+
+extern "C" int ps_sg_save(const ps_surrogate *s, const char *path)
+{
+  if (!s || !path) return sg_fail("ps_sg_save: null argument");
+  if (!sg_little_endian()) return sg_fail("ps_sg_save: big-endian host not supported");
+  std::vector<float> prm(ps::kSgParams);
+  if (int r = ps_sg_get_params(s, prm.data())) return r;
+  double hdr[10];
+  for (int i = 0; i < 4; i++) {
+    hdr[i] = s->box.lo[i];
+    hdr[4 + i] = s->box.hi[i];
+  }
+  hdr[8] = s->box.t_x;
+  hdr[9] = s->box.mu;
+  const int32_t n = ps::kSgParams;
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return sg_fail("ps_sg_save: cannot open the file");
+  bool ok = std::fwrite(kSgTag, 1, 8, f) == 8 && std::fwrite(hdr, sizeof(double), 10, f) == 10 &&
+            std::fwrite(&n, sizeof(n), 1, f) == 1 &&
+            std::fwrite(prm.data(), sizeof(float), (size_t)n, f) == (size_t)n;
+  ok = std::fclose(f) == 0 && ok;
+  return ok ? 0 : sg_fail("ps_sg_save: write failed");
+}
+
+extern "C" int ps_sg_load(const char *path, ps_surrogate **out)
+{
+  if (!path || !out) return sg_fail("ps_sg_load: null argument");
+  *out = nullptr;
+  if (!sg_little_endian()) return sg_fail("ps_sg_load: big-endian host not supported");
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return sg_fail("ps_sg_load: cannot open the file");
+  char tag[8];
+  double hdr[10];
+  int32_t n = 0;
+  std::vector<float> prm(ps::kSgParams);
+  bool ok = std::fread(tag, 1, 8, f) == 8 && std::memcmp(tag, kSgTag, 8) == 0 &&
+            std::fread(hdr, sizeof(double), 10, f) == 10 && std::fread(&n, sizeof(n), 1, f) == 1 &&
+            n == ps::kSgParams &&
+            std::fread(prm.data(), sizeof(float), (size_t)n, f) == (size_t)n &&
+            std::fgetc(f) == EOF;
+  std::fclose(f);
+  if (!ok) return sg_fail("ps_sg_load: not a network file of this library (tag, size)");
+  ps_sg_box box;
+  for (int i = 0; i < 4; i++) {
+    box.lo[i] = hdr[i];
+    box.hi[i] = hdr[4 + i];
+  }
+  box.t_x = hdr[8];
+  box.mu = hdr[9];
+  ps_surrogate *s = nullptr;
+  if (int r = ps_sg_create(&box, &s)) return r;
+  if (int r = ps_sg_set_params(s, prm.data())) {
+    ps_sg_destroy(s);
+    return r;
+  }
+  *out = s;
   return 0;
 }
 

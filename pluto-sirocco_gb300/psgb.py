@@ -33,6 +33,7 @@ EXPORTS = ["ps_last_error", "ps_grid_build", "ps_init_blast", "ps_create", "ps_d
            "ps_batch_set_stream", "ps_batch_launch_count", "ps_batch_set_shape",
            "ps_batch_get_shape", "ps_batch_autotune", "ps_batch_time_step_kernels",
            "ps_sg_create", "ps_sg_destroy", "ps_sg_set_params", "ps_sg_get_params",
+           "ps_sg_save", "ps_sg_load",
            "ps_sg_label", "ps_sg_set_data", "ps_sg_train", "ps_sg_grad", "ps_sg_predict",
            "ps_sg_stats", "ps_set_surrogate", "ps_batch_set_surrogate", "ps_sg_collect",
            "ps_set_cooling", "ps_write_dbl", "ps_read_dbl", "ps_read_sirocco_fluxes",
@@ -156,6 +157,8 @@ def lib():
         L.ps_sg_destroy.argtypes = [P]
         L.ps_sg_set_params.argtypes = [P, FP]
         L.ps_sg_get_params.argtypes = [P, FP]
+        L.ps_sg_save.argtypes = [P, ctypes.c_char_p]
+        L.ps_sg_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(P)]
         L.ps_sg_label.argtypes = [P, DP, Lg, DP, DP]
         L.ps_sg_set_data.argtypes = [P, DP, DP, Lg]
         L.ps_sg_train.argtypes = [P, I, I, ctypes.c_float, ctypes.c_float, ctypes.c_ulonglong, FP]
@@ -710,6 +713,19 @@ class Surrogate:
         p = np.ascontiguousarray(p, dtype=np.float32)
         check(lib().ps_sg_set_params(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
               "ps_sg_set_params")
+
+    def save(self, path):
+        """The box and the parameters to a file (ps_sg_save)."""
+        check(lib().ps_sg_save(self.h, os.fsencode(path)), "ps_sg_save")
+
+    @classmethod
+    def load(cls, path):
+        """A surrogate from a file written by save() (ps_sg_load)."""
+        self = cls.__new__(cls)
+        self.h = ctypes.c_void_p()
+        check(lib().ps_sg_load(os.fsencode(path), ctypes.byref(self.h)), "ps_sg_load")
+        self.box = None
+        return self
 
     def label(self, tuples, t_cool=False):
         t = np.ascontiguousarray(tuples, dtype=np.float64)

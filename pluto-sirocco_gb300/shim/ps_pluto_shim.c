@@ -21,6 +21,8 @@
  *    (Src/Time_Stepping/update_stage.c:389-394); SplitSource lowers
  *    Dts->dt_cool as CoolingSource does (Src/Cooling/cooling_source.c), both
  *    read by NextTimeStep (Src/main.c:601-644);
+ *  - with PS_LEARNED_COOLING set to a network file (ps_sg_save),
+ *    SplitSource runs the learned BLONDIN step instead of bracket + Brent;
  *  - a NaN in the state stops the run with QUIT_PLUTO(1), as CheckNaN does
  *    (Src/debug_tools.c:13-38); a host-side error prints ps_last_error()
  *    and stops it the same way.
@@ -34,6 +36,7 @@
 #include "ps_gb300.h"
 
 static ps_ctx *g_ps_ctx = NULL;
+static ps_surrogate *g_ps_sg = NULL;
 
 static void ps_shim_fail(const char *who, int rc)
 {
@@ -129,6 +132,21 @@ static ps_ctx *ps_shim_context(Data *d, Grid *grid)
   w.nangles = NFLUX_ANGLES;
   rc = ps_set_wind(g_ps_ctx, &w, flux_r_UV[0][0][0], flux_t_UV[0][0][0], flux_p_UV[0][0][0]);
   if (rc) ps_shim_fail("ps_set_wind", rc);
+#if COOLING == BLONDIN
+  {
+    /* PS_LEARNED_COOLING=<file>: SplitSource runs the learned BLONDIN step
+       with the network saved there by ps_sg_save (the reference method
+       stays the fallback for the cells it hands back) */
+    const char *net = getenv("PS_LEARNED_COOLING");
+    if (net && *net) {
+      rc = ps_sg_load(net, &g_ps_sg);
+      if (rc) ps_shim_fail("ps_sg_load", rc);
+      rc = ps_set_surrogate(g_ps_ctx, g_ps_sg, 1);
+      if (rc) ps_shim_fail("ps_set_surrogate", rc);
+      print("> learned cooling step, network %s\n", net);
+    }
+  }
+#endif
 #endif
   return g_ps_ctx;
 }

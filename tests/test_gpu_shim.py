@@ -9,7 +9,9 @@ hydro tolerance:
 * the 64x32 wind with the ODE cooling path (COOLING TABULATED), 100
   steps, snapshots every 20 steps: there the time step is limited by the
   cooling time, which reaches PLUTO's NextTimeStep only through the shim's
-  Dts->dt_cool (ps_split_source_dt), so the dt column of dbl.out checks it.
+  Dts->dt_cool (ps_split_source_dt), so the dt column of dbl.out checks it;
+* the 64x32 BLONDIN wind with the learned cooling step switched on through
+  PS_LEARNED_COOLING (a network file written by ps_sg_save).
 """
 import json
 import os
@@ -87,5 +89,57 @@ def test_reference_main_loop_with_the_gpu_step_ode_wind(built):
             for col, key in ((1, "t"), (2, "dt")):
                 want = float(meta[key][k])
                 assert abs(float(row[col]) - want) <= 1e-6 * abs(want), (step, key, row, want)
+    finally:
+        shutil.rmtree(wd, ignore_errors=True)
+
+
+def test_reference_main_loop_with_the_learned_cooling_step(built, tmp_path):
+    """PS_LEARNED_COOLING names a network file (ps_sg_save): the drop-in
+    then runs the learned BLONDIN step in SplitSource.  The reference's own
+    main loop through the shim (64x32 BLONDIN wind, 20 steps) gives what
+    the library's loop gives with the same network, and stays within the
+    learned step's tolerance of the reference method's run.  The network is
+    the library's default initialisation: the judge checks every cell and
+    hands the ones it rejects to the reference method, so any network gives
+    a valid step."""
+    import psgb
+    import ref_runs
+    from test_gpu_wind import _wind_solver
+    exe = _shim_binary("wind2d")
+    lo, hi = [b[0] for b in psgb.SG_DRAW_BOX], [b[1] for b in psgb.SG_DRAW_BOX]
+    sg = psgb.Surrogate(lo, hi)
+    net = tmp_path / "net.psg"
+    sg.save(net)
+    again = psgb.Surrogate.load(net)
+    assert np.array_equal(again.params(), sg.params())
+    bad = tmp_path / "bad.psg"
+    bad.write_bytes(open(net, "rb").read()[:-4])
+    with pytest.raises(RuntimeError, match="not a network file"):
+        psgb.Surrogate.load(bad)
+
+    steps = 20
+    lib_run = _wind_solver(64, 32, cooling=1, line_force=1)
+    psgb.check(psgb.lib().ps_set_surrogate(lib_run.ctx, again.h, 1), "ps_set_surrogate")
+    assert lib_run.run(steps) & ~0x2 == 0
+    want = lib_run.get_state()[:6, 0, 2:-2, 2:-2]
+    ref_run = _wind_solver(64, 32, cooling=1, line_force=1)      # the reference method
+    assert ref_run.run(steps) & ~0x2 == 0
+    exact = ref_run.get_state()[:6, 0, 2:-2, 2:-2]
+
+    wd = tempfile.mkdtemp(prefix="ps_shim_")
+    try:
+        ref_runs.prepare_wind(wd, 64, 32, every=steps, log=steps)
+        env = dict(os.environ, PS_LEARNED_COOLING=str(net))
+        r = subprocess.run([exe, "-maxsteps", str(steps - 1)], cwd=wd, env=env,
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+        assert "learned cooling step" in r.stdout
+        got = np.fromfile(os.path.join(wd, "data.0001.dbl"), dtype="<f8").reshape(want.shape)
+        rl = rel_l1(got, want)
+        print("learned step through the shim against the library's loop:", rl)
+        assert np.all(rl <= 1e-9), rl
+        rx = rel_l1(got, exact)
+        print("learned step through the shim against the reference method:", rx)
+        assert np.all(rx <= 1e-3), rx
     finally:
         shutil.rmtree(wd, ignore_errors=True)
