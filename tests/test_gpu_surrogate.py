@@ -239,3 +239,21 @@ def test_fallback_equals_reference_method(built, grid):
     acc, oob, rej, below, evals, stiff = sg.stats()
     assert acc == 0 and oob > 0
     batch.close()
+
+
+def test_train_network_tool_writes_a_loadable_network(built, tmp_path):
+    """pluto-sirocco_gb300/train_network.py (the network file for the
+    drop-in's PS_LEARNED_COOLING), on a small wind and a short training."""
+    import psgb
+    import train_network
+    out = tmp_path / "wind.psg"
+    assert train_network.main(["--grid", "128", "64", "--steps", "0", "10",
+                               "--per-snapshot", "4000", "--draws", "60000",
+                               "--train-steps", "3000", "--out", str(out)]) == 0
+    sg = psgb.Surrogate.load(out)
+    s = psgb.wind_model_solver(dict(grid=(128, 64), l_star=1e37, krad=0.2, alpharad=-0.6))
+    psgb.check(psgb.lib().ps_set_surrogate(s.ctx, sg.h, 1), "ps_set_surrogate")
+    sg.stats(reset=True)
+    assert s.run(6) & ~0x2 == 0
+    acc, oob, rej, below, evals, stiff = sg.stats()
+    assert acc > 0.9 * (acc + oob + rej)
