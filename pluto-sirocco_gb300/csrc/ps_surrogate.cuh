@@ -281,10 +281,13 @@ __device__ __forceinline__ double sg_z(const SgCtx &b, double T, double &dz, dou
 // kSgResidual, at most kSgMaxNewton evaluations, starting from the
 // network's prediction T0 when it moves T by more than kSgJump (from T when
 // from_net is false or the predicted change is small); a final Newton step
-// polishes the converged point.  Rejected: no convergence, z' <= 0, the net
-// rate at the root of opposite sign to the initial one (the reference then
-// solves for the equilibrium temperature instead), or a root on the wrong
-// side of T.  Sets hc_init.
+// polishes the converged point.  When the net rate at the converged point
+// has the opposite sign of the initial one, the answer is instead the
+// equilibrium temperature between T and that point (the reference's second
+// Brent solve, cooling.c:150-157), found by a bracketed Newton iteration
+// on the net rate (sg_judge_equilibrium).  Rejected: no convergence,
+// z' <= 0, or a root more than 1e-8 T on the wrong side of T.  Sets
+// hc_init.
 //
 // In three parts, so that a kernel can settle the non-stiff cells before
 // it knows whether it needs the network at all (sg_cool_items):
@@ -294,12 +297,62 @@ __device__ __forceinline__ double sg_z(const SgCtx &b, double T, double &dz, dou
 // the checks of both.
 constexpr int SG_PENDING = 4;
 
-__device__ __forceinline__ int sg_judge_final(const SgCtx &b, double T, double Tk, double z,
-                                              double dz, double hc, double &T_f)
+constexpr int kSgMaxEquil = 8;   // net-rate evaluations of the equilibrium iteration
+
+// The equilibrium temperature, the root of the net rate hc between T (rate
+// hc_init) and Tk (rate hc_k, of the opposite sign): Newton steps on hc,
+// each kept inside the bracket, which shrinks to the side whose rate has
+// the sign of the lower end's (a step that would leave it bisects
+// instead); converged when a step moves T by at most 1e-10 T.  dhc_k is
+// dhc/dT at Tk.
+__device__ __forceinline__ int sg_judge_equilibrium(const SgCtx &b, double T, double Tk,
+                                                    double hc_k, double dhc_k, double &T_f,
+                                                    int &evals)
 {
-  if (!gt0(dz) || lt0(hc * b.hc_init)) return SG_REJECT;
+  double lo = fmin(T, Tk), hi = fmax(T, Tk);
+  double flo = T <= Tk ? b.hc_init : hc_k;
+  double x = Tk, fx = hc_k, dfx = dhc_k;
+  for (int it = 0; it < kSgMaxEquil; it++) {
+    double xn = x - fx / dfx;
+    if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);   // outside, or not a number
+    double dfn;
+    const double fn = sg_heatcool_d(b, xn, dfn);
+    evals++;
+    if (lt0(fn * flo)) {
+      hi = xn;
+    } else {
+      lo = xn;
+      flo = fn;
+    }
+    const double step = fabs(xn - x);
+    x = xn;
+    fx = fn;
+    dfx = dfn;
+    if (step <= 1e-10 * x || fn == 0.0) {
+      if (!gt0(x) || !isfinite(x)) return SG_REJECT;
+      T_f = x;
+      return SG_ACCEPT;
+    }
+  }
+  return SG_REJECT;
+}
+
+__device__ __forceinline__ int sg_judge_final(const SgCtx &b, double T, double Tk, double z,
+                                              double dz, double hc, double &T_f, int &evals)
+{
+  if (!gt0(dz)) return SG_REJECT;
+  if (lt0(hc * b.hc_init)) {
+    // dhc/dT at Tk from z' = n kB 3/2 - dt dhc/dT / 2
+    const double dhc = (b.n * kKB * 1.5 - dz) * 2.0 / b.dt;
+    return sg_judge_equilibrium(b, T, Tk, hc, dhc, T_f, evals);
+  }
   const double Tn = Tk - z / dz;
-  if (!gt0(Tn) || !isfinite(Tn) || lt0((Tn - T) * b.hc_init)) return SG_REJECT;
+  // a root on the wrong side of T (against the initial net rate) is refused
+  // unless the move is below 1e-8 T: at thermal equilibrium dt hc is below
+  // the rounding of T n kB 3/2 - E and the step's sign is noise (the
+  // reference's Brent solve stops within 1 K)
+  if (!gt0(Tn) || !isfinite(Tn) || (lt0((Tn - T) * b.hc_init) && fabs(Tn - T) > 1e-8 * T))
+    return SG_REJECT;
   T_f = Tn;
   return SG_ACCEPT;
 }
@@ -313,7 +366,8 @@ __device__ __forceinline__ int sg_judge_first(SgCtx &b, double T, double &z, dou
   z = T * cth - b.E - b.dt * b.hc_init;
   dz = cth - b.dt * dhc * 0.5;
   if (!(fabs(z) <= kSgResidual * T * cth)) return SG_PENDING;
-  return sg_judge_final(b, T, T, z, dz, b.hc_init, T_f);
+  int evals = 1;   // hc at T is hc_init: no sign change, no further evaluation
+  return sg_judge_final(b, T, T, z, dz, b.hc_init, T_f, evals);
 }
 
 // evals counts the evaluation of sg_judge_first
@@ -336,7 +390,7 @@ __device__ __forceinline__ int sg_judge_rest(const SgCtx &b, double T, double T0
     evals++;
     conv = fabs(z) <= kSgResidual * Tk * cth;
   }
-  return sg_judge_final(b, T, Tk, z, dz, hc, T_f);
+  return sg_judge_final(b, T, Tk, z, dz, hc, T_f, evals);
 }
 
 __device__ __forceinline__ int sg_judge(SgCtx &b, double T, double T0, bool from_net, double &T_f,
