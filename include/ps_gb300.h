@@ -382,10 +382,12 @@ int  ps_batch_time_step_kernels(ps_batch *b, float ms[3]);
  * implicit energy equation judge and polish the result: a cell whose
  * residual at the old temperature is already within 1e-3 of its thermal
  * energy takes one Newton step from there; a stiff cell iterates from the
- * network's prediction (at most 5 net-rate evaluations in all).  A cell is
- * left to the reference method (bracket + Brent) when its inputs leave the
- * box, when the residual does not reach 1e-3, or when the net rate changes
- * sign (the reference's equilibrium branch).
+ * network's prediction (at most 5 net-rate evaluations in all); when the
+ * net rate at the solution has changed sign, the equilibrium temperature
+ * between the two is solved for, as the reference does.  A cell is left to
+ * the reference method (bracket + Brent) when its inputs leave the box,
+ * when the residual does not reach 1e-3, or when the energy equation is
+ * not monotone there (thermally unstable cells).
  * Parameter vector (FP32, 4545 values): W1[64][4], b1[64], W2[64][64],
  * b2[64], w3[64], b3. */
 typedef struct ps_surrogate ps_surrogate;
