@@ -157,6 +157,15 @@ __global__ void k_batch_gather_flags(const BatchModel *__restrict__ models, int 
 // are instantiated in ps_batch_c.cu (characteristic limiting), ps_batch7.cu
 // and ps_batch_c7.cu (the 7-variable state of ENTROPY_SWITCH contexts)
 const void *batch_kernel_c6(int shape, int lim, int solver, int stage);
+// the 6-variable primitive-PLM set, one translation unit per tile shape
+// (ps_batch6_s<shape>.cu), so that they build in parallel
+const void *batch_kernel6_s0(int lim, int solver, int stage);
+const void *batch_kernel6_s1(int lim, int solver, int stage);
+const void *batch_kernel6_s2(int lim, int solver, int stage);
+const void *batch_kernel6_s3(int lim, int solver, int stage);
+const void *batch_kernel6_s4(int lim, int solver, int stage);
+const void *batch_kernel6_s5(int lim, int solver, int stage);
+const void *batch_kernel6_s6(int lim, int solver, int stage);
 const void *batch_kernel7(int shape, int lim, int solver, int stage);
 const void *batch_kernel_c7(int shape, int lim, int solver, int stage);
 size_t batch_smem7(int shape);
@@ -166,8 +175,16 @@ static const void *batch_kernel(int nv, bool ch, int shape, int lim, int solver,
   if (nv == 7)
     return ch ? batch_kernel_c7(shape, lim, solver, stage)
               : batch_kernel7(shape, lim, solver, stage);
-  return ch ? batch_kernel_c6(shape, lim, solver, stage)
-            : batch_kernel_nv<6, false>(shape, lim, solver, stage);
+  if (ch) return batch_kernel_c6(shape, lim, solver, stage);
+  switch (shape) {
+    case 1: return batch_kernel6_s1(lim, solver, stage);
+    case 2: return batch_kernel6_s2(lim, solver, stage);
+    case 3: return batch_kernel6_s3(lim, solver, stage);
+    case 4: return batch_kernel6_s4(lim, solver, stage);
+    case 5: return batch_kernel6_s5(lim, solver, stage);
+    case 6: return batch_kernel6_s6(lim, solver, stage);
+    default: return batch_kernel6_s0(lim, solver, stage);
+  }
 }
 
 static size_t batch_smem(int nv, int shape)

@@ -92,18 +92,32 @@ const void *pick_batch_shape(int lim, int solver, int stage)
   return pick_batch<NV, CHAR, LIM_MC, HLLC, TL>(stage);
 }
 
-// CHAR: CHAR_LIMITING YES
+// One tile shape's kernels (CHAR: CHAR_LIMITING YES)
+template <int NV, bool CHAR, int S>
+const void *batch_kernel_s(int lim, int solver, int stage)
+{
+  if constexpr (S == 1) return pick_batch_shape<NV, CHAR, Tile2D<16, 16>>(lim, solver, stage);
+  else if constexpr (S == 2) return pick_batch_shape<NV, CHAR, Tile2D<64, 4>>(lim, solver, stage);
+  else if constexpr (S == 3) return pick_batch_shape<NV, CHAR, Shape3>(lim, solver, stage);
+  else if constexpr (S == 4)
+    return pick_batch_shape<NV, CHAR, typename Shape4<NV, CHAR>::T>(lim, solver, stage);
+  else if constexpr (S == 5)
+    return pick_batch_shape<NV, CHAR, typename Shape5<NV, CHAR>::T>(lim, solver, stage);
+  else if constexpr (S == 6) return pick_batch_shape<NV, CHAR, Shape6>(lim, solver, stage);
+  else return pick_batch_shape<NV, CHAR, Tile2D<32, 8>>(lim, solver, stage);
+}
+
 template <int NV, bool CHAR>
 const void *batch_kernel_nv(int shape, int lim, int solver, int stage)
 {
   switch (shape) {
-    case 1: return pick_batch_shape<NV, CHAR, Tile2D<16, 16>>(lim, solver, stage);
-    case 2: return pick_batch_shape<NV, CHAR, Tile2D<64, 4>>(lim, solver, stage);
-    case 3: return pick_batch_shape<NV, CHAR, Shape3>(lim, solver, stage);
-    case 4: return pick_batch_shape<NV, CHAR, typename Shape4<NV, CHAR>::T>(lim, solver, stage);
-    case 5: return pick_batch_shape<NV, CHAR, typename Shape5<NV, CHAR>::T>(lim, solver, stage);
-    case 6: return pick_batch_shape<NV, CHAR, Shape6>(lim, solver, stage);
-    default: return pick_batch_shape<NV, CHAR, Tile2D<32, 8>>(lim, solver, stage);
+    case 1: return batch_kernel_s<NV, CHAR, 1>(lim, solver, stage);
+    case 2: return batch_kernel_s<NV, CHAR, 2>(lim, solver, stage);
+    case 3: return batch_kernel_s<NV, CHAR, 3>(lim, solver, stage);
+    case 4: return batch_kernel_s<NV, CHAR, 4>(lim, solver, stage);
+    case 5: return batch_kernel_s<NV, CHAR, 5>(lim, solver, stage);
+    case 6: return batch_kernel_s<NV, CHAR, 6>(lim, solver, stage);
+    default: return batch_kernel_s<NV, CHAR, 0>(lim, solver, stage);
   }
 }
 

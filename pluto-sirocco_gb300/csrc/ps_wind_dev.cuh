@@ -46,6 +46,13 @@ struct WindDev {
 // device helpers
 // ------------------------------------------------------------------
 
+// The stage kernels whose products no add absorbs run on the integer pipes
+// (ps_dmul.cuh, the same bits as the FP64 unit's): the 6-variable
+// primitive-PLM set of the batched wind.  The characteristic-limiting and
+// entropy-switch sets keep the FP64 unit (and their build time).
+template <int NV, bool CHAR>
+constexpr bool kIntProducts = NV == NFLX + 1 && !CHAR;
+
 template <int LIM>
 __device__ __forceinline__ double limited_slope_general(double dvp, double dvm, double cp,
                                                         double cm)
@@ -66,39 +73,57 @@ __device__ __forceinline__ double limited_slope_general(double dvp, double dvm, 
   }
 }
 
-// The van Leer slopes of n variables of one cell with one division: the
-// denominators' reciprocals by Montgomery's simultaneous inversion (prefix
-// products, one reciprocal of the total, a backward pass).  Variables whose
-// one-sided differences have opposite signs get slope 0 and denominator 1.
-// When the product of the denominators leaves the normal range, each slope
-// takes its own division.  The slopes stay within a few ulps of the direct
-// quotients.
-template <int N>
-__device__ __forceinline__ void vl_slopes(const double (&dvp)[N], const double (&dvm)[N],
-                                          double cp, double cm, double (&dv)[N])
+// PLM of one cell with the van Leer limiter on the general grid: the
+// weighted one-sided differences, the slopes of all NV variables with one
+// division, the states at the cell's faces.  The denominators' reciprocals
+// come from Montgomery's simultaneous inversion (prefix products, one
+// reciprocal of the total, a backward pass); variables whose one-sided
+// differences have opposite signs get slope 0 and denominator 1; when the
+// product of the denominators leaves the normal range, each slope takes its
+// own division.  The slopes stay within a few ulps of the direct quotients.
+// The products that no add absorbs are formed by dmul_t<INT>: on the
+// integer pipes with INT (ps_dmul.cuh); a cell whose operands leave the
+// range of the integer product (`bad`) is done again with INT = false,
+// which gives the same bits wherever the integer form applies.  Each
+// variable's differences are formed where its numerator and denominator
+// are, and the cell values are read again for the face states, so that
+// few values stay live across the passes.
+template <int NV, bool INT, class G>
+__device__ __forceinline__ void plm_vl_cell(const double *__restrict__ sv,
+                                            double *__restrict__ svp,
+                                            double *__restrict__ svm, int s0, int sst, int q,
+                                            double wp, double wm, double cp, double cm,
+                                            double dp, double dm, bool &bad)
 {
   const double c2 = cp + cm - 2.0;
-  double num[N], den[N], pre[N];
+  double num[NV], den[NV], pre[NV];
   double prod = 1.0;
 #pragma unroll
-  for (int k = 0; k < N; k++) {
-    const double pm = dvp[k] * dvm[k];
+  for (int k = 0; k < NV; k++) {
+    const double v0 = sv[k * G::VS + s0];
+    const double dvp = dmul_t<INT>(sv[k * G::VS + s0 + sst] - v0, wp, bad);
+    const double dvm = dmul_t<INT>(v0 - sv[k * G::VS + s0 - sst], wm, bad);
+    const double pm = dmul_t<INT>(dvp, dvm, bad);
     const bool on = gt0(pm);
-    num[k] = on ? pm * (cp * dvm[k] + cm * dvp[k]) : 0.0;
-    den[k] = on ? dvp[k] * dvp[k] + dvm[k] * dvm[k] + c2 * pm : 1.0;
+    num[k] = on ? dmul_t<INT>(pm, fma(cm, dvp, dmul_t<INT>(cp, dvm, bad)), bad) : 0.0;
+    den[k] = on ? fma(c2, pm, fma(dvm, dvm, dmul_t<INT>(dvp, dvp, bad))) : 1.0;
     pre[k] = prod;
-    prod *= den[k];
+    prod = k == 0 ? den[0] : dmul_t<INT>(prod, den[k], bad);
   }
-  if (normal_pos(prod)) {
-    double r = 1.0 / prod;
+  const bool one = normal_pos(prod);
+  double r = one ? 1.0 / prod : 0.0;
 #pragma unroll
-    for (int k = N - 1; k >= 0; k--) {
-      dv[k] = num[k] * (r * pre[k]);
-      r *= den[k];
+  for (int k = NV - 1; k >= 0; k--) {
+    double dv;
+    if (one) {
+      dv = dmul_t<INT>(num[k], k == 0 ? r : dmul_t<INT>(r, pre[k], bad), bad);
+      if (k > 0) r = dmul_t<INT>(r, den[k], bad);
+    } else {
+      dv = num[k] / den[k];
     }
-  } else {
-#pragma unroll
-    for (int k = 0; k < N; k++) dv[k] = num[k] / den[k];
+    const double v0 = sv[k * G::VS + s0];
+    svp[k * G::NPMAX + q] = fma(dv, dp, v0);
+    svm[k * G::NPMAX + q] = fma(-dv, dm, v0);
   }
 }
 
@@ -502,15 +527,18 @@ __device__ __forceinline__ void ode_wind_cell(double *V, const double *xi_s, con
 
 // bilinear() of line_connect.c:746-777 with the weights of the target
 // point given: ans = (1-fy)((1-fx) v11 + fx v21) + fy((1-fx) v12 + fx v22)
+// (products by dmul_t<INT>, ps_dmul.cuh: the same bits either way)
+template <bool INT>
 __device__ __forceinline__ void bilinear_w(double fx, double fy, const double (&v11)[2],
                                            const double (&v12)[2], const double (&v21)[2],
-                                           const double (&v22)[2], double (&ans)[2])
+                                           const double (&v22)[2], double (&ans)[2], bool &bad)
 {
+  const double gx = 1.0 - fx, gy = 1.0 - fy;
 #pragma unroll
   for (int k = 0; k < 2; k++) {
-    const double t1 = (1.0 - fx) * v11[k] + fx * v21[k];
-    const double t2 = (1.0 - fx) * v12[k] + fx * v22[k];
-    ans[k] = (1.0 - fy) * t1 + fy * t2;
+    const double t1 = fma(fx, v21[k], dmul_t<INT>(gx, v11[k], bad));
+    const double t2 = fma(fx, v22[k], dmul_t<INT>(gx, v12[k], bad));
+    ans[k] = fma(fy, t2, dmul_t<INT>(gy, t1, bad));
   }
 }
 
@@ -598,6 +626,78 @@ __device__ __forceinline__ double line_force(const double (&vg)[NV], const LineL
 
 // CHAR: CHAR_LIMITING YES (a kernel of its own, so that the primitive
 // path keeps its register budget)
+// The right-hand side of one own cell in direction D (Src/MHD/rhs.c:234-351,
+// 423-630; Src/MHD/rhs_source.c:101-420): -dt/dV (F_r A_r - F_l A_l) with
+// the area and dt/dV folded into one weight per face (the phi momentum's
+// face factors as well), the pressure gradient, the curvilinear source of
+// the momentum along D, gravity and the line force `glf` (both along x1
+// only in this problem; the reference's x2 and x3 components of gravity
+// and the x3 component of the line force are exact zeros and are left
+// out); with stage1 the cell's CFL sum `cdt` gains its term.  vc is the
+// face-averaged state for D = 0 and the cell value for D = 1.  Products by
+// dmul_t<INT> (on the integer pipes with INT, the same bits either way).
+template <int D, int NV, bool INT, class G>
+__device__ __forceinline__ void sph_rhs(const double *__restrict__ sf,
+                                        const double *__restrict__ spr,
+                                        const double *__restrict__ scm, const double (&vc)[NV],
+                                        double glf, const WindStageArgs &A, int gi, int gj,
+                                        int ql, int qr, double dt, double dtdV, bool stage1,
+                                        double (&rhs)[NV], double &cdt, bool &bad)
+{
+  constexpr int VN = VX1 + D;
+  const SphGeom &g = A.g;
+  double Al, Ar, fl_phi, fr_phi, dtdl;
+  if (D == 0) {
+    Al = dmul_t<INT>(g.A1f[gi - 1], g.dmu[gj], bad);
+    Ar = dmul_t<INT>(g.A1f[gi], g.dmu[gj], bad);
+    fl_phi = g.absx1p[gi - 1];
+    fr_phi = g.absx1p[gi];
+    dtdl = A.s.dtdx[0][gi];
+  } else {
+    Al = dmul_t<INT>(g.rdr[gi], g.sxp[gj - 1], bad);
+    Ar = dmul_t<INT>(g.rdr[gi], g.sxp[gj], bad);
+    fl_phi = g.spabs[gj - 1];
+    fr_phi = g.spabs[gj];
+    dtdl = dmul_t<INT>(A.s.dtdx[1][gj], g.rtinv[gi], bad);
+  }
+  const double cl = dmul_t<INT>(dtdV, Al, bad), cr = -dmul_t<INT>(dtdV, Ar, bad);
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    const double wl = nv == VX3 ? dmul_t<INT>(cl, fl_phi, bad) : cl;
+    const double wr = nv == VX3 ? dmul_t<INT>(cr, fr_phi, bad) : cr;
+    rhs[nv] = fma(sf[nv * G::NFMAX + ql], wl, dmul_t<INT>(sf[nv * G::NFMAX + qr], wr, bad));
+  }
+  rhs[VN] = fma(-dtdl, spr[qr] - spr[ql], rhs[VN]);
+  rhs[VX3] = dmul_t<INT>(rhs[VX3], D == 0 ? g.inv_absx1[gi] : g.inv_sn[gj], bad);
+  const double mflux = sf[RHO * G::NFMAX + qr] + sf[RHO * G::NFMAX + ql];
+  const double dtr = dmul_t<INT>(dt, vc[RHO], bad);
+  const double dtm = dmul_t<INT>(dhalf_t<INT>(dt, bad), mflux, bad);
+  const double vphi = vc[VX3];
+  if (D == 0) {
+    const double Sm =
+        dmul_t<INT>(vc[RHO], fma(vphi, vphi, dmul_t<INT>(vc[VX2], vc[VX2], bad)), bad);
+    rhs[VX1] = fma(dmul_t<INT>(dt, Sm, bad), g.rinv[gi], rhs[VX1]);
+    if (A.w.body_force) {
+      const double g0 = g.g0[gi];
+      rhs[VX1] = fma(dtr, g0, rhs[VX1]);
+      rhs[PRS] = fma(dtm, g0, rhs[PRS]);
+    }
+  } else {
+    const double Sm = dmul_t<INT>(
+        vc[RHO],
+        fma(dmul_t<INT>(g.ct[gj], vphi, bad), vphi, -dmul_t<INT>(vc[VX2], vc[VX1], bad)), bad);
+    rhs[VX2] = fma(dmul_t<INT>(dt, Sm, bad), g.rtinv[gi], rhs[VX2]);
+  }
+  if (A.w.line_force) {
+    rhs[VN] = fma(dtr, glf, rhs[VN]);
+    rhs[PRS] = fma(dtm, glf, rhs[PRS]);
+  }
+  if (stage1) {
+    const double inv_dl = D == 0 ? g.inv_dx1[gi] : dmul_t<INT>(g.inv_dx2[gj], g.rinv[gi], bad);
+    cdt = fma(dhalf_t<INT>(scm[ql] + scm[qr], bad), inv_dl, cdt);
+  }
+}
+
 template <int D, int NV, int LIM, int SOLVER, class TL, bool CHAR>
 __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double *__restrict__ svp,
                                           double *__restrict__ svm, double *__restrict__ sf,
@@ -607,6 +707,7 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
                                           const WindStageArgs &A, bool stage1, int ox, int oy)
 {
   using G = TileGeom<TL>;
+  constexpr bool IP = kIntProducts<NV, CHAR>;
   constexpr int PX = G::ext(0, D, 2), PY = G::ext(1, D, 2);
   constexpr int FX = G::ext(0, D, 1), FY = G::ext(1, D, 1);
   constexpr int NP = PX * PY, NF = FX * FY;
@@ -666,19 +767,10 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
       continue;
     }
     if constexpr (LIM == LIM_VL) {
-      double v0[NV], dvp[NV], dvm[NV], dv[NV];
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) {
-        v0[nv] = sv[nv * G::VS + s0];
-        dvp[nv] = (sv[nv * G::VS + s0 + SST] - v0[nv]) * wp;
-        dvm[nv] = (v0[nv] - sv[nv * G::VS + s0 - SST]) * wm;
-      }
-      vl_slopes<NV>(dvp, dvm, cp, cm, dv);
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) {
-        svp[nv * G::NPMAX + q] = v0[nv] + dv[nv] * dp;
-        svm[nv * G::NPMAX + q] = v0[nv] - dv[nv] * dm;
-      }
+      // on the FP64 unit: the integer form's live values cost the 16x16
+      // tiles at three CTAs per multiprocessor more in spills than it saves
+      bool bad = false;
+      plm_vl_cell<NV, false, G>(sv, svp, svm, s0, SST, q, wp, wm, cp, cm, dp, dm, bad);
       continue;
     }
 #pragma unroll
@@ -715,7 +807,11 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
         }
       }
     }
-    riemann<NV, SOLVER, VN>(vL, vR, gam, p.igmm1, f, pr, cmx, hll);
+    bool bad = false;
+    riemann_t<NV, SOLVER, VN, IP>(vL, vR, gam, p.igmm1, f, pr, cmx, hll, bad);
+    if constexpr (IP) {
+      if (bad) riemann_t<NV, SOLVER, VN, false>(vL, vR, gam, p.igmm1, f, pr, cmx, hll, bad);
+    }
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) sf[nv * G::NFMAX + q] = f[nv];
     spr[q] = pr;
@@ -728,79 +824,78 @@ __device__ __forceinline__ void sweep_sph(const double *__restrict__ sv, double 
     const int ql = cy * FX + cx;
     constexpr int FST = D == 0 ? 1 : FX;
     const int qr = ql + FST;
-    double Al, Ar, fl_phi, fr_phi, dtdl;
-    if (D == 0) {
-      Al = g.A1f[gi - 1] * g.dmu[gj];
-      Ar = g.A1f[gi] * g.dmu[gj];
-      fl_phi = g.absx1p[gi - 1];
-      fr_phi = g.absx1p[gi];
-      dtdl = A.s.dtdx[0][gi];
-    } else {
-      Al = g.rdr[gi] * g.sxp[gj - 1];
-      Ar = g.rdr[gi] * g.sxp[gj];
-      fl_phi = g.spabs[gj - 1];
-      fr_phi = g.spabs[gj];
-      dtdl = A.s.dtdx[1][gj] * g.rtinv[gi];
-    }
-    // -dt/dV (F_r A_r - F_l A_l) with the area and dt/dV folded into one
-    // weight per face (the phi momentum's face factors as well)
-    double rhs[NV];
-    const double cl = dtdV * Al, cr = -dtdV * Ar;
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      const double wl = nv == VX3 ? cl * fl_phi : cl, wr = nv == VX3 ? cr * fr_phi : cr;
-      rhs[nv] = sf[nv * G::NFMAX + qr] * wr + sf[nv * G::NFMAX + ql] * wl;
-    }
-    rhs[VN] -= dtdl * (spr[qr] - spr[ql]);
-    rhs[VX3] *= D == 0 ? g.inv_absx1[gi] : g.inv_sn[gj];
-    const double mflux = sf[RHO * G::NFMAX + qr] + sf[RHO * G::NFMAX + ql];
     double vc[NV];
     if (D == 0) {
       // face-averaged state of the cell: mean of its own + and - states
-      constexpr int PSTC = 1;
-      const int pc = cy * PX + cx + PSTC;
+      const int pc = cy * PX + cx + 1;
+      bool bad = !IP;
+      if constexpr (IP) {
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++)
-        vc[nv] = 0.5 * (svp[nv * G::NPMAX + pc] + svm[nv * G::NPMAX + pc]);
-      const double r_1 = g.rinv[gi];
-      const double vphi = vc[VX3];
-      const double Sm = vc[RHO] * (vc[VX2] * vc[VX2] + vphi * vphi);
-      rhs[VX1] += dt * Sm * r_1;
-      if (A.w.body_force) {
-        const double g0 = g.g0[gi];
-        rhs[VX1] += dt * vc[RHO] * g0;
-        rhs[PRS] += dt * 0.5 * mflux * g0;
+        for (int nv = 0; nv < NV; nv++)
+          vc[nv] = dhalf_int(svp[nv * G::NPMAX + pc] + svm[nv * G::NPMAX + pc], bad);
       }
-      if (A.w.line_force) {
-        const double gr = line_force<NV>(vc, A.L, A.w, e0, e1, 0, vcell(p, gj, gi), p.vstride);
-        rhs[VX1] += dt * vc[RHO] * gr;
-        rhs[PRS] += dt * 0.5 * mflux * gr;
+      if (bad) {
+#pragma unroll
+        for (int nv = 0; nv < NV; nv++)
+          vc[nv] = 0.5 * (svp[nv * G::NPMAX + pc] + svm[nv * G::NPMAX + pc]);
       }
     } else {
       const int s0 = (cy + TL::HY) * G::SX + cx + TL::HX;
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) vc[nv] = sv[nv * G::VS + s0];
-      const double r_1 = g.rtinv[gi], ct = g.ct[gj];
-      const double vphi = vc[VX3];
-      // the reference also adds the x2 and x3 components of the point-mass
-      // gravity and the x3 component of the line force, all exact zeros
-      // (rhs_source.c:339-396); they are left out
-      const double Sm = vc[RHO] * (-vc[VX2] * vc[VX1] + ct * vphi * vphi);
-      rhs[VX2] += dt * Sm * r_1;
-      if (A.w.line_force) {
-        const double gt = line_force<NV>(vc, A.L, A.w, e0, e1, 1, vcell(p, gj, gi), p.vstride);
-        rhs[VX2] += dt * vc[RHO] * gt;
-        rhs[PRS] += dt * 0.5 * mflux * gt;
-      }
+    }
+    const double glf =
+        A.w.line_force ? line_force<NV>(vc, A.L, A.w, e0, e1, D, vcell(p, gj, gi), p.vstride) : 0.0;
+    double rhs[NV], cdt1 = cdt;
+    bool bad = false;
+    sph_rhs<D, NV, IP, G>(sf, spr, scm, vc, glf, A, gi, gj, ql, qr, dt, dtdV, stage1, rhs, cdt1,
+                          bad);
+    if (IP && bad) {
+      cdt1 = cdt;
+      sph_rhs<D, NV, false, G>(sf, spr, scm, vc, glf, A, gi, gj, ql, qr, dt, dtdV, stage1, rhs,
+                               cdt1, bad);
     }
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) U[nv] += rhs[nv];
-    if (stage1) {
-      const double inv_dl = D == 0 ? g.inv_dx1[gi] : g.inv_dx2[gj] * g.rinv[gi];
-      cdt += 0.5 * (scm[ql] + scm[qr]) * inv_dl;
-    }
+    cdt = cdt1;
   }
   __syncthreads();
+}
+
+// dv/ds of one bin of VGradCalc (line_connect.c:690-717): the velocity at
+// the bin's far point (bilinear in the cell's four corner velocities) and at
+// the cell, projected on the bin's direction, differenced over the path.
+template <bool INT>
+__device__ __forceinline__ void vgrad_bin(const LineList &L, int e, double ids,
+                                          const double (&v11)[2], const double (&v12)[2],
+                                          const double (&v21)[2], const double (&v22)[2],
+                                          const double (&ans1)[2], double &dvds, bool &bad)
+{
+  double ans2[2];
+  bilinear_w<INT>(L.fr1[e], L.fr2[e], v11, v12, v21, v22, ans2, bad);
+  const double v1 = fma(ans1[1], L.c1b[e], dmul_t<INT>(ans1[0], L.c1a[e], bad));
+  const double v2 = fma(ans2[1], L.c2b[e], dmul_t<INT>(ans2[0], L.c2a[e], bad));
+  dvds = dmul_t<INT>(fabs(v2 - v1), ids, bad);
+}
+
+// The end of a stage for one own cell: with STAGE 2 the RK2 average
+// U = U0 / 2 + U / 2 with U0 from V^n (halvings are exact, so this is the
+// reference's 0.5 U0 + 0.5 U); then ConsToPrim.  U holds the stage's
+// conserved state on entry and the (repaired) state on return.
+template <int NV, int STAGE, bool INT>
+__device__ __forceinline__ unsigned stage_out(double (&U)[NV], double (&v)[NV],
+                                              const StageArgs &a, const Params &p,
+                                              long long cell, int ent, bool &bad)
+{
+  if constexpr (STAGE == 2) {
+    double v0[NV], U0[NV];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
+    prim_to_cons_t<NV, INT>(v0, U0, p.igmm1, bad);
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) U[nv] = dhalf_t<INT>(U0[nv], bad) + dhalf_t<INT>(U[nv], bad);
+  }
+  return cons_to_prim_t<NV, INT>(U, v, p.gmm1, ent, bad);
 }
 
 // One tile (bx, by) of one stage of one wind grid.
@@ -809,6 +904,7 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
                                                int bx, int by, unsigned char *smem_raw)
 {
   using G = TileGeom<TL>;
+  constexpr bool IP = kIntProducts<NV, CHAR>;
   double *sv = reinterpret_cast<double *>(smem_raw);
   double *svp = sv + NV * G::VS;
   double *svm = svp + NV * G::NPMAX;
@@ -857,8 +953,21 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
     for (int k = tid; k < CX * CY; k += G::NT) {
       const int kx = k % CX, ky = k / CX;
       const int s = (ky + TL::HY) * G::SX + kx + TL::HX, sm = s - G::SX;
-      sf[k] = (V1[sm - 1] + V1[sm] + V1[s - 1] + V1[s]) / 4.0;
-      sf[CX * CY + k] = (V2[sm - 1] + V2[sm] + V2[s - 1] + V2[s]) / 4.0;
+      // the quotients by 4 as exact quarterings on the integer pipes
+      const double s1 = V1[sm - 1] + V1[sm] + V1[s - 1] + V1[s];
+      const double s2 = V2[sm - 1] + V2[sm] + V2[s - 1] + V2[s];
+      bool bad = !IP;
+      double c1 = 0.0, c2 = 0.0;
+      if constexpr (IP) {
+        c1 = dpow2m_int<2>(s1, bad);
+        c2 = dpow2m_int<2>(s2, bad);
+      }
+      if (bad) {
+        c1 = s1 / 4.0;
+        c2 = s2 / 4.0;
+      }
+      sf[k] = c1;
+      sf[CX * CY + k] = c2;
     }
     __syncthreads();
   }
@@ -875,17 +984,21 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
   int e0 = 0, e1 = 0;
   unsigned flags = 0;
   if (own) {
+    bool bad = false;
     if constexpr (STAGE == 1) {
       double v[NV];
       const int s0 = (cy + TL::HY) * G::SX + cx + TL::HX;
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v[nv] = sv[nv * G::VS + s0];
-      prim_to_cons<NV>(v, U, p.igmm1);
+      prim_to_cons_t<NV, IP>(v, U, p.igmm1, bad);
+      if (IP && bad) prim_to_cons_t<NV, false>(v, U, p.igmm1, bad);
     } else {
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = a.Us[nv * p.vstride + cell];
     }
-    dtdV = dt * g.inv_dVr[gi] * g.inv_dmu[gj];
+    bad = bad || !IP;
+    if constexpr (IP) dtdV = dmul_int(dmul_int(dt, g.inv_dVr[gi], bad), g.inv_dmu[gj], bad);
+    if (bad) dtdV = dt * g.inv_dVr[gi] * g.inv_dmu[gj];
     if (A.w.line_force) {
       // VGradCalc for the bins of this cell (line_connect.c:628-738)
       const int dc = (oy + cy) * p.nx[0] + (ox + cx);
@@ -902,7 +1015,9 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
       v22[1] = cv2[k0 + CX + 1];
       v21[0] = cv1[k0 + 1];
       v21[1] = cv2[k0 + 1];
-      bilinear_w(g.fx[gi], g.fy[gj], v11, v12, v21, v22, ans1);
+      bool bad = false;
+      bilinear_w<IP>(g.fx[gi], g.fy[gj], v11, v12, v21, v22, ans1, bad);
+      if (IP && bad) bilinear_w<false>(g.fx[gi], g.fy[gj], v11, v12, v21, v22, ans1, bad);
       const double alpha = A.w.alpharad;
       // two or more bins: the bin's factor k C^alpha (dv/ds)^-alpha is kept
       // instead of its log, so that each sweep needs one power of rho p and
@@ -912,11 +1027,10 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
         const double ids = A.L.inv_ds[e];
         double lq = A.w.mfit ? -INFINITY : 0.0;
         if (ids != 0.0) {
-          double ans2[2];
-          bilinear_w(A.L.fr1[e], A.L.fr2[e], v11, v12, v21, v22, ans2);
-          const double v1 = ans1[0] * A.L.c1a[e] + ans1[1] * A.L.c1b[e];
-          const double v2 = ans2[0] * A.L.c2a[e] + ans2[1] * A.L.c2b[e];
-          const double dvds = fabs(v2 - v1) * ids;
+          double dvds;
+          bool badb = false;
+          vgrad_bin<IP>(A.L, e, ids, v11, v12, v21, v22, ans1, dvds, badb);
+          if (IP && badb) vgrad_bin<false>(A.L, e, ids, v11, v12, v21, v22, ans1, dvds, badb);
           if (is_nan_bits(dvds)) flags |= F_NAN;
           if (gt0(dvds))
             lq = A.w.mfit ? -log10(dvds)
@@ -935,14 +1049,6 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
 
   if (own) {
     double v[NV];
-    if constexpr (STAGE == 2) {
-      double v0[NV], U0[NV];
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
-      prim_to_cons<NV>(v0, U0, p.igmm1);
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) U[nv] = 0.5 * U0[nv] + 0.5 * U[nv];
-    }
     int ent = 0;
     if constexpr (NV == NFLX + 2) {
       // FLAG_ENTROPY: every zone with ALWAYS; with SELECTIVE not in or next
@@ -955,7 +1061,21 @@ __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const Wind
         if (e & 2) ent = 1;
       }
     }
-    flags |= cons_to_prim<NV>(U, v, p.gmm1, ent);
+    // stage 2: U = (U0 + U*) / 2 with U0 from V^n; then the primitive state
+    // (the integer form first, again on the FP64 unit if it hands back)
+    double Uw[NV];
+    bool bad = false;
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) Uw[nv] = U[nv];
+    unsigned f = stage_out<NV, STAGE, IP>(Uw, v, a, p, cell, ent, bad);
+    if (IP && bad) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) Uw[nv] = U[nv];
+      f = stage_out<NV, STAGE, false>(Uw, v, a, p, cell, ent, bad);
+    }
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) U[nv] = Uw[nv];
+    flags |= f;
 #pragma unroll
     for (int nv = 0; nv < NV; nv++)
       if (is_nan_bits(v[nv])) flags |= F_NAN;

@@ -11,12 +11,19 @@
 //                        some lanes active (how the cost of a double-
 //                        precision instruction depends on the active lanes,
 //                        for the kernels that run few cells per warp);
+//   ps_probe_dmul_rate   throughput of binary64 products on the FP64 unit,
+//                        on the integer pipes (csrc/ps_dmul.cuh) and in
+//                        mixes of the two;
+//   ps_probe_dmul_check  the integer product against the hardware multiply,
+//                        bit for bit, on the GPU or (the same code compiled
+//                        for the host) against the host's multiply;
 //   ps_probe_wait_timeout
 //                        the bounded mbarrier wait of the stage and learned-
 //                        step kernels (ps_tma.cuh) on a barrier that nothing
 //                        completes: it must give up after its poll limit and
 //                        report, leaving the context usable (the failure test
 //                        of a wait, without a GPU fault).
+#include "ps_dmul.cuh"
 #include "ps_fastmath.cuh"
 #include "ps_tma.cuh"
 
@@ -87,7 +94,207 @@ __global__ void k_fastmath(int op, const double *x, double *fast, double *ref, l
   }
 }
 
+// `emul` of every 8 chains take the integer product, the others the FP64
+// unit's; the multipliers alternate between m0 and m1 so that the chains
+// stay near 1
+template <int EMUL>
+__global__ void k_dmul_rate(double *out, int iters, double m0, double m1)
+{
+  double x[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; c++) x[c] = 1.0 + (double)(threadIdx.x + c) * 1e-6;
+  bool bad = false;
+  for (int it = 0; it < iters; it++) {
+    const double m = (it & 1) ? m0 : m1;
+#pragma unroll
+    for (int c = 0; c < kChains; c++) x[c] = c < EMUL ? dmul_int(x[c], m, bad) : __dmul_rn(x[c], m);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < kChains; c++) s += x[c];
+  if (s == 12345.678 || bad) out[0] = s;
+}
+
+// Operand pairs for the check, five kinds by i % 5: exponents near the
+// middle of the range; short significands (exact products and exact ties);
+// any bit pattern; products near either end of the normal range; zeros,
+// powers of two and sign mixes.
+__host__ __device__ __forceinline__ uint64_t dm_mix(uint64_t z)
+{
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__host__ __device__ __forceinline__ void dm_pair(uint64_t seed, long long i, uint64_t &A,
+                                                 uint64_t &B)
+{
+  const uint64_t k0 = seed + 4ull * (uint64_t)i;
+  A = dm_mix(k0);
+  B = dm_mix(k0 + 1);
+  const uint64_t r0 = dm_mix(k0 + 2), r1 = dm_mix(k0 + 3);
+  const uint64_t SG = 0x8000000000000000ull, MT = 0x000fffffffffffffull;
+  switch ((int)(i % 5)) {
+    case 0:
+      A = (A & (SG | MT)) | ((uint64_t)(923 + r0 % 200) << 52);
+      B = (B & (SG | MT)) | ((uint64_t)(923 + r1 % 200) << 52);
+      break;
+    case 1: {
+      const int ka = 1 + (int)(r0 % 53), kb = 1 + (int)((r0 >> 8) % 53);
+      const uint64_t ma = ka == 1 ? 0 : (A & MT) >> (53 - ka) << (53 - ka);
+      const uint64_t mb = kb == 1 ? 0 : (B & MT) >> (53 - kb) << (53 - kb);
+      A = (A & SG) | ma | ((uint64_t)(993 + r1 % 60) << 52);
+      B = (B & SG) | mb | ((uint64_t)(993 + (r1 >> 8) % 60) << 52);
+      break;
+    }
+    case 2:
+      break;
+    case 3: {
+      const int ea = (int)(r0 % 2048);
+      const int target = (r1 & 1) ? 2042 + (int)((r1 >> 1) % 8) : -3 + (int)((r1 >> 1) % 8);
+      int eb = target - ea + 1023;
+      eb = eb < 0 ? 0 : (eb > 2047 ? 2047 : eb);
+      A = (A & (SG | MT)) | ((uint64_t)ea << 52);
+      B = (B & (SG | MT)) | ((uint64_t)eb << 52);
+      break;
+    }
+    default: {
+      const int k = (int)(r0 % 4);
+      if (k == 0) A &= SG;
+      else if (k == 1) B &= SG;
+      else if (k == 2) A &= 0xfff0000000000000ull;
+      break;
+    }
+  }
+}
+
+// cnt[0]: pairs whose integer product differs from the hardware's,
+// cnt[1]: pairs handed back (bad); first[0..1]: the first differing pair
+__global__ void k_dmul_check(uint64_t seed, long long n, unsigned long long *cnt,
+                             unsigned long long *first)
+{
+  unsigned long long mism = 0, nbad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    uint64_t A, B;
+    dm_pair(seed, i, A, B);
+    const double a = dm_double(A), b = dm_double(B);
+    bool bad = false, bh = false, bq = false;
+    const double r = dmul_int(a, b, bad);
+    const double h = dpow2m_int<1>(a, bh), qt = dpow2m_int<2>(a, bq);
+    const bool off = (!bad && dm_bits(r) != dm_bits(__dmul_rn(a, b))) ||
+                     (!bh && dm_bits(h) != dm_bits(__dmul_rn(a, 0.5))) ||
+                     (!bq && dm_bits(qt) != dm_bits(__dmul_rn(a, 0.25)));
+    if (bad) nbad++;
+    if (off) {
+      if (atomicCAS(first + 2, 0ull, 1ull) == 0ull) {
+        first[0] = A;
+        first[1] = B;
+      }
+      mism++;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mism += __shfl_down_sync(0xffffffffu, mism, o);
+    nbad += __shfl_down_sync(0xffffffffu, nbad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(cnt, mism);
+    atomicAdd(cnt + 1, nbad);
+  }
+}
+
 }  // namespace ps
+
+// Milliseconds of `iters` steps of 8 product chains per thread, `emul`
+// (0..8) of them on the integer pipes, on `blocks` CTAs of `warps` warps
+// (best of 3 after a warm-up); -1 on a bad argument or a CUDA error.
+extern "C" double ps_probe_dmul_rate(int emul, int blocks, int warps, int iters)
+{
+  if (emul < 0 || emul > 8 || blocks < 1 || blocks > 65535 || warps < 1 || warps > 32 ||
+      iters < 1)
+    return -1.0;
+  using K = void (*)(double *, int, double, double);
+  const K ks[9] = {ps::k_dmul_rate<0>, ps::k_dmul_rate<1>, ps::k_dmul_rate<2>,
+                   ps::k_dmul_rate<3>, ps::k_dmul_rate<4>, ps::k_dmul_rate<5>,
+                   ps::k_dmul_rate<6>, ps::k_dmul_rate<7>, ps::k_dmul_rate<8>};
+  const double m0 = 1.0 + 0x1p-20, m1 = 1.0 / m0;
+  double *out = nullptr;
+  if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return -1.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  ks[emul]<<<blocks, 32 * warps>>>(out, 16, m0, m1);
+  float best = -1.f;
+  for (int r = 0; r < 3; r++) {
+    cudaEventRecord(e0);
+    ks[emul]<<<blocks, 32 * warps>>>(out, iters, m0, m1);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (best < 0.f || ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  return best;
+}
+
+// n operand pairs (dm_pair) through the integer product, and the first
+// operand through the exact halving and quartering, compared bit for bit
+// with the GPU's multiply (on_gpu 1) or the host's (on_gpu 0).  out[0]:
+// pairs with a differing result, out[1]: products handed back (bad),
+// out[2..3]: the first differing pair's bit patterns.  Returns 0, or -1 on a bad argument or a
+// CUDA error.
+extern "C" int ps_probe_dmul_check(int on_gpu, unsigned long long seed, long long n,
+                                   unsigned long long *out)
+{
+  if (n < 0 || !out) return -1;
+  out[0] = out[1] = out[2] = out[3] = 0;
+  if (!on_gpu) {
+    bool seen = false;
+    for (long long i = 0; i < n; i++) {
+      uint64_t A, B;
+      ps::dm_pair(seed, i, A, B);
+      const double a = ps::dm_double(A), b = ps::dm_double(B);
+      bool bad = false, bh = false, bq = false;
+      const double r = ps::dmul_int(a, b, bad);
+      const double h = ps::dpow2m_int<1>(a, bh), qt = ps::dpow2m_int<2>(a, bq);
+      const volatile double ref = a * b, rh = a * 0.5, rq = a * 0.25;
+      const bool off = (!bad && ps::dm_bits(r) != ps::dm_bits(ref)) ||
+                       (!bh && ps::dm_bits(h) != ps::dm_bits(rh)) ||
+                       (!bq && ps::dm_bits(qt) != ps::dm_bits(rq));
+      if (bad) out[1]++;
+      if (off) {
+        if (!seen) {
+          out[2] = A;
+          out[3] = B;
+          seen = true;
+        }
+        out[0]++;
+      }
+    }
+    return 0;
+  }
+  unsigned long long *d = nullptr;
+  if (cudaMalloc(&d, 5 * sizeof(unsigned long long)) != cudaSuccess) return -1;
+  cudaError_t e = cudaMemset(d, 0, 5 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    ps::k_dmul_check<<<4096, 256>>>(seed, n, d, d + 2);
+    e = cudaGetLastError();
+  }
+  unsigned long long h[5] = {0, 0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = h[2];
+  out[3] = h[3];
+  return e == cudaSuccess ? 0 : -1;
+}
 
 // op 0: exp, 1: log.  x, fast and ref are host arrays of n doubles; returns
 // 0 or -1 on a CUDA error.

@@ -89,9 +89,11 @@ def build_lib(force=False, verbose=False):
 
 def build_probe(force=False):
     """libps_probe.so: measurement helpers for bench.py and the tests (the
-    FP64 issue-rate probe, the fast-math check); not part of the C ABI."""
+    FP64 issue-rate probe, the fast-math check, the integer product's rate
+    and check); not part of the C ABI."""
     deps = [PROBE_SRC, os.path.join(CSRC, "ps_fastmath.cuh"),
-            os.path.join(CSRC, "ps_fastmath_tables.cuh")]
+            os.path.join(CSRC, "ps_fastmath_tables.cuh"), os.path.join(CSRC, "ps_dmul.cuh"),
+            os.path.join(CSRC, "ps_tma.cuh")]
     if force or _newer(deps, PROBE):
         _run([nvcc()] + ARCH + NVFLAGS + ["-shared", PROBE_SRC, "-o", PROBE, "-lcudart"])
     return PROBE

@@ -201,6 +201,10 @@ def probe():
         L.ps_probe_fastmath.argtypes = [ctypes.c_int, DP, DP, DP, ctypes.c_long]
         L.ps_probe_fp64_lanes.argtypes = [ctypes.c_int] * 5
         L.ps_probe_fp64_lanes.restype = ctypes.c_double
+        L.ps_probe_dmul_rate.argtypes = [ctypes.c_int] * 4
+        L.ps_probe_dmul_rate.restype = ctypes.c_double
+        L.ps_probe_dmul_check.argtypes = [ctypes.c_int, ctypes.c_ulonglong, ctypes.c_longlong,
+                                          ctypes.POINTER(ctypes.c_ulonglong)]
         L.ps_probe_wait_timeout.argtypes = [ctypes.c_int, ctypes.c_int,
                                             ctypes.POINTER(ctypes.c_int)]
         _probe = L
