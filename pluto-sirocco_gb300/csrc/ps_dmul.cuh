@@ -106,6 +106,15 @@ __host__ __device__ __forceinline__ double dhalf_int(double x, bool &bad)
 {
   return dpow2m_int<1>(x, bad);
 }
+// 4 x, exact when x and the result are normal
+__host__ __device__ __forceinline__ double dquad_int(double x, bool &bad)
+{
+  const uint64_t X = dm_bits(x);
+  const uint32_t e = (uint32_t)(X >> 52) & 0x7ffu;
+  const bool z = (X << 1) == 0u;
+  bad = bad | (!z && e - 1u >= 2044u);
+  return z ? x : dm_double(X + (2ull << 52));
+}
 
 #ifdef __CUDACC__
 // The product on the integer pipes (INT) or on the FP64 unit.  The hardware
@@ -127,6 +136,14 @@ __device__ __forceinline__ double dhalf_t(double x, bool &bad)
     return dhalf_int(x, bad);
   else
     return __dmul_rn(0.5, x);
+}
+template <bool INT>
+__device__ __forceinline__ double dquad_t(double x, bool &bad)
+{
+  if constexpr (INT)
+    return dquad_int(x, bad);
+  else
+    return __dmul_rn(4.0, x);
 }
 #endif
 

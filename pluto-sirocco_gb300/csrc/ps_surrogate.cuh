@@ -219,47 +219,62 @@ struct SgCtx {
 //   line term 1e-16 e^(-1.3e5/T) / (sqrt(xi) T): ' = term (1.3e5/T - 1) / T;
 //   the min() term: 0, 2.5e-27/sqrt(T) or -1.5e-17/T^2 by the active branch;
 //   brem' = brem / (2T).
-__device__ __forceinline__ double sg_heatcool_d(const SgCtx &b, double T, double &dhc)
+template <bool INT>
+__device__ __forceinline__ double sg_heatcool_d_t(const SgCtx &b, double T, double &dhc,
+                                                  bool &bad)
 {
+  // products no add absorbs by dmul_t<INT> (on the integer pipes with INT,
+  // ps_dmul.cuh; the same bits either way)
   // 1/T and sqrt(T) from one reciprocal square root (the judge's own
   // arithmetic: it only has to find the root the network points at)
-  const double rT = rsqrt(T), sqT = T * rT, iT = rT * rT;
+  const double rT = rsqrt(T), sqT = dmul_t<INT>(T, rT, bad), iT = dmul_t<INT>(rT, rT, bad);
   double r, dr;
   if (T < 1.5e4) {
     const double q = fm::exp(2.302585092994046 * (-51.59417133) + 12.27740153 * fm::log(T));
     r = 1e-2 + q;
-    dr = 12.27740153 * q * iT;
+    dr = dmul_t<INT>(dmul_t<INT>(12.27740153, q, bad), iT, bad);
   } else if (T < 3.3e4) {
     const double q = fm::exp(2.302585092994046 * (-3.80749689) + 0.86092628 * fm::log(T));
     r = q;
-    dr = 0.86092628 * q * iT;
+    dr = dmul_t<INT>(dmul_t<INT>(0.86092628, q, bad), iT, bad);
   } else {
     r = 1.21;
     dr = 0.0;
   }
-  const double ne = b.nH * r, dne = b.nH * dr;
-  const double comp_heat = 8.9e-36 * b.xi * b.tx;
-  const double comp_cool = 8.9e-36 * b.xi * (4.0 * T), dcomp_cool = 8.9e-36 * b.xi * 4.0;
-  const double xray_heat = 1.5e-21 * b.sqsqxi * rT, dxray_heat = -0.5 * xray_heat * iT;
-  const double l1 = 1e-16 * fm::exp(-1.3e5 * iT) * b.isqxi * iT;
-  const double dl1 = l1 * (1.3e5 * iT - 1.0) * iT;
-  const double m1 = 5e-27 * sqT, m2 = 1.5e-17 * iT;
+  const double ne = dmul_t<INT>(b.nH, r, bad), dne = dmul_t<INT>(b.nH, dr, bad);
+  const double cxi = dmul_t<INT>(8.9e-36, b.xi, bad);
+  const double comp_heat = dmul_t<INT>(cxi, b.tx, bad);
+  const double comp_cool = dmul_t<INT>(cxi, dquad_t<INT>(T, bad), bad);
+  const double dcomp_cool = dquad_t<INT>(cxi, bad);
+  const double xray_heat = dmul_t<INT>(dmul_t<INT>(1.5e-21, b.sqsqxi, bad), rT, bad);
+  const double dxray_heat = dmul_t<INT>(-dhalf_t<INT>(xray_heat, bad), iT, bad);
+  const double l1 = dmul_t<INT>(
+      dmul_t<INT>(dmul_t<INT>(1e-16, fm::exp(dmul_t<INT>(-1.3e5, iT, bad)), bad), b.isqxi, bad),
+      iT, bad);
+  const double dl1 = dmul_t<INT>(dmul_t<INT>(l1, fma(1.3e5, iT, -1.0), bad), iT, bad);
+  const double m1 = dmul_t<INT>(5e-27, sqT, bad), m2 = dmul_t<INT>(1.5e-17, iT, bad);
   double l2, dl2;
   if (1e-24 <= m1 && 1e-24 <= m2) {
     l2 = 1e-24;
     dl2 = 0.0;
   } else if (m1 <= m2) {
     l2 = m1;
-    dl2 = 0.5 * m1 * iT;
+    dl2 = dmul_t<INT>(dhalf_t<INT>(m1, bad), iT, bad);
   } else {
     l2 = m2;
-    dl2 = -m2 * iT;
+    dl2 = -dmul_t<INT>(m2, iT, bad);
   }
-  const double brem_cool = 3.3e-27 * sqT, dbrem_cool = 0.5 * brem_cool * iT;
+  const double brem_cool = dmul_t<INT>(3.3e-27, sqT, bad);
+  const double dbrem_cool = dmul_t<INT>(dhalf_t<INT>(brem_cool, bad), iT, bad);
   const double net = comp_heat - comp_cool - (l1 + l2) - brem_cool;
   const double dnet = -dcomp_cool - (dl1 + dl2) - dbrem_cool;
-  dhc = b.nH * (dne * net + ne * dnet + b.nH * dxray_heat);
-  return b.nH * (ne * net + b.nH * xray_heat);
+  dhc = dmul_t<INT>(b.nH, fma(b.nH, dxray_heat, fma(ne, dnet, dmul_t<INT>(dne, net, bad))), bad);
+  return dmul_t<INT>(b.nH, fma(b.nH, xray_heat, dmul_t<INT>(ne, net, bad)), bad);
+}
+__device__ __forceinline__ double sg_heatcool_d(const SgCtx &b, double T, double &dhc)
+{
+  bool bad = false;
+  return sg_heatcool_d_t<false>(b, T, dhc, bad);
 }
 
 // z(T) = T n kB / (2/3) - E - dt (hc(T_old) + hc(T)) / 2 (cooling.c:233-237)
@@ -357,17 +372,26 @@ __device__ __forceinline__ int sg_judge_final(const SgCtx &b, double T, double T
   return SG_ACCEPT;
 }
 
-__device__ __forceinline__ int sg_judge_first(SgCtx &b, double T, double &z, double &dz,
-                                              double &T_f)
+// (the first rate evaluation with its products by dmul_t<INT>: on the
+// integer pipes with INT, the same bits either way)
+template <bool INT>
+__device__ __forceinline__ int sg_judge_first_t(SgCtx &b, double T, double &z, double &dz,
+                                                double &T_f, bool &bad)
 {
   const double cth = b.n * kKB * 1.5;
   double dhc;
-  b.hc_init = sg_heatcool_d(b, T, dhc);
+  b.hc_init = sg_heatcool_d_t<INT>(b, T, dhc, bad);
   z = T * cth - b.E - b.dt * b.hc_init;
   dz = cth - b.dt * dhc * 0.5;
   if (!(fabs(z) <= kSgResidual * T * cth)) return SG_PENDING;
   int evals = 1;   // hc at T is hc_init: no sign change, no further evaluation
   return sg_judge_final(b, T, T, z, dz, b.hc_init, T_f, evals);
+}
+__device__ __forceinline__ int sg_judge_first(SgCtx &b, double T, double &z, double &dz,
+                                              double &T_f)
+{
+  bool bad = false;
+  return sg_judge_first_t<false>(b, T, z, dz, T_f, bad);
 }
 
 // evals counts the evaluation of sg_judge_first

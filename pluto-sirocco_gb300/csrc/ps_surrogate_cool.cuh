@@ -182,7 +182,9 @@ __device__ __forceinline__ void sg_cool_items(const SgNet &net, const SgBox &bx,
       b.isqxi = rsqrt(b.xi);
       b.sqsqxi = rsqrt(b.isqxi);
       evals = 1;
-      st = sg_judge_first(b, T, z, dz, T_f);
+      bool bad = false;
+      st = sg_judge_first_t<true>(b, T, z, dz, T_f, bad);
+      if (bad) st = sg_judge_first_t<false>(b, T, z, dz, T_f, bad);
       stiff = st == SG_PENDING;
     } else if (kind == 1) {
       st = SG_OUT_OF_BOX;
