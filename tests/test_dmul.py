@@ -38,3 +38,40 @@ def test_integer_product_matches_gpu_multiply(built):
     mism, bad, first = _check(1, 23, n)
     assert mism == 0, f"first differing pair {first[0]:016x} {first[1]:016x}"
     assert 0.05 * n < bad < 0.4 * n
+
+
+@pytest.mark.gpu
+def test_subnormal_state_takes_the_fp64_path_and_matches_oracle(built):
+    """Subnormal velocities planted in a fifth of a 64x32 wind's cells make
+    the integer products of the stage kernel hand back in the cells that
+    read them, which are done again on the FP64 unit; after 10 steps the
+    run is within 1e-11 of the oracle started from the same state (the
+    planted values change the run: it differs from the unplanted one)."""
+    import numpy as np
+    import psgb
+    from conftest import assert_hydro_close
+    from oracle import wind_oracle
+    nr, nt, ng = 64, 32, 2
+    cfg = psgb.make_wind_config(nr, nt, cooling=0)
+    w = psgb.make_wind(line_force=0)
+    g = psgb.WindGrid(cfg)
+    V = psgb.wind_state(cfg, w, g)
+    act = V[:, 0, ng:-ng, ng:-ng].copy()
+    rng = np.random.default_rng(3)
+    mask = rng.random(act.shape[1:]) < 0.2
+    act[2][mask] = np.where(rng.random(mask.sum()) < 0.5, -3e-310, 3e-310)
+    act[3][mask] = np.where(rng.random(mask.sum()) < 0.5, -1e-315, 7e-312)
+    V[:, 0, ng:-ng, ng:-ng] = act
+    runs = {}
+    for name, state in (("planted", V), ("plain", psgb.wind_state(cfg, w, g))):
+        s = psgb.Solver(cfg, g)
+        s.set_state(state)
+        s.set_time(0.0, 1e-4, 0)
+        s.set_wind(w, None)
+        assert s.run(10) & ~0x2 == 0
+        runs[name] = s.get_state()[:6, 0, ng:-ng, ng:-ng]
+    o = wind_oracle(nr, nt, cooling=0, line_force=0, initial=act)
+    o.run(10)
+    r = assert_hydro_close(runs["planted"], np.asarray(o.active()), "planted subnormals")
+    print("relative L1 per variable against the oracle", r)
+    assert not np.array_equal(runs["planted"], runs["plain"])
