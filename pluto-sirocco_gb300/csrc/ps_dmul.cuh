@@ -115,6 +115,28 @@ __host__ __device__ __forceinline__ double dquad_int(double x, bool &bad)
   bad = bad | (!z && e - 1u >= 2044u);
   return z ? x : dm_double(X + (2ull << 52));
 }
+// 2 x, exact when x and the result are normal
+__host__ __device__ __forceinline__ double dtwice_int(double x, bool &bad)
+{
+  const uint64_t X = dm_bits(x);
+  const uint32_t e = (uint32_t)(X >> 52) & 0x7ffu;
+  const bool z = (X << 1) == 0u;
+  bad = bad | (!z && e - 1u >= 2045u);
+  return z ? x : dm_double(X + (1ull << 52));
+}
+// a b > 0 without the product: both nonzero with one sign, and (unless
+// `bad` is set) both normal with a product far above the underflow
+// threshold (biased exponents summing to at least 1026, the product at
+// least 2^-1020), so that the rounded product is positive exactly when the
+// signs agree
+__host__ __device__ __forceinline__ bool dposprod_int(double a, double b, bool &bad)
+{
+  const uint64_t A = dm_bits(a), B = dm_bits(b);
+  const uint32_t ea = (uint32_t)(A >> 52) & 0x7ffu, eb = (uint32_t)(B >> 52) & 0x7ffu;
+  const bool z = (A << 1) == 0u || (B << 1) == 0u;
+  bad = bad | (!z && (ea - 1u >= 2046u || eb - 1u >= 2046u || ea + eb < 1026u));
+  return !z && ((A ^ B) >> 63) == 0u;
+}
 
 #ifdef __CUDACC__
 // The product on the integer pipes (INT) or on the FP64 unit.  The hardware

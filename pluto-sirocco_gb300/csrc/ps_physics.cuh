@@ -103,6 +103,35 @@ __device__ __forceinline__ double limited_slope(double dvp, double dvm)
   }
 }
 
+// |a| < |b| ? a : b on the bit patterns, for a and b that are not NaN
+__device__ __forceinline__ double abs_min_nn(double a, double b)
+{
+  return (dm_bits(a) << 1) < (dm_bits(b) << 1) ? a : b;
+}
+
+// limited_slope with INT: the sign test without the product (dposprod_int),
+// the factors 1/2 and 2 as exponent shifts, the magnitude compares on the
+// bit patterns (no NaN past the sign test), the van Leer product by
+// dmul_int; the same value as limited_slope unless `bad` is set
+template <int LIM, bool INT>
+__device__ __forceinline__ double limited_slope_t(double dvp, double dvm, bool &bad)
+{
+  if constexpr (!INT) {
+    return limited_slope<LIM>(dvp, dvm);
+  } else {
+    if (!dposprod_int(dvp, dvm, bad)) return 0.0;
+    if constexpr (LIM == LIM_MC) {
+      const double qc = dhalf_int(dvm + dvp, bad);
+      const double scrh = dtwice_int(abs_min_nn(dvp, dvm), bad);
+      return abs_min_nn(qc, scrh);
+    } else if constexpr (LIM == LIM_VL) {
+      return dmul_int(dtwice_int(dvp, bad), dvm, bad) / (dvp + dvm);
+    } else {
+      return abs_min_nn(dvp, dvm);
+    }
+  }
+}
+
 // The products no add absorbs by dmul_t<INT> (ps_dmul.cuh): on the integer
 // pipes with INT, the same bits either way.
 template <int NV, bool INT>
@@ -200,9 +229,8 @@ __device__ __forceinline__ unsigned cons_to_prim(double (&u)[NV], double (&v)[NV
 // USE_PRS_GRADIENT), the interface pressure and cmax = max(|SL|, |SR|).
 // `hll`: HLLC takes the HLL flux at this interface (FLAG_HLL on either
 // side with SHOCK_FLATTENING MULTID, Src/HD/hllc.c:93-104).
-// The HLL branches and the supersonic ones with their products by
-// dmul_t<INT> (on the integer pipes with INT, the same bits either way);
-// the HLLC branch on the FP64 unit.
+// The products no add absorbs by dmul_t<INT> (on the integer pipes with
+// INT, the same bits either way).
 template <int NV, int SOLVER, int VN, bool INT>
 __device__ __forceinline__ void riemann_t(const double (&vL)[NV], const double (&vR)[NV],
                                           double gam, double igmm1, double (&f)[NV],
@@ -264,12 +292,12 @@ __device__ __forceinline__ void riemann_t(const double (&vL)[NV], const double (
   } else {
     // HLLC: only the star state on the side selected by the contact speed
     // is formed; the reference forms both and discards one.
-    prim_to_cons_t<NV, false>(vL, uL, igmm1, bad);
-    prim_to_cons_t<NV, false>(vR, uR, igmm1, bad);
-    const double qL = vL[PRS] + uL[VN] * (vL[VN] - SL);
-    const double qR = vR[PRS] + uR[VN] * (vR[VN] - SR);
-    const double wL = vL[RHO] * (vL[VN] - SL);
-    const double wR = vR[RHO] * (vR[VN] - SR);
+    prim_to_cons_t<NV, INT>(vL, uL, igmm1, bad);
+    prim_to_cons_t<NV, INT>(vR, uR, igmm1, bad);
+    const double qL = fma(uL[VN], vL[VN] - SL, vL[PRS]);
+    const double qR = fma(uR[VN], vR[VN] - SR, vR[PRS]);
+    const double wL = dmul_t<INT>(vL[RHO], vL[VN] - SL, bad);
+    const double wR = dmul_t<INT>(vR[RHO], vR[VN] - SR, bad);
     const double vs = (qR - qL) / (wR - wL);
     const bool left = vs >= 0.0;
     const double S = left ? SL : SR;
@@ -282,18 +310,19 @@ __device__ __forceinline__ void riemann_t(const double (&vL)[NV], const double (
     }
     double fs[NFLX];
     fs[RHO] = u[VN];
-    fs[VX1] = u[VX1] * v[VN];
-    fs[VX2] = u[VX2] * v[VN];
-    fs[VX3] = u[VX3] * v[VN];
-    fs[PRS] = (u[PRS] + v[PRS]) * v[VN];
+    fs[VX1] = dmul_t<INT>(u[VX1], v[VN], bad);
+    fs[VX2] = dmul_t<INT>(u[VX2], v[VN], bad);
+    fs[VX3] = dmul_t<INT>(u[VX3], v[VN], bad);
+    fs[PRS] = dmul_t<INT>(u[PRS] + v[PRS], v[VN], bad);
     double us[NFLX];
-    us[RHO] = u[RHO] * (S - vx) / (S - vs);
+    us[RHO] = dmul_t<INT>(u[RHO], S - vx, bad) / (S - vs);
 #pragma unroll
-    for (int nv = VX1; nv <= VX3; nv++) us[nv] = (nv == VN) ? us[RHO] * vs : us[RHO] * v[nv];
-    us[PRS] = u[PRS] / v[RHO] + (vs - vx) * (vs + v[PRS] / (v[RHO] * (S - vx)));
-    us[PRS] *= us[RHO];
+    for (int nv = VX1; nv <= VX3; nv++)
+      us[nv] = dmul_t<INT>(us[RHO], nv == VN ? vs : v[nv], bad);
+    us[PRS] = fma(vs - vx, vs + v[PRS] / dmul_t<INT>(v[RHO], S - vx, bad), u[PRS] / v[RHO]);
+    us[PRS] = dmul_t<INT>(us[PRS], us[RHO], bad);
 #pragma unroll
-    for (int nv = 0; nv < NFLX; nv++) f[nv] = fs[nv] + S * (us[nv] - u[nv]);
+    for (int nv = 0; nv < NFLX; nv++) f[nv] = fma(S, us[nv] - u[nv], fs[nv]);
     pr = v[PRS];
   }
   if constexpr (NV > NFLX) {

@@ -157,6 +157,53 @@ __global__ void k_fill_ghosts(double *V, const Params p)
   }
 }
 
+// The Cartesian stage kernels whose products no add absorbs run on the
+// integer pipes (ps_dmul.cuh, the same bits as the FP64 unit's): the
+// 5-variable set of the blast and the cooling cube.
+template <int NV>
+constexpr bool kIntProductsCart = NV == NFLX;
+
+// PLM of one cell along one direction on the uniform grid: + and - states
+// of all variables (limited_slope_t<LIM, INT>; a cell whose operands leave
+// the integer forms' range is done again with INT = false, the same bits)
+template <int NV, int LIM, bool INT, class G>
+__device__ __forceinline__ void plm_cart_cell(const double *__restrict__ sv,
+                                              double *__restrict__ svp,
+                                              double *__restrict__ svm, int s0, int sst, int q,
+                                              bool &bad)
+{
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    const double vm1 = sv[nv * G::VS + s0 - sst], v0 = sv[nv * G::VS + s0],
+                 vp1 = sv[nv * G::VS + s0 + sst];
+    const double dvp = vp1 - v0, dvm = v0 - vm1;
+    const double dv = limited_slope_t<LIM, INT>(dvp, dvm, bad);
+    svp[nv * G::NPMAX + q] = v0 + dv * 0.5;
+    svm[nv * G::NPMAX + q] = v0 - dv * 0.5;
+  }
+}
+
+// The end of a stage for one own cell: with STAGE 2 the RK2 average
+// U = U0 / 2 + U / 2 with U0 from V^n (halvings are exact, so this is the
+// reference's 0.5 U0 + 0.5 U); then ConsToPrim.  U holds the stage's
+// conserved state on entry and the (repaired) state on return.  Products
+// by dmul_t<INT> (ps_dmul.cuh).
+template <int NV, int STAGE, bool INT>
+__device__ __forceinline__ unsigned stage_out(double (&U)[NV], double (&v)[NV],
+                                              const StageArgs &a, const Params &p,
+                                              long long cell, int ent, bool &bad)
+{
+  if constexpr (STAGE == 2) {
+    double v0[NV], U0[NV];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
+    prim_to_cons_t<NV, INT>(v0, U0, p.igmm1, bad);
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) U[nv] = dhalf_t<INT>(U0[nv], bad) + dhalf_t<INT>(U[nv], bad);
+  }
+  return cons_to_prim_t<NV, INT>(U, v, p.gmm1, ent, bad);
+}
+
 // One direction of the unsplit update on the tile held in shared memory.
 template <int D, int NV, int LIM, int SOLVER, class TL>
 __device__ __forceinline__ void sweep(const double *__restrict__ sv, double *__restrict__ svp,
@@ -171,6 +218,7 @@ __device__ __forceinline__ void sweep(const double *__restrict__ sv, double *__r
   constexpr int NP = PX * PY * PZ, NF = FX * FY * FZ;
   constexpr int SST = D == 0 ? 1 : (D == 1 ? G::SX : G::SX * G::SY);  // smem stride along D
   constexpr int VN = VX1 + D;
+  constexpr bool IP = kIntProductsCart<NV>;
   const double gam = a.p.gamma;
 
   // (1) PLM: + and - states of cells -1 .. T_D along D
@@ -179,15 +227,9 @@ __device__ __forceinline__ void sweep(const double *__restrict__ sv, double *__r
     const int sx = ix + TL::HX - (D == 0), sy = iy + TL::HY - (D == 1),
               sz = iz + TL::HZ - (D == 2);
     const int s0 = (sz * G::SY + sy) * G::SX + sx;
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      const double vm1 = sv[nv * G::VS + s0 - SST], v0 = sv[nv * G::VS + s0],
-                   vp1 = sv[nv * G::VS + s0 + SST];
-      const double dvp = vp1 - v0, dvm = v0 - vm1;
-      const double dv = limited_slope<LIM>(dvp, dvm);
-      svp[nv * G::NPMAX + q] = v0 + dv * 0.5;
-      svm[nv * G::NPMAX + q] = v0 - dv * 0.5;
-    }
+    bool bad = false;
+    plm_cart_cell<NV, LIM, IP, G>(sv, svp, svm, s0, SST, q, bad);
+    if (IP && bad) plm_cart_cell<NV, LIM, false, G>(sv, svp, svm, s0, SST, q, bad);
   }
   __syncthreads();
 
@@ -205,7 +247,11 @@ __device__ __forceinline__ void sweep(const double *__restrict__ sv, double *__r
       vL[nv] = svp[nv * G::NPMAX + pl];
       vR[nv] = svm[nv * G::NPMAX + pr_];
     }
-    riemann<NV, SOLVER, VN>(vL, vR, gam, a.p.igmm1, f, pr, cm);
+    bool bad = false;
+    riemann_t<NV, SOLVER, VN, IP>(vL, vR, gam, a.p.igmm1, f, pr, cm, false, bad);
+    if constexpr (IP) {
+      if (bad) riemann_t<NV, SOLVER, VN, false>(vL, vR, gam, a.p.igmm1, f, pr, cm, false, bad);
+    }
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) sf[nv * G::NFMAX + q] = f[nv];
     spr[q] = pr;
@@ -219,13 +265,28 @@ __device__ __forceinline__ void sweep(const double *__restrict__ sv, double *__r
     constexpr int FST = D == 0 ? 1 : (D == 1 ? FX : FX * FY);
     const int qr = ql + FST;
     const double scrh = a.dtdx[D][gcell];
+    double rhs[NV];
+    bool bad = !IP;
+    if constexpr (IP) {
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      double rhs = -scrh * (sf[nv * G::NFMAX + qr] - sf[nv * G::NFMAX + ql]);
-      if (nv == VN) rhs -= scrh * (spr[qr] - spr[ql]);
-      U[nv] += rhs;
+      for (int nv = 0; nv < NV; nv++)
+        rhs[nv] = -dmul_int(scrh, sf[nv * G::NFMAX + qr] - sf[nv * G::NFMAX + ql], bad);
     }
-    if (stage1) cdt += 0.5 * (scm[ql] + scm[qr]) * a.inv_dx[D][gcell];
+    if (bad) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++)
+        rhs[nv] = -__dmul_rn(scrh, sf[nv * G::NFMAX + qr] - sf[nv * G::NFMAX + ql]);
+    }
+    rhs[VN] = fma(-scrh, spr[qr] - spr[ql], rhs[VN]);
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) U[nv] += rhs[nv];
+    if (stage1) {
+      bool badc = !IP;
+      double h = 0.0;
+      if constexpr (IP) h = dhalf_int(scm[ql] + scm[qr], badc);
+      if (badc) h = 0.5 * (scm[ql] + scm[qr]);
+      cdt = fma(h, a.inv_dx[D][gcell], cdt);
+    }
   }
   __syncthreads();
 }
@@ -279,6 +340,7 @@ __global__ void __launch_bounds__(TileGeom<TileT<DIMS>>::NT)
   const int gi = p.beg[0] + ox + cx, gj = p.beg[1] + oy + cy, gk = p.beg[2] + oz + cz;
   const long long cell = ((long long)gk * p.ntot[1] + gj) * p.px + gi;
 
+  constexpr bool IP = kIntProductsCart<NV>;
   double U[NV];
   double cdt = 0.0;
   if (own) {
@@ -287,7 +349,9 @@ __global__ void __launch_bounds__(TileGeom<TileT<DIMS>>::NT)
       const int s0 = ((cz + TL::HZ) * G::SY + cy + TL::HY) * G::SX + cx + TL::HX;
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v[nv] = sv[nv * G::VS + s0];
-      prim_to_cons<NV>(v, U, p.igmm1);
+      bool bad = false;
+      prim_to_cons_t<NV, IP>(v, U, p.igmm1, bad);
+      if (IP && bad) prim_to_cons_t<NV, false>(v, U, p.igmm1, bad);
     } else {
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) U[nv] = a.Us[nv * p.vstride + cell];
@@ -304,17 +368,22 @@ __global__ void __launch_bounds__(TileGeom<TileT<DIMS>>::NT)
 
   unsigned flags = 0;
   if (own) {
-    double v[NV];
-    if constexpr (STAGE == 2) {
-      // U^{n+1} = 1/2 U0 + 1/2 (U* + dt L(V*)), U0 = PrimToCons(V^n)
-      double v0[NV], U0[NV];
+    // U^{n+1} = 1/2 U0 + 1/2 (U* + dt L(V*)), U0 = PrimToCons(V^n), then
+    // the primitive state (the integer form first, again on the FP64 unit
+    // if it hands back)
+    double v[NV], Uw[NV];
+    bool bad = false;
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
-      prim_to_cons<NV>(v0, U0, p.igmm1);
+    for (int nv = 0; nv < NV; nv++) Uw[nv] = U[nv];
+    unsigned f = stage_out<NV, STAGE, IP>(Uw, v, a, p, cell, 0, bad);
+    if (IP && bad) {
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) U[nv] = 0.5 * U0[nv] + 0.5 * U[nv];
+      for (int nv = 0; nv < NV; nv++) Uw[nv] = U[nv];
+      f = stage_out<NV, STAGE, false>(Uw, v, a, p, cell, 0, bad);
     }
-    flags |= cons_to_prim<NV>(U, v, p.gmm1);
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) U[nv] = Uw[nv];
+    flags |= f;
 #pragma unroll
     for (int nv = 0; nv < NV; nv++)
       if (is_nan_bits(v[nv])) flags |= F_NAN;

@@ -890,26 +890,6 @@ __device__ __forceinline__ void vgrad_bin(const LineList &L, int e, double ids,
   dvds = dmul_t<INT>(fabs(v2 - v1), ids, bad);
 }
 
-// The end of a stage for one own cell: with STAGE 2 the RK2 average
-// U = U0 / 2 + U / 2 with U0 from V^n (halvings are exact, so this is the
-// reference's 0.5 U0 + 0.5 U); then ConsToPrim.  U holds the stage's
-// conserved state on entry and the (repaired) state on return.
-template <int NV, int STAGE, bool INT>
-__device__ __forceinline__ unsigned stage_out(double (&U)[NV], double (&v)[NV],
-                                              const StageArgs &a, const Params &p,
-                                              long long cell, int ent, bool &bad)
-{
-  if constexpr (STAGE == 2) {
-    double v0[NV], U0[NV];
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) v0[nv] = a.Vn[nv * p.vstride + cell];
-    prim_to_cons_t<NV, INT>(v0, U0, p.igmm1, bad);
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) U[nv] = dhalf_t<INT>(U0[nv], bad) + dhalf_t<INT>(U[nv], bad);
-  }
-  return cons_to_prim_t<NV, INT>(U, v, p.gmm1, ent, bad);
-}
-
 // One tile (bx, by) of one stage of one wind grid.
 template <int NV, int LIM, int SOLVER, int STAGE, class TL, bool CHAR>
 __device__ __forceinline__ void stage_sph_tile(const CUtensorMap *tm, const WindStageArgs &A,
