@@ -469,9 +469,11 @@ def _batch_e2e_parts(solvers, batch, V0s, steps, sg, psgb, k=E2E_PARTS):
     previous result before handing its states in again.  The parts start
     one after another on the first step, so that their transfers do not
     coincide.  With two parts both compute at once and then copy at once
-    (16.4 ms a step on the benchmark batch); with three 14.5 ms and with
-    four 14.2 ms, against 14.1 ms for the device-only step.  Tile shapes as
-    the autotuner chose for the whole batch; wall time."""
+    (16.4 ms a step on the benchmark batch against 14.1 ms device-only, in
+    an earlier build); in the current build four parts take 12.9 ms a step
+    against 12.2 ms device-only, six 12.8 ms and eight 13.1 ms (no gain past
+    four).  Tile shapes as the autotuner chose for the whole batch; wall
+    time."""
     import torch
     order = sorted(range(len(solvers)), key=lambda m: -V0s[m].size)
     groups = [order[i::k] for i in range(k)]
