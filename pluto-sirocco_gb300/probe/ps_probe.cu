@@ -180,12 +180,18 @@ __global__ void k_dmul_check(uint64_t seed, long long n, unsigned long long *cnt
     uint64_t A, B;
     dm_pair(seed, i, A, B);
     const double a = dm_double(A), b = dm_double(B);
-    bool bad = false, bh = false, bq = false;
+    bool bad = false, bh = false, bq = false, bt = false, b4 = false, bp = false;
     const double r = dmul_int(a, b, bad);
     const double h = dpow2m_int<1>(a, bh), qt = dpow2m_int<2>(a, bq);
-    const bool off = (!bad && dm_bits(r) != dm_bits(__dmul_rn(a, b))) ||
+    const double tw = dtwice_int(a, bt), x4 = dquad_int(a, b4);
+    const bool pos = dposprod_int(a, b, bp);
+    const double pr = __dmul_rn(a, b);
+    const bool off = (!bad && dm_bits(r) != dm_bits(pr)) ||
                      (!bh && dm_bits(h) != dm_bits(__dmul_rn(a, 0.5))) ||
-                     (!bq && dm_bits(qt) != dm_bits(__dmul_rn(a, 0.25)));
+                     (!bq && dm_bits(qt) != dm_bits(__dmul_rn(a, 0.25))) ||
+                     (!bt && dm_bits(tw) != dm_bits(__dmul_rn(a, 2.0))) ||
+                     (!b4 && dm_bits(x4) != dm_bits(__dmul_rn(a, 4.0))) ||
+                     (!bp && pos != (pr > 0.0));
     if (bad) nbad++;
     if (off) {
       if (atomicCAS(first + 2, 0ull, 1ull) == 0ull) {
@@ -243,9 +249,10 @@ extern "C" double ps_probe_dmul_rate(int emul, int blocks, int warps, int iters)
   return best;
 }
 
-// n operand pairs (dm_pair) through the integer product, and the first
-// operand through the exact halving and quartering, compared bit for bit
-// with the GPU's multiply (on_gpu 1) or the host's (on_gpu 0).  out[0]:
+// n operand pairs (dm_pair) through the integer product and the product's
+// sign test (dposprod_int), and the first operand through the exact
+// halving, quartering, doubling and quadrupling, compared bit for bit with
+// the GPU's multiply (on_gpu 1) or the host's (on_gpu 0).  out[0]:
 // pairs with a differing result, out[1]: products handed back (bad),
 // out[2..3]: the first differing pair's bit patterns.  Returns 0, or -1 on a bad argument or a
 // CUDA error.
@@ -260,13 +267,19 @@ extern "C" int ps_probe_dmul_check(int on_gpu, unsigned long long seed, long lon
       uint64_t A, B;
       ps::dm_pair(seed, i, A, B);
       const double a = ps::dm_double(A), b = ps::dm_double(B);
-      bool bad = false, bh = false, bq = false;
+      bool bad = false, bh = false, bq = false, bt = false, b4 = false, bp = false;
       const double r = ps::dmul_int(a, b, bad);
       const double h = ps::dpow2m_int<1>(a, bh), qt = ps::dpow2m_int<2>(a, bq);
-      const volatile double ref = a * b, rh = a * 0.5, rq = a * 0.25;
+      const double tw = ps::dtwice_int(a, bt), x4 = ps::dquad_int(a, b4);
+      const bool pos = ps::dposprod_int(a, b, bp);
+      const volatile double ref = a * b, rh = a * 0.5, rq = a * 0.25, rt = a * 2.0,
+                            r4 = a * 4.0;
       const bool off = (!bad && ps::dm_bits(r) != ps::dm_bits(ref)) ||
                        (!bh && ps::dm_bits(h) != ps::dm_bits(rh)) ||
-                       (!bq && ps::dm_bits(qt) != ps::dm_bits(rq));
+                       (!bq && ps::dm_bits(qt) != ps::dm_bits(rq)) ||
+                       (!bt && ps::dm_bits(tw) != ps::dm_bits(rt)) ||
+                       (!b4 && ps::dm_bits(x4) != ps::dm_bits(r4)) ||
+                       (!bp && pos != (ref > 0.0));
       if (bad) out[1]++;
       if (off) {
         if (!seen) {

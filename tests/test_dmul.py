@@ -1,6 +1,7 @@
 """The binary64 product on the integer pipes (csrc/ps_dmul.cuh) that the
-wind stage kernels use in place of the FP64 unit, and its exact halving
-and quartering, against the hardware multiply, bit for bit.
+stage kernels use in place of the FP64 unit, its exact scalings by 1/4,
+1/2, 2 and 4 and the product's sign test, against the hardware multiply,
+bit for bit.
 
 Five kinds of operand pairs (ps_probe.cu dm_pair): exponents near the
 middle of the range; short significands, whose products are exact or exact
