@@ -4,7 +4,8 @@
 // instruction every 16 cycles), while the integer multiply-add and logic
 // pipes take 64 to 128 lanes per cycle.  Kernels that are bound by the FP64
 // unit leave most issue slots idle; a product formed on the integer pipes
-// takes about forty of those slots in place of one FP64 slot.
+// takes about sixty of those slots (39 ALU, 19 multiply-add) in place of
+// one FP64 slot, and the two kinds of product overlap.
 //
 // dmul_int(a, b, bad) returns the IEEE 754 binary64 product of a and b
 // rounded to nearest, ties to even (IEEE 754-2019, 4.3.1), the same bit
@@ -22,8 +23,8 @@
 //     rounding carry out of it both landing in the exponent field.
 // Zeros give the signed zero.  For subnormal, infinite or NaN operands and
 // for products outside the normal range the result is not formed: `bad` is
-// set and the caller takes the hardware multiply for them (in the kernels,
-// for the whole warp, so that the results are the hardware's in every case).
+// set and the caller redoes that cell's phase with the hardware multiply
+// at the same places, so that the results are the hardware's in every case.
 #pragma once
 
 #include <stdint.h>
